@@ -1,0 +1,343 @@
+#!/usr/bin/env python
+"""Benchmark of the two-site effective-Hamiltonian matvec (src/apply.jl:93-105) at chi=2048.
+
+Workload: XXZ chain (Delta = 0.5) two-site tensor with chi = 2048 on both bonds over 25 charges
+with a binomial sector profile, d = 2, MPO bond 5, blocks N(0,1) from a seeded Philox stream
+(synthetic: the reference publishes no dataset).  One step = one H_eff application
+v -> envL . W1 . W2 . envR . v with every input resident in HBM.
+
+Metric: H_eff GFLOP/s = planner-counted algorithmic flops (sum over the sector GEMMs of the four
+contractions of 2*M*N*K) / seconds per step.  Every timed step is preceded by an L2 flush
+(a 512 MiB write on the library's stream) outside the timed events.
+
+    python bench.py [--steps K] [--warmup W] [--precision P] [--impl ours|reference]
+
+Multi-GPU (torchrun): one independent replica per rank (a DMRG chain does not shard), value =
+all ranks' flops / max-over-ranks time, "scaling": "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "H_eff matvec GFLOP/s at chi=2048 (2-site DMRG hot path)"
+UNIT = "GFLOP/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--chi", type=int, default=2048)
+    p.add_argument("--precision", type=int, default=None,
+                   help="0 = FP64; s >= 2 = split bf16 with s slices (default: best available)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------------------------
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+def profile_traffic(kernel_key):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        return json.load(open(path)).get(kernel_key)
+    except (OSError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------------------------
+def oracle_inputs(chi):
+    from mps_gb300 import dmrg as gd
+    from oracle import mps as om
+    from oracle import symtensors as st
+    (sv, sl, sr), flats = gd.heff_inputs_host(chi)
+    conv = lambda sp: tuple(st.VectorSpace(V.sectors, V.isdual) for V in sp)
+    O = [st.from_flat(0, conv(s), f) for s, f in zip((sv, sl, sr), flats)]
+    W = om.xxz_u1mpo(3, 0.5)[1]
+    return O + [W, W]
+
+
+def cpu_heff_rate(chi, flops, budget_s=15.0, max_reps=40):
+    """Oracle (NumPy/OpenBLAS restatement of the reference path) H_eff matvecs on the host
+    cores: repeated until ~budget_s of CPU work."""
+    from oracle import mps as om
+    O = oracle_inputs(chi)
+    om.applymps2site(*O)  # warm-up
+    times = []
+    t_all = time.perf_counter()
+    while len(times) < max_reps and time.perf_counter() - t_all < budget_s:
+        t0 = time.perf_counter()
+        om.applymps2site(*O)
+        times.append(time.perf_counter() - t0)
+    cores = int(os.environ.get("OPENBLAS_NUM_THREADS", os.cpu_count() or 1))
+    return flops / statistics.mean(times) / 1e9, len(times), statistics.mean(times), cores
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm's CPU path (the oracle restatement; Julia is not
+    available) timed on the host cores, same metric and workload."""
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", str(os.cpu_count() or 1))
+    from mps_gb300 import dmrg as gd
+    from oracle import mps as om
+    flops = gd.heff_flops_meta(*gd.heff_problem(args.chi, meta_only=True))
+    O = oracle_inputs(args.chi)
+    for _ in range(max(1, min(args.warmup, 2))):
+        om.applymps2site(*O)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        om.applymps2site(*O)
+        times.append(time.perf_counter() - t0)
+    t = statistics.mean(times)
+    value = flops / t / 1e9
+    cores = int(os.environ["OPENBLAS_NUM_THREADS"])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Philox N(0,1) blocks)",
+        "config": {"workload": f"H_eff matvec, XXZ Delta=0.5, chi={args.chi} on both bonds, "
+                               "25 charges binomial profile, d=2, MPO bond 5",
+                   "chi": args.chi},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full H_eff matvecs (NumPy/OpenBLAS oracle; "
+                                   "Julia is absent)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import mps_gb300 as mg
+    from mps_gb300 import dmrg as gd
+
+    ctx = mg.get_context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    prob = gd.heff_problem(args.chi, ctx=ctx)
+    flops = mg.applymps2site_flops(*prob)
+    precision = 0 if args.precision is None else args.precision
+    flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def timed_steps(k, with_kernel_timing=False):
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        ctx.set_timing(with_kernel_timing)
+        with torch.cuda.stream(stream):
+            for i in range(k):
+                flush.zero_()
+                starts[i].record(stream)
+                out = mg.applymps2site(*prob, precision=precision)
+                ends[i].record(stream)
+                del out
+        torch.cuda.synchronize()
+        ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        return ms
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            out = mg.applymps2site(*prob, precision=precision)
+            del out
+    barrier()
+    launches0, _ = ctx.counters()
+    with ClockSampler(local) as cs:
+        ms = timed_steps(args.steps)
+    launches = ctx.counters()[0] - launches0
+    clocks = cs.summary()
+    t_local = sum(ms) / len(ms) / 1e3
+    t = t_local
+    if ws > 1:
+        tt = torch.tensor([t_local], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    value = ws * flops / t / 1e9
+
+    # per-kernel CUDA-event times (second pass over the same steps)
+    timed_steps(args.steps, with_kernel_timing=True)
+    kinds = {k: ctx.kernel_time(k) for k in ("copy", "gemm_f64", "gemm_split", "pack")}
+    ctx.set_timing(False)
+
+    # end to end through the C ABI with host buffers: H2D of all five inputs, D2H of v'
+    host_in = [torch.from_numpy(x.to_flat()).pin_memory() for x in prob]
+    host_out = torch.empty(prob[0].numel(), dtype=torch.float64).pin_memory()
+    dev = [mg.zeros(x.charge, x.space, ctx) for x in prob]
+    h2d = sum(h.numel() * 8 for h in host_in)
+    d2h = host_out.numel() * 8
+    e2e_t = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for d, h in zip(dev, host_in):
+            mg._lib.call("mpsg_tensor_upload", d.handle,
+                         mg._lib.C.cast(h.data_ptr(), mg._lib.PF64), h.numel())
+        r = mg.applymps2site(*dev, precision=precision)
+        mg._lib.call("mpsg_tensor_download", r.handle,
+                     mg._lib.C.cast(host_out.data_ptr(), mg._lib.PF64), host_out.numel())
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_t.append(t1 - t0)
+        del r
+    e2e_value = ws * flops / statistics.mean(e2e_t) / 1e9
+
+    peaks = measured_peaks()
+    if precision == 0:
+        gem_ms, gem_n, gem_f = kinds["gemm_f64"]
+        # FP64 peak: cuBLAS DGEMM measured now on this GPU (the driver's peaks file has none)
+        a = torch.randn(8192, 8192, dtype=torch.float64, device=f"cuda:{local}")
+        torch.matmul(a, a)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            torch.matmul(a, a)
+        e1.record()
+        torch.cuda.synchronize()
+        peak = 3 * 2 * 8192 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
+        peak_src = "cuBLAS DGEMM 8192^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)"
+        del a
+        pipe = "fp64"
+        dtype = "f64"
+    else:
+        gem_ms, gem_n, gem_f = kinds["gemm_split"]
+        peak = peaks["bf16_tflops"] if peaks else 1900.0
+        peak_src = "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback 1.9 PFLOP/s"
+        pipe = "bf16-tensor"
+        dtype = f"bf16x{precision}-split (fp32 accumulate, f64 epilogue)"
+    # algorithmic flops of the timed GEMM launches / their summed CUDA-event durations
+    achieved = gem_f / (gem_ms / 1e3) / 1e12 if gem_n else None
+    roof = {"bound": "tensor", "pipe": pipe, "kernel": "grouped block GEMM (one launch per "
+            "contraction)", "launches_timed": gem_n,
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": (achieved / peak) if achieved else None, "peak_source": peak_src,
+            "traffic": profile_traffic(f"gemm_p{precision}_chi{args.chi}")}
+    step_ms = sum(ms) / len(ms)
+    share = {k: round(v[0] / args.steps / step_ms, 4) for k, v in kinds.items() if v[1]}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+        "data": "synthetic (seeded Philox N(0,1) blocks)",
+        "config": {"workload": f"H_eff matvec, XXZ Delta=0.5, chi={args.chi} on both bonds, "
+                               "25 charges binomial profile, d=2, MPO bond 5",
+                   "chi": args.chi, "precision": precision, "gflop_per_step": flops / 1e9,
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "flushed before every timed step (512 MiB write)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "kernel_share_of_step": share,
+        "roofline": roof,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline and ws == 1:
+        os.environ.setdefault("OPENBLAS_NUM_THREADS", str(os.cpu_count() or 1))
+        v, n, tm, cores = cpu_heff_rate(args.chi, flops)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{n} full H_eff matvecs of the same workload "
+                                          f"({tm:.2f} s each), NumPy/OpenBLAS oracle"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

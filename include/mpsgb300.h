@@ -1,0 +1,161 @@
+/* mpsgb300 — C ABI of the GB300 block-sparse U(1) tensor library.
+ *
+ * The entry points replace the SymTensors / TensorNetAlgs functions of amiragha/mps on the
+ * 2-site DMRG hot path.  Each declaration cites the reference routine it stands in for (paths
+ * relative to the reference project root).  A Julia `ccall` binding and a Python ctypes binding
+ * map these one to one.
+ *
+ * Conventions
+ *   - Every function returns an int status: 0 = success, otherwise one of MPSG_ERR_*;
+ *     mpsg_last_error() returns the message of the last failure on the calling thread.
+ *   - Leg positions are 1-based and contraction index tuples are ncon-style (negative labels are
+ *     contracted, positive labels give the output leg order), exactly as in the reference.
+ *   - A leg space is passed as parallel arrays: `nsect[l]` charges for leg l, then the charges
+ *     and dims of all legs concatenated, and `isdual[l]`.
+ *   - Tensor data crosses the boundary as one flat float64 array: blocks in reference sector order
+ *     (column-major sector order, last leg slowest, src/sector.jl:35-36), each block
+ *     column-major, blocks concatenated (mpsg_tensor_sectors gives the offsets).
+ *   - `precision` selects the block-GEMM arithmetic: 0 = FP64 (the plain drop-in);
+ *     s >= 2 = split precision with s bf16 slices per operand, FP32 accumulation in tensor memory
+ *     and an FP64 epilogue.
+ *   - All work is ordered on the context's CUDA stream; calls that return host values
+ *     synchronise that stream.
+ */
+#ifndef MPSGB300_H
+#define MPSGB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPSG_OK 0
+#define MPSG_ERR_ARGUMENT 1
+#define MPSG_ERR_SPACE_MISMATCH 2   /* reference: SpaceMismatch / SectorMismatch / error() */
+#define MPSG_ERR_CUDA 3
+#define MPSG_ERR_NO_CONVERGENCE 4
+#define MPSG_ERR_UNSUPPORTED 5
+#define MPSG_ERR_TOLERANCE 6        /* reference: "largest singular value is smaller than tol" */
+
+typedef struct mpsg_ctx mpsg_ctx;
+typedef struct mpsg_tensor mpsg_tensor;
+
+/* ---- library and context ---------------------------------------------------------------- */
+int mpsg_version(void);
+const char* mpsg_last_error(void);
+/* Context = one device + one CUDA stream + plan caches.  No reference counterpart (the
+ * reference is single-threaded host code, src/TensorNetAlgs.jl). */
+int mpsg_ctx_create(int device, mpsg_ctx** out);
+int mpsg_ctx_destroy(mpsg_ctx* ctx);
+int mpsg_ctx_synchronize(mpsg_ctx* ctx);
+/* Counters: kernels launched by this library and algorithmic block-GEMM flops issued. */
+int mpsg_ctx_counters(mpsg_ctx* ctx, int64_t* kernel_launches, double* gemm_flops);
+int mpsg_ctx_clear_caches(mpsg_ctx* ctx);
+/* The context's cudaStream_t, so callers can order their own work (or events) with it. */
+int mpsg_ctx_stream(mpsg_ctx* ctx, void** stream);
+/* Per-kernel CUDA-event timing: when enabled, every launch of kernel class `kind`
+ * (0 = block-permute copy, 1 = FP64 block GEMM, 2 = split-precision block GEMM,
+ *  3 = split-precision operand packing, 4 = vector ops) is bracketed by events on the context
+ * stream; mpsg_ctx_kernel_time synchronises and returns the summed milliseconds, launch
+ * count and algorithmic flops (GEMM classes) since the last reset. */
+int mpsg_ctx_set_timing(mpsg_ctx* ctx, int32_t enable);
+int mpsg_ctx_kernel_time(mpsg_ctx* ctx, int32_t kind, double* total_ms, int64_t* launches,
+                         double* flops);
+
+/* ---- tensors (src/symtensor.jl:12-30; constructors :132-191) ----------------------------- */
+/* Zero-filled tensor holding every allowed sector of (charge, space)  (fill, symtensor.jl:157). */
+int mpsg_tensor_create(mpsg_ctx* ctx, int32_t charge, int32_t nlegs, const int32_t* nsect,
+                       const int32_t* charges, const int64_t* dims, const int32_t* isdual,
+                       mpsg_tensor** out);
+int mpsg_tensor_free(mpsg_tensor* t);
+int mpsg_tensor_rank(const mpsg_tensor* t, int32_t* nlegs);
+int mpsg_tensor_charge(const mpsg_tensor* t, int32_t* charge);
+int mpsg_tensor_numel(const mpsg_tensor* t, int64_t* nblocks, int64_t* nelem);
+int mpsg_tensor_is_diagonal(const mpsg_tensor* t, int32_t* isdiag);
+/* Leg space `leg` (1-based): call once with charges=dims=NULL to get nsect. */
+int mpsg_tensor_space(const mpsg_tensor* t, int32_t leg, int32_t* nsect, int32_t* charges,
+                      int64_t* dims, int32_t* isdual);
+/* Sector labels [nblocks*nlegs], block sizes [nblocks*nlegs], offsets [nblocks] (any may be
+ * NULL).  Order = SortedDict order of the reference (src/sorteddict.jl:39-45). */
+int mpsg_tensor_sectors(const mpsg_tensor* t, int32_t* labels, int64_t* sizes, int64_t* offsets);
+int mpsg_tensor_upload(mpsg_tensor* t, const double* host, int64_t nelem);
+int mpsg_tensor_download(const mpsg_tensor* t, double* host, int64_t nelem);
+/* Raw device pointer of the flat buffer (for callers that keep data resident). */
+int mpsg_tensor_device_ptr(const mpsg_tensor* t, double** dptr);
+int mpsg_tensor_copy(mpsg_ctx* ctx, const mpsg_tensor* t, mpsg_tensor** out);
+/* dual(A): negated charge, flipped leg flags, same blocks (symtensor.jl:201-212). */
+int mpsg_dual(mpsg_ctx* ctx, const mpsg_tensor* a, mpsg_tensor** out);
+
+/* ---- releg (src/symreleg.jl) -------------------------------------------------------------- */
+int mpsg_permutelegs(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* perm,
+                     mpsg_tensor** out);                                   /* :34-51   */
+int mpsg_fuselegs(mpsg_ctx* ctx, const mpsg_tensor* a, int32_t l, int32_t n, int32_t dual,
+                  mpsg_tensor** out);                                      /* :79-146  */
+int mpsg_splitleg(mpsg_ctx* ctx, const mpsg_tensor* a, int32_t l, int32_t nspaces,
+                  const int32_t* nsect, const int32_t* charges, const int64_t* dims,
+                  const int32_t* isdual, mpsg_tensor** out);               /* :160-214 */
+
+/* ---- contraction (src/contract.jl) -------------------------------------------------------- */
+int mpsg_symmatrix(mpsg_ctx* ctx, const mpsg_tensor* a, int32_t nrows, const int32_t* rows,
+                   int32_t ncols, const int32_t* cols, mpsg_tensor** out); /* :112-171 */
+int mpsg_matmul(mpsg_ctx* ctx, const mpsg_tensor* a, const mpsg_tensor* b, int32_t precision,
+                mpsg_tensor** out);                                        /* :234-298 */
+/* contract(A, idxA, B, idxB) (:11-47).  When every leg is contracted the result is the scalar in
+ * *scalar and *out is set to NULL. */
+int mpsg_contract(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
+                  const int32_t* idxb, int32_t precision, mpsg_tensor** out, double* scalar);
+/* Algorithmic flops of contract(A, idxA, B, idxB) as planned (sum of 2*M*N*K over sectors). */
+int mpsg_contract_flops(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa,
+                        const mpsg_tensor* b, const int32_t* idxb, double* flops);
+
+/* ---- effective Hamiltonian and environments (src/apply.jl) -------------------------------- */
+int mpsg_applymps2site(mpsg_ctx* ctx, const mpsg_tensor* v, const mpsg_tensor* envl,
+                       const mpsg_tensor* envr, const mpsg_tensor* w1, const mpsg_tensor* w2,
+                       int32_t precision, mpsg_tensor** out);              /* :93-105 */
+int mpsg_applymps2site_flops(mpsg_ctx* ctx, const mpsg_tensor* v, const mpsg_tensor* envl,
+                             const mpsg_tensor* envr, const mpsg_tensor* w1,
+                             const mpsg_tensor* w2, double* flops);
+int mpsg_mpsupdateleft(mpsg_ctx* ctx, const mpsg_tensor* env, const mpsg_tensor* a,
+                       const mpsg_tensor* w, int32_t precision, mpsg_tensor** out); /* :49-58 */
+int mpsg_mpsupdateright(mpsg_ctx* ctx, const mpsg_tensor* env, const mpsg_tensor* a,
+                        const mpsg_tensor* w, int32_t precision, mpsg_tensor** out); /* :17-25 */
+
+/* ---- structure-only planning (no device memory; usable on hosts without a GPU) ---------- */
+/* A structure-only tensor carries charge, spaces and the sector table but no data; every
+ * mpsg_plan_* call returns the structure the matching operation would produce, computed by the
+ * same planner that drives the kernels.  Query them with mpsg_tensor_space/_sectors/_numel. */
+int mpsg_meta_create(int32_t charge, int32_t nlegs, const int32_t* nsect, const int32_t* charges,
+                     const int64_t* dims, const int32_t* isdual, mpsg_tensor** out);
+int mpsg_plan_permutelegs(const mpsg_tensor* a, const int32_t* perm, mpsg_tensor** out);
+int mpsg_plan_fuselegs(const mpsg_tensor* a, int32_t l, int32_t n, int32_t dual,
+                       mpsg_tensor** out);
+int mpsg_plan_splitleg(const mpsg_tensor* a, int32_t l, int32_t nspaces, const int32_t* nsect,
+                       const int32_t* charges, const int64_t* dims, const int32_t* isdual,
+                       mpsg_tensor** out);
+int mpsg_plan_symmatrix(const mpsg_tensor* a, int32_t nrows, const int32_t* rows, int32_t ncols,
+                        const int32_t* cols, mpsg_tensor** out);
+int mpsg_plan_matmul(const mpsg_tensor* a, const mpsg_tensor* b, mpsg_tensor** out,
+                     double* flops);
+/* *out is NULL for a full contraction (scalar result). */
+int mpsg_plan_contract(const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
+                       const int32_t* idxb, mpsg_tensor** out, double* flops);
+/* Number of copy tasks and GEMM tasks the planner emits for contract (diagnostics). */
+int mpsg_plan_contract_tasks(const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
+                             const int32_t* idxb, int64_t* copy_tasks, int64_t* gemm_tasks);
+
+/* ---- vector operations used by the Krylov solver (src/symtensor.jl:252-323) -------------- */
+int mpsg_fill(mpsg_ctx* ctx, mpsg_tensor* a, double x);                          /* :166-171 */
+int mpsg_rmul(mpsg_ctx* ctx, mpsg_tensor* a, double alpha);                      /* :280-285 */
+int mpsg_mul(mpsg_ctx* ctx, mpsg_tensor* b, const mpsg_tensor* a, double alpha); /* :268-276 */
+int mpsg_axpy(mpsg_ctx* ctx, double alpha, const mpsg_tensor* a, mpsg_tensor* b); /* :288-296 */
+int mpsg_axpby(mpsg_ctx* ctx, double alpha, const mpsg_tensor* a, double beta,
+               mpsg_tensor* b);                                                  /* :299-308 */
+int mpsg_dot(mpsg_ctx* ctx, const mpsg_tensor* a, const mpsg_tensor* b, double* out); /* :314 */
+int mpsg_norm(mpsg_ctx* ctx, const mpsg_tensor* a, double* out);                 /* :321-323 */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPSGB300_H */

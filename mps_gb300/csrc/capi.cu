@@ -1,0 +1,601 @@
+// C ABI (include/mpsgb300.h): contexts, device tensors, releg, contraction, the effective
+// Hamiltonian / environment updates and the Krylov vector operations.
+#include <cstring>
+#include <sstream>
+
+#include "../../include/mpsgb300.h"
+#include "ops.hpp"
+
+struct mpsg_ctx {
+  mpsg::Context c;
+};
+struct mpsg_tensor {
+  mpsg::DeviceTensor t;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    f();
+    return mpsg::kOk;
+  } catch (const mpsg::Error& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return mpsg::kErrArgument;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return mpsg::kErrArgument;
+  }
+}
+
+void need(const void* p, const char* what) {
+  if (!p) throw mpsg::Error(mpsg::kErrArgument, std::string("null argument: ") + what);
+}
+
+std::vector<mpsg::Space> parse_spaces(int32_t nlegs, const int32_t* nsect, const int32_t* charges,
+                                      const int64_t* dims, const int32_t* isdual) {
+  if (nlegs < 1 || nlegs > mpsg::kMaxLegs)
+    throw mpsg::Error(mpsg::kErrArgument, "number of legs out of range");
+  need(nsect, "nsect");
+  need(isdual, "isdual");
+  std::vector<mpsg::Space> sp;
+  int64_t p = 0;
+  for (int l = 0; l < nlegs; ++l) {
+    if (nsect[l] < 1) throw mpsg::Error(mpsg::kErrArgument, "a leg needs at least one charge");
+    need(charges, "charges");
+    need(dims, "dims");
+    std::vector<std::pair<int, int64_t>> pairs;
+    for (int k = 0; k < nsect[l]; ++k, ++p) pairs.push_back({charges[p], dims[p]});
+    sp.push_back(mpsg::Space::make(pairs, isdual[l] != 0));
+  }
+  return sp;
+}
+
+mpsg_tensor* wrap(mpsg::DeviceTensor&& t) {
+  auto* h = new mpsg_tensor;
+  h->t = std::move(t);
+  return h;
+}
+
+std::vector<int> ivec(const int32_t* p, int n) { return std::vector<int>(p, p + n); }
+
+}  // namespace
+
+extern "C" {
+
+int mpsg_version(void) { return 1; }
+
+const char* mpsg_last_error(void) { return g_last_error.c_str(); }
+
+int mpsg_ctx_create(int device, mpsg_ctx** out) {
+  return guarded([&] {
+    need(out, "out");
+    auto* h = new mpsg_ctx;
+    try {
+      mpsg::context_init(&h->c, device);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int mpsg_ctx_destroy(mpsg_ctx* ctx) {
+  return guarded([&] {
+    if (!ctx) return;
+    cudaStreamSynchronize(ctx->c.stream);
+    delete ctx;
+  });
+}
+
+int mpsg_ctx_synchronize(mpsg_ctx* ctx) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    MPSG_CUDA(cudaStreamSynchronize(ctx->c.stream));
+  });
+}
+
+int mpsg_ctx_counters(mpsg_ctx* ctx, int64_t* launches, double* flops) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    if (launches) *launches = ctx->c.kernel_launches;
+    if (flops) *flops = ctx->c.gemm_flops;
+  });
+}
+
+int mpsg_ctx_clear_caches(mpsg_ctx* ctx) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    MPSG_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    ctx->c.contract_cache.clear();
+    ctx->c.releg_cache.clear();
+    ctx->c.matmul_cache.clear();
+  });
+}
+
+int mpsg_ctx_stream(mpsg_ctx* ctx, void** stream) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(stream, "stream");
+    *stream = (void*)ctx->c.stream;
+  });
+}
+
+int mpsg_ctx_set_timing(mpsg_ctx* ctx, int32_t enable) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    mpsg::collect_kernel_times(&ctx->c);
+    ctx->c.timing = enable != 0;
+    for (int k = 0; k < mpsg::Context::kKinds; ++k) {
+      ctx->c.timed_ms[k] = 0;
+      ctx->c.timed_launches[k] = 0;
+      ctx->c.timed_flops[k] = 0;
+    }
+  });
+}
+
+int mpsg_ctx_kernel_time(mpsg_ctx* ctx, int32_t kind, double* total_ms, int64_t* launches,
+                         double* flops) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    if (kind < 0 || kind >= mpsg::Context::kKinds)
+      throw mpsg::Error(mpsg::kErrArgument, "kernel kind out of range");
+    mpsg::collect_kernel_times(&ctx->c);
+    if (total_ms) *total_ms = ctx->c.timed_ms[kind];
+    if (launches) *launches = ctx->c.timed_launches[kind];
+    if (flops) *flops = ctx->c.timed_flops[kind];
+  });
+}
+
+int mpsg_tensor_create(mpsg_ctx* ctx, int32_t charge, int32_t nlegs, const int32_t* nsect,
+                       const int32_t* charges, const int64_t* dims, const int32_t* isdual,
+                       mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(out, "out");
+    auto sp = parse_spaces(nlegs, nsect, charges, dims, isdual);
+    auto meta = mpsg::TensorMeta::build(charge, sp);
+    *out = wrap(mpsg::new_tensor(&ctx->c, meta, /*zero=*/true));
+  });
+}
+
+int mpsg_tensor_free(mpsg_tensor* t) {
+  return guarded([&] { delete t; });
+}
+
+int mpsg_tensor_rank(const mpsg_tensor* t, int32_t* n) {
+  return guarded([&] {
+    need(t, "t");
+    need(n, "n");
+    *n = t->t.meta.N();
+  });
+}
+
+int mpsg_tensor_charge(const mpsg_tensor* t, int32_t* c) {
+  return guarded([&] {
+    need(t, "t");
+    need(c, "c");
+    *c = t->t.meta.charge;
+  });
+}
+
+int mpsg_tensor_numel(const mpsg_tensor* t, int64_t* nb, int64_t* ne) {
+  return guarded([&] {
+    need(t, "t");
+    if (nb) *nb = (int64_t)t->t.meta.nblocks();
+    if (ne) *ne = t->t.meta.total;
+  });
+}
+
+int mpsg_tensor_is_diagonal(const mpsg_tensor* t, int32_t* d) {
+  return guarded([&] {
+    need(t, "t");
+    need(d, "d");
+    *d = t->t.diag ? 1 : 0;
+  });
+}
+
+int mpsg_tensor_space(const mpsg_tensor* t, int32_t leg, int32_t* nsect, int32_t* charges,
+                      int64_t* dims, int32_t* isdual) {
+  return guarded([&] {
+    need(t, "t");
+    if (leg < 1 || leg > t->t.meta.N()) throw mpsg::Error(mpsg::kErrArgument, "leg out of range");
+    const mpsg::Space& V = t->t.meta.space[leg - 1];
+    if (nsect) *nsect = V.size();
+    if (isdual) *isdual = V.dual ? 1 : 0;
+    for (int i = 0; i < V.size(); ++i) {
+      if (charges) charges[i] = V.ch[i];
+      if (dims) dims[i] = V.dm[i];
+    }
+  });
+}
+
+int mpsg_tensor_sectors(const mpsg_tensor* t, int32_t* labels, int64_t* sizes, int64_t* offsets) {
+  return guarded([&] {
+    need(t, "t");
+    const auto& m = t->t.meta;
+    if (labels)
+      for (size_t i = 0; i < m.sec.lab.size(); ++i) labels[i] = m.sec.lab[i];
+    if (sizes) std::memcpy(sizes, m.sec.sz.data(), sizeof(int64_t) * m.sec.sz.size());
+    if (offsets) std::memcpy(offsets, m.off.data(), sizeof(int64_t) * m.off.size());
+  });
+}
+
+int mpsg_tensor_upload(mpsg_tensor* t, const double* host, int64_t n) {
+  return guarded([&] {
+    need(t, "t");
+    if (n != t->t.meta.total) throw mpsg::Error(mpsg::kErrArgument, "upload: size mismatch");
+    if (n == 0) return;
+    need(host, "host");
+    MPSG_CUDA(cudaMemcpyAsync(t->t.data(), host, sizeof(double) * n, cudaMemcpyHostToDevice,
+                              t->t.ctx->stream));
+    MPSG_CUDA(cudaStreamSynchronize(t->t.ctx->stream));
+  });
+}
+
+int mpsg_tensor_download(const mpsg_tensor* t, double* host, int64_t n) {
+  return guarded([&] {
+    need(t, "t");
+    if (n != t->t.meta.total) throw mpsg::Error(mpsg::kErrArgument, "download: size mismatch");
+    if (n == 0) return;
+    need(host, "host");
+    MPSG_CUDA(cudaMemcpyAsync(host, t->t.data(), sizeof(double) * n, cudaMemcpyDeviceToHost,
+                              t->t.ctx->stream));
+    MPSG_CUDA(cudaStreamSynchronize(t->t.ctx->stream));
+  });
+}
+
+int mpsg_tensor_device_ptr(const mpsg_tensor* t, double** p) {
+  return guarded([&] {
+    need(t, "t");
+    need(p, "p");
+    *p = t->t.data();
+  });
+}
+
+int mpsg_tensor_copy(mpsg_ctx* ctx, const mpsg_tensor* t, mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(t, "t");
+    need(out, "out");
+    *out = wrap(mpsg::copy_tensor(&ctx->c, t->t));
+  });
+}
+
+int mpsg_dual(mpsg_ctx* ctx, const mpsg_tensor* a, mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(out, "out");
+    *out = wrap(mpsg::dual_view(a->t));
+  });
+}
+
+int mpsg_permutelegs(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* perm,
+                     mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(perm, "perm");
+    need(out, "out");
+    *out = wrap(mpsg::permutelegs(&ctx->c, a->t, ivec(perm, a->t.meta.N())));
+  });
+}
+
+int mpsg_fuselegs(mpsg_ctx* ctx, const mpsg_tensor* a, int32_t l, int32_t n, int32_t dual,
+                  mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(out, "out");
+    *out = wrap(mpsg::fuselegs(&ctx->c, a->t, l, n, dual != 0));
+  });
+}
+
+int mpsg_splitleg(mpsg_ctx* ctx, const mpsg_tensor* a, int32_t l, int32_t nspaces,
+                  const int32_t* nsect, const int32_t* charges, const int64_t* dims,
+                  const int32_t* isdual, mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(out, "out");
+    auto sp = parse_spaces(nspaces, nsect, charges, dims, isdual);
+    *out = wrap(mpsg::splitleg(&ctx->c, a->t, l, sp));
+  });
+}
+
+int mpsg_symmatrix(mpsg_ctx* ctx, const mpsg_tensor* a, int32_t nrows, const int32_t* rows,
+                   int32_t ncols, const int32_t* cols, mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(out, "out");
+    if (nrows < 0 || ncols < 0) throw mpsg::Error(mpsg::kErrArgument, "negative count");
+    std::vector<int> r = nrows ? ivec(rows, nrows) : std::vector<int>();
+    std::vector<int> c = ncols ? ivec(cols, ncols) : std::vector<int>();
+    *out = wrap(mpsg::symmatrix(&ctx->c, a->t, r, c));
+  });
+}
+
+int mpsg_matmul(mpsg_ctx* ctx, const mpsg_tensor* a, const mpsg_tensor* b, int32_t precision,
+                mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(b, "b");
+    need(out, "out");
+    *out = wrap(mpsg::matmul(&ctx->c, a->t, b->t, precision));
+  });
+}
+
+int mpsg_contract(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
+                  const int32_t* idxb, int32_t precision, mpsg_tensor** out, double* scalar) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(b, "b");
+    need(idxa, "idxa");
+    need(idxb, "idxb");
+    need(out, "out");
+    double s = 0.0;
+    mpsg::DeviceTensor r = mpsg::contract(&ctx->c, a->t, ivec(idxa, a->t.meta.N()), b->t,
+                                          ivec(idxb, b->t.meta.N()), precision, &s);
+    if (!r.buf && r.meta.space.empty()) {
+      *out = nullptr;
+      if (scalar) *scalar = s;
+    } else {
+      *out = wrap(std::move(r));
+    }
+  });
+}
+
+int mpsg_contract_flops(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa,
+                        const mpsg_tensor* b, const int32_t* idxb, double* flops) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(b, "b");
+    need(flops, "flops");
+    auto p = mpsg::get_contract_plan(&ctx->c, a->t.meta, ivec(idxa, a->t.meta.N()), b->t.meta,
+                                     ivec(idxb, b->t.meta.N()));
+    *flops = p->host->flops;
+  });
+}
+
+int mpsg_applymps2site(mpsg_ctx* ctx, const mpsg_tensor* v, const mpsg_tensor* envl,
+                       const mpsg_tensor* envr, const mpsg_tensor* w1, const mpsg_tensor* w2,
+                       int32_t precision, mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(v, "v");
+    need(envl, "envl");
+    need(envr, "envr");
+    need(w1, "w1");
+    need(w2, "w2");
+    need(out, "out");
+    *out = wrap(mpsg::applymps2site(&ctx->c, v->t, envl->t, envr->t, w1->t, w2->t, precision));
+  });
+}
+
+int mpsg_applymps2site_flops(mpsg_ctx* ctx, const mpsg_tensor* v, const mpsg_tensor* envl,
+                             const mpsg_tensor* envr, const mpsg_tensor* w1,
+                             const mpsg_tensor* w2, double* flops) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(v, "v");
+    need(envl, "envl");
+    need(envr, "envr");
+    need(w1, "w1");
+    need(w2, "w2");
+    need(flops, "flops");
+    *flops = mpsg::applymps2site_flops(&ctx->c, v->t.meta, envl->t.meta, envr->t.meta,
+                                       w1->t.meta, w2->t.meta);
+  });
+}
+
+int mpsg_mpsupdateleft(mpsg_ctx* ctx, const mpsg_tensor* env, const mpsg_tensor* a,
+                       const mpsg_tensor* w, int32_t precision, mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(env, "env");
+    need(a, "a");
+    need(w, "w");
+    need(out, "out");
+    *out = wrap(mpsg::mpsupdateleft(&ctx->c, env->t, a->t, w->t, precision));
+  });
+}
+
+int mpsg_mpsupdateright(mpsg_ctx* ctx, const mpsg_tensor* env, const mpsg_tensor* a,
+                        const mpsg_tensor* w, int32_t precision, mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(env, "env");
+    need(a, "a");
+    need(w, "w");
+    need(out, "out");
+    *out = wrap(mpsg::mpsupdateright(&ctx->c, env->t, a->t, w->t, precision));
+  });
+}
+
+static mpsg_tensor* meta_only(const mpsg::TensorMeta& m) {
+  mpsg::DeviceTensor t;
+  t.meta = m;
+  return wrap(std::move(t));
+}
+
+int mpsg_meta_create(int32_t charge, int32_t nlegs, const int32_t* nsect, const int32_t* charges,
+                     const int64_t* dims, const int32_t* isdual, mpsg_tensor** out) {
+  return guarded([&] {
+    need(out, "out");
+    auto sp = parse_spaces(nlegs, nsect, charges, dims, isdual);
+    *out = meta_only(mpsg::TensorMeta::build(charge, sp));
+  });
+}
+
+int mpsg_plan_permutelegs(const mpsg_tensor* a, const int32_t* perm, mpsg_tensor** out) {
+  return guarded([&] {
+    need(a, "a");
+    need(perm, "perm");
+    need(out, "out");
+    auto p = mpsg::plan_permutelegs(a->t.meta, ivec(perm, a->t.meta.N()));
+    mpsg::validate_copy_tasks(p.tasks, a->t.meta.total, p.out.total);
+    *out = meta_only(p.out);
+  });
+}
+
+int mpsg_plan_fuselegs(const mpsg_tensor* a, int32_t l, int32_t n, int32_t dual,
+                       mpsg_tensor** out) {
+  return guarded([&] {
+    need(a, "a");
+    need(out, "out");
+    auto p = mpsg::plan_fuselegs(a->t.meta, l, n, dual != 0);
+    mpsg::validate_copy_tasks(p.tasks, a->t.meta.total, p.out.total);
+    *out = meta_only(p.out);
+  });
+}
+
+int mpsg_plan_splitleg(const mpsg_tensor* a, int32_t l, int32_t nspaces, const int32_t* nsect,
+                       const int32_t* charges, const int64_t* dims, const int32_t* isdual,
+                       mpsg_tensor** out) {
+  return guarded([&] {
+    need(a, "a");
+    need(out, "out");
+    auto sp = parse_spaces(nspaces, nsect, charges, dims, isdual);
+    auto p = mpsg::plan_splitleg(a->t.meta, l, sp);
+    mpsg::validate_copy_tasks(p.tasks, a->t.meta.total, p.out.total);
+    *out = meta_only(p.out);
+  });
+}
+
+int mpsg_plan_symmatrix(const mpsg_tensor* a, int32_t nrows, const int32_t* rows, int32_t ncols,
+                        const int32_t* cols, mpsg_tensor** out) {
+  return guarded([&] {
+    need(a, "a");
+    need(out, "out");
+    if (nrows < 0 || ncols < 0) throw mpsg::Error(mpsg::kErrArgument, "negative count");
+    std::vector<int> r = nrows ? ivec(rows, nrows) : std::vector<int>();
+    std::vector<int> c = ncols ? ivec(cols, ncols) : std::vector<int>();
+    auto p = mpsg::plan_symmatrix(a->t.meta, r, c);
+    mpsg::validate_copy_tasks(p.tasks, a->t.meta.total, p.out.total);
+    *out = meta_only(p.out);
+  });
+}
+
+int mpsg_plan_matmul(const mpsg_tensor* a, const mpsg_tensor* b, mpsg_tensor** out,
+                     double* flops) {
+  return guarded([&] {
+    need(a, "a");
+    need(b, "b");
+    need(out, "out");
+    auto p = mpsg::plan_matmul(a->t.meta, b->t.meta);
+    mpsg::validate_gemms(p.gemms, a->t.meta.total, b->t.meta.total, p.out.total);
+    if (flops) *flops = p.flops;
+    *out = meta_only(p.out);
+  });
+}
+
+int mpsg_plan_contract(const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
+                       const int32_t* idxb, mpsg_tensor** out, double* flops) {
+  return guarded([&] {
+    need(a, "a");
+    need(b, "b");
+    need(idxa, "idxa");
+    need(idxb, "idxb");
+    need(out, "out");
+    auto p = mpsg::plan_contract(a->t.meta, ivec(idxa, a->t.meta.N()), b->t.meta,
+                                 ivec(idxb, b->t.meta.N()));
+    mpsg::validate_contract(*p, a->t.meta, b->t.meta);
+    if (flops) *flops = p->flops;
+    *out = p->scalar ? nullptr : meta_only(p->split.out);
+  });
+}
+
+int mpsg_plan_contract_tasks(const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
+                             const int32_t* idxb, int64_t* copy_tasks, int64_t* gemm_tasks) {
+  return guarded([&] {
+    need(a, "a");
+    need(b, "b");
+    need(idxa, "idxa");
+    need(idxb, "idxb");
+    auto p = mpsg::plan_contract(a->t.meta, ivec(idxa, a->t.meta.N()), b->t.meta,
+                                 ivec(idxb, b->t.meta.N()));
+    if (copy_tasks)
+      *copy_tasks = (int64_t)(p->fa.tasks.size() + p->fb.tasks.size() + p->split.tasks.size());
+    if (gemm_tasks) *gemm_tasks = (int64_t)p->mm.gemms.size();
+  });
+}
+
+int mpsg_fill(mpsg_ctx* ctx, mpsg_tensor* a, double x) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    mpsg::launch_fill(&ctx->c, a->t.data(), a->t.meta.total, x);
+  });
+}
+
+int mpsg_rmul(mpsg_ctx* ctx, mpsg_tensor* a, double alpha) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    mpsg::launch_scale(&ctx->c, a->t.meta.total, alpha, a->t.data(), a->t.data());
+  });
+}
+
+int mpsg_mul(mpsg_ctx* ctx, mpsg_tensor* b, const mpsg_tensor* a, double alpha) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(b, "b");
+    mpsg::require_similar(a->t, b->t, "oops");
+    mpsg::launch_scale(&ctx->c, a->t.meta.total, alpha, a->t.data(), b->t.data());
+  });
+}
+
+int mpsg_axpy(mpsg_ctx* ctx, double alpha, const mpsg_tensor* a, mpsg_tensor* b) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(b, "b");
+    mpsg::require_similar(a->t, b->t, "axpy! The two matrices are not simliar!");
+    mpsg::launch_axpby(&ctx->c, a->t.meta.total, alpha, a->t.data(), 1.0, b->t.data());
+  });
+}
+
+int mpsg_axpby(mpsg_ctx* ctx, double alpha, const mpsg_tensor* a, double beta, mpsg_tensor* b) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(b, "b");
+    mpsg::require_similar(a->t, b->t, "axpy! The two matrices are not simliar!");
+    mpsg::launch_axpby(&ctx->c, a->t.meta.total, alpha, a->t.data(), beta, b->t.data());
+  });
+}
+
+int mpsg_dot(mpsg_ctx* ctx, const mpsg_tensor* a, const mpsg_tensor* b, double* out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(b, "b");
+    need(out, "out");
+    mpsg::require_similar(a->t, b->t, "The two SymTensors have to be similar to dot!");
+    *out = mpsg::dot(&ctx->c, a->t, b->t);
+  });
+}
+
+int mpsg_norm(mpsg_ctx* ctx, const mpsg_tensor* a, double* out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(out, "out");
+    *out = std::sqrt(mpsg::dot(&ctx->c, a->t, a->t));
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,220 @@
+// Plain FP64 path: grouped block GEMM (one persistent launch over every sector GEMM of a
+// contraction) and the FP64 vector operations of the Krylov solver.
+//
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the GEMM is a register-blocked
+// DFMA kernel whose only job is to keep the FP64 pipe busy: 64x64 output tile per CTA, 4x4
+// accumulators per thread, K staged through shared memory in steps of 16.
+#include "runtime.hpp"
+
+namespace mpsg {
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16;
+
+__global__ void __launch_bounds__(256) gemm_f64_grouped_kernel(
+    const GemmTask* __restrict__ tasks, const int64_t* __restrict__ prefix, int ntasks,
+    int64_t ntiles, const double* __restrict__ A, const double* __restrict__ B,
+    double* __restrict__ C) {
+  __shared__ double As[BK][BM + 1];
+  __shared__ double Bs[BK][BN + 1];
+  __shared__ GemmTask g;
+  __shared__ int64_t first;
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    if (tid == 0) {
+      int lo = 0, hi = ntasks - 1;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= t) lo = mid;
+        else hi = mid - 1;
+      }
+      g = tasks[lo];
+      first = prefix[lo];
+    }
+    __syncthreads();
+    const int64_t tm = (g.M + BM - 1) / BM;
+    const int64_t lt = t - first;
+    const int64_t m0 = (lt % tm) * BM, n0 = (lt / tm) * BN;
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    const double* Ab = A + g.offA;
+    const double* Bb = B + g.offB;
+    for (int64_t k0 = 0; k0 < g.K; k0 += BK) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        int m = tid & 63, k = (tid >> 6) + 4 * r;
+        int64_t gm = m0 + m, gk = k0 + k;
+        As[k][m] = (gm < g.M && gk < g.K) ? __ldg(Ab + gm + gk * g.lda) : 0.0;
+        int kb = tid & 15, n = (tid >> 4) + 16 * r;
+        int64_t gkb = k0 + kb, gn = n0 + n;
+        Bs[kb][n] = (gkb < g.K && gn < g.N) ? __ldg(Bb + gkb + gn * g.ldb) : 0.0;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < BK; ++k) {
+        double a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[k][tx + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = Bs[k][ty + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
+      __syncthreads();
+    }
+    double* Cb = C + g.offC;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int64_t gn = n0 + ty + 16 * j;
+      if (gn >= g.N) continue;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        int64_t gm = m0 + tx + 16 * i;
+        if (gm < g.M) Cb[gm + gn * g.ldc] = acc[i][j];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void fill_kernel(double* __restrict__ x, int64_t n, double v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = v;
+}
+
+__global__ void axpby_kernel(int64_t n, double a, const double* __restrict__ x, double b,
+                             double* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = fma(a, x[i], b * y[i]);
+}
+
+__global__ void scale_kernel(int64_t n, double a, const double* __restrict__ x,
+                             double* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i];
+}
+
+__device__ inline double block_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += sh[i];
+  return r;
+}
+
+// Pass 1: fixed-grid partial sums; pass 2: one CTA sums the partials in a fixed order.
+__global__ void __launch_bounds__(256) dot_partial_kernel(int64_t n, const double* __restrict__ x,
+                                                          const double* __restrict__ y,
+                                                          double* __restrict__ partial) {
+  __shared__ double sh[8];
+  double v = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    v = fma(x[i], y[i], v);
+  double r = block_sum(v, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = r;
+}
+
+__global__ void __launch_bounds__(256) sum_partials_kernel(int np, const double* __restrict__ p,
+                                                           double* __restrict__ out) {
+  __shared__ double sh[8];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) v += p[i];
+  double r = block_sum(v, sh);
+  if (threadIdx.x == 0) *out = r;
+}
+
+int vec_grid(Context* ctx, int64_t n) {
+  int64_t g = (n + 255) / 256;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * 4));
+}
+
+}  // namespace
+
+void DevGemmPlan::upload(const std::vector<GemmTask>& g, double flops_) {
+  release();
+  host = g;
+  flops = flops_;
+  n = (int)g.size();
+  std::vector<int64_t> prefix(n + 1, 0);
+  for (int k = 0; k < n; ++k) {
+    int64_t tiles = ((g[k].M + BM - 1) / BM) * ((g[k].N + BN - 1) / BN);
+    prefix[k + 1] = prefix[k] + tiles;
+  }
+  ntiles = prefix[n];
+  if (n == 0) return;
+  MPSG_CUDA(cudaMalloc(&d_tasks, sizeof(GemmTask) * n));
+  MPSG_CUDA(cudaMalloc(&d_prefix, sizeof(int64_t) * (n + 1)));
+  MPSG_CUDA(cudaMemcpy(d_tasks, g.data(), sizeof(GemmTask) * n, cudaMemcpyHostToDevice));
+  MPSG_CUDA(cudaMemcpy(d_prefix, prefix.data(), sizeof(int64_t) * (n + 1),
+                       cudaMemcpyHostToDevice));
+}
+
+void DevGemmPlan::release() {
+  if (d_tasks) cudaFree(d_tasks);
+  if (d_prefix) cudaFree(d_prefix);
+  d_tasks = nullptr;
+  d_prefix = nullptr;
+  n = 0;
+  ntiles = 0;
+}
+
+void launch_gemm_f64(Context* ctx, const DevGemmPlan& p, const double* A, const double* B,
+                     double* C) {
+  if (p.ntiles == 0) return;
+  int64_t grid = std::min<int64_t>(p.ntiles, (int64_t)ctx->num_sms * 4);
+  KernelTimer timer(ctx, kKindGemmF64, p.flops);
+  gemm_f64_grouped_kernel<<<(unsigned)grid, 256, 0, ctx->stream>>>(p.d_tasks, p.d_prefix, p.n,
+                                                                   p.ntiles, A, B, C);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches++;
+  ctx->gemm_flops += p.flops;
+}
+
+void launch_fill(Context* ctx, double* x, int64_t n, double v) {
+  if (n == 0) return;
+  fill_kernel<<<vec_grid(ctx, n), 256, 0, ctx->stream>>>(x, n, v);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches++;
+}
+
+void launch_axpby(Context* ctx, int64_t n, double a, const double* x, double b, double* y) {
+  if (n == 0) return;
+  axpby_kernel<<<vec_grid(ctx, n), 256, 0, ctx->stream>>>(n, a, x, b, y);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches++;
+}
+
+void launch_scale(Context* ctx, int64_t n, double a, const double* x, double* y) {
+  if (n == 0) return;
+  scale_kernel<<<vec_grid(ctx, n), 256, 0, ctx->stream>>>(n, a, x, y);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches++;
+}
+
+void launch_dot(Context* ctx, int64_t n, const double* x, const double* y, double* d_out) {
+  if (n == 0) {
+    launch_fill(ctx, d_out, 1, 0.0);
+    return;
+  }
+  int g = vec_grid(ctx, n);
+  dot_partial_kernel<<<g, 256, 0, ctx->stream>>>(n, x, y, ctx->d_partials);
+  sum_partials_kernel<<<1, 256, 0, ctx->stream>>>(g, ctx->d_partials, d_out);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches += 2;
+}
+
+}  // namespace mpsg

@@ -1,0 +1,370 @@
+// Tensor-level operations: plan lookup (cached per structure), scratch management and the
+// launch sequences of each SymTensors operation.
+#include <sstream>
+
+#include "ops.hpp"
+
+namespace mpsg {
+
+// ------------------------------------------------------------------------------------------
+// context and buffers
+// ------------------------------------------------------------------------------------------
+Buffer::~Buffer() {
+  if (ptr) cudaFreeAsync(ptr, ctx->stream);
+}
+
+std::shared_ptr<Buffer> alloc_buffer(Context* ctx, int64_t n) {
+  auto b = std::make_shared<Buffer>();
+  b->ctx = ctx;
+  b->n = n;
+  if (n > 0) MPSG_CUDA(cudaMallocAsync((void**)&b->ptr, sizeof(double) * n, ctx->stream));
+  return b;
+}
+
+void context_init(Context* ctx, int device) {
+  ctx->device = device;
+  MPSG_CUDA(cudaSetDevice(device));
+  MPSG_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+  MPSG_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  cudaMemPool_t pool;
+  MPSG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+  uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
+  MPSG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  MPSG_CUDA(cudaMalloc(&ctx->d_partials, sizeof(double) * (ctx->num_sms * 4 + 64)));
+  MPSG_CUDA(cudaMallocHost(&ctx->h_pinned, sizeof(double) * 64));
+}
+
+static cudaEvent_t take_event(Context* ctx) {
+  if (!ctx->event_pool.empty()) {
+    cudaEvent_t e = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  MPSG_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+KernelTimer::KernelTimer(Context* c, int k, double f) : ctx(c), kind(k), flops(f) {
+  if (!ctx->timing) return;
+  a = take_event(ctx);
+  b = take_event(ctx);
+  MPSG_CUDA(cudaEventRecord(a, ctx->stream));
+}
+
+KernelTimer::~KernelTimer() {
+  if (!a) return;
+  cudaEventRecord(b, ctx->stream);
+  ctx->events[kind].push_back({a, b, flops});
+}
+
+void collect_kernel_times(Context* ctx) {
+  MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int k = 0; k < Context::kKinds; ++k) {
+    for (auto& ev : ctx->events[k]) {
+      float ms = 0.f;
+      MPSG_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+      ctx->timed_ms[k] += ms;
+      ctx->timed_launches[k] += 1;
+      ctx->timed_flops[k] += ev.flops;
+      ctx->event_pool.push_back(ev.a);
+      ctx->event_pool.push_back(ev.b);
+    }
+    ctx->events[k].clear();
+  }
+}
+
+Context::~Context() {
+  contract_cache.clear();
+  releg_cache.clear();
+  matmul_cache.clear();
+  if (stream) cudaStreamSynchronize(stream);
+  for (auto& v : events)
+    for (auto& ev : v) {
+      cudaEventDestroy(ev.a);
+      cudaEventDestroy(ev.b);
+    }
+  for (auto e : event_pool) cudaEventDestroy(e);
+  if (d_partials) cudaFree(d_partials);
+  if (h_pinned) cudaFreeHost(h_pinned);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+DevContract::~DevContract() {
+  fa.release();
+  fb.release();
+  split.release();
+  mm.release();
+}
+
+DevReleg::~DevReleg() { cp.release(); }
+
+// ------------------------------------------------------------------------------------------
+// tensors
+// ------------------------------------------------------------------------------------------
+DeviceTensor new_tensor(Context* ctx, const TensorMeta& meta, bool zero) {
+  DeviceTensor t;
+  t.ctx = ctx;
+  t.meta = meta;
+  t.buf = alloc_buffer(ctx, meta.total);
+  if (zero && meta.total)
+    MPSG_CUDA(cudaMemsetAsync(t.buf->ptr, 0, sizeof(double) * meta.total, ctx->stream));
+  return t;
+}
+
+DeviceTensor copy_tensor(Context* ctx, const DeviceTensor& a) {
+  DeviceTensor t = new_tensor(ctx, a.meta, false);
+  t.diag = a.diag;
+  if (a.meta.total)
+    MPSG_CUDA(cudaMemcpyAsync(t.data(), a.data(), sizeof(double) * a.meta.total,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+  return t;
+}
+
+DeviceTensor dual_view(const DeviceTensor& a) {
+  DeviceTensor t = a;
+  t.meta.charge = -a.meta.charge;
+  for (auto& V : t.meta.space) V.dual = !V.dual;
+  return t;
+}
+
+void require_similar(const DeviceTensor& a, const DeviceTensor& b, const char* msg) {
+  if (!same_meta(a.meta, b.meta)) throw Error(kErrSpaceMismatch, msg);
+}
+
+// ------------------------------------------------------------------------------------------
+// releg
+// ------------------------------------------------------------------------------------------
+static std::string vkey(const std::vector<int>& v) {
+  std::ostringstream os;
+  for (int x : v) os << x << ',';
+  return os.str();
+}
+
+static std::string spaces_key(const std::vector<Space>& sp) {
+  TensorMeta m;
+  m.space = sp;
+  return meta_key(m);
+}
+
+template <class Build>
+static std::shared_ptr<DevReleg> releg_plan(Context* ctx, const std::string& key, Build&& build) {
+  auto it = ctx->releg_cache.find(key);
+  if (it != ctx->releg_cache.end()) return it->second;
+  auto p = std::make_shared<DevReleg>();
+  p->host = build();
+  p->cp.upload(p->host.tasks, p->host.identity);
+  ctx->releg_cache[key] = p;
+  return p;
+}
+
+static DeviceTensor run_releg(Context* ctx, const DevReleg& p, const DeviceTensor& a) {
+  DeviceTensor t;
+  t.ctx = ctx;
+  t.meta = p.host.out;
+  if (p.host.identity) {
+    t.buf = a.buf;  // same bytes: share the buffer
+    return t;
+  }
+  t.buf = alloc_buffer(ctx, t.meta.total);
+  launch_copy(ctx, p.cp, a.data(), t.data());
+  return t;
+}
+
+DeviceTensor permutelegs(Context* ctx, const DeviceTensor& a, const std::vector<int>& perm1) {
+  auto p = releg_plan(ctx, "P|" + meta_key(a.meta) + vkey(perm1),
+                      [&] { return plan_permutelegs(a.meta, perm1); });
+  DeviceTensor t = run_releg(ctx, *p, a);
+  t.diag = a.diag;
+  return t;
+}
+
+DeviceTensor fuselegs(Context* ctx, const DeviceTensor& a, int l1, int n, bool dual) {
+  auto p = releg_plan(ctx, "F|" + meta_key(a.meta) + vkey({l1, n, (int)dual}),
+                      [&] { return plan_fuselegs(a.meta, l1, n, dual); });
+  return run_releg(ctx, *p, a);
+}
+
+DeviceTensor splitleg(Context* ctx, const DeviceTensor& a, int l1, const std::vector<Space>& sp) {
+  auto p = releg_plan(ctx, "S|" + meta_key(a.meta) + vkey({l1}) + spaces_key(sp),
+                      [&] { return plan_splitleg(a.meta, l1, sp); });
+  return run_releg(ctx, *p, a);
+}
+
+DeviceTensor symmatrix(Context* ctx, const DeviceTensor& a, const std::vector<int>& rows,
+                       const std::vector<int>& cols) {
+  auto p = releg_plan(ctx, "M|" + meta_key(a.meta) + vkey(rows) + "/" + vkey(cols), [&] {
+    FusePlan f = plan_symmatrix(a.meta, rows, cols);
+    RelegPlan r;
+    r.out = f.out;
+    r.tasks = f.tasks;
+    r.identity = f.identity;
+    return r;
+  });
+  return run_releg(ctx, *p, a);
+}
+
+// ------------------------------------------------------------------------------------------
+// block GEMM dispatch
+// ------------------------------------------------------------------------------------------
+static void run_gemm(Context* ctx, const DevGemmPlan& g, const double* A, const double* B,
+                     double* C, int precision) {
+  if (precision == 0) {
+    launch_gemm_f64(ctx, g, A, B, C);
+    return;
+  }
+  throw Error(kErrUnsupported, "split-precision GEMM not available in this build");
+}
+
+DeviceTensor matmul(Context* ctx, const DeviceTensor& a, const DeviceTensor& b, int precision) {
+  std::string key = "G|" + meta_key(a.meta) + "*" + meta_key(b.meta);
+  std::shared_ptr<DevGemmPlan> g;
+  std::shared_ptr<TensorMeta> outmeta;
+  auto it = ctx->matmul_cache.find(key);
+  MatmulPlan mp;
+  if (it == ctx->matmul_cache.end()) {
+    mp = plan_matmul(a.meta, b.meta);
+    g = std::make_shared<DevGemmPlan>();
+    g->upload(mp.gemms, mp.flops);
+    ctx->matmul_cache[key] = g;
+  } else {
+    g = it->second;
+  }
+  DeviceTensor t;
+  t.ctx = ctx;
+  t.meta = TensorMeta::build(a.meta.charge + b.meta.charge, {a.meta.space[0], b.meta.space[1]});
+  t.buf = alloc_buffer(ctx, t.meta.total);
+  run_gemm(ctx, *g, a.data(), b.data(), t.data(), precision);
+  return t;
+}
+
+// ------------------------------------------------------------------------------------------
+// contract
+// ------------------------------------------------------------------------------------------
+std::shared_ptr<DevContract> get_contract_plan(Context* ctx, const TensorMeta& A,
+                                               const std::vector<int>& idxA,
+                                               const TensorMeta& B,
+                                               const std::vector<int>& idxB) {
+  std::string key = "C|" + meta_key(A) + vkey(idxA) + "|" + meta_key(B) + vkey(idxB);
+  auto it = ctx->contract_cache.find(key);
+  if (it != ctx->contract_cache.end()) return it->second;
+  auto p = std::make_shared<DevContract>();
+  p->host = plan_contract(A, idxA, B, idxB);
+  if (!p->host->scalar) {
+    p->fa.upload(p->host->fa.tasks, p->host->fa.identity);
+    p->fb.upload(p->host->fb.tasks, p->host->fb.identity);
+    p->mm.upload(p->host->mm.gemms, p->host->mm.flops);
+    p->split.upload(p->host->split.tasks, p->host->split.identity);
+  }
+  ctx->contract_cache[key] = p;
+  return p;
+}
+
+DeviceTensor contract(Context* ctx, const DeviceTensor& a, const std::vector<int>& idxA,
+                      const DeviceTensor& b, const std::vector<int>& idxB, int precision,
+                      double* scalar) {
+  auto p = get_contract_plan(ctx, a.meta, idxA, b.meta, idxB);
+  if (p->host->scalar) {
+    // SymVector(A) .* SymVector(B) summed (contract.jl:24-28, 226-232)
+    std::vector<int> ra, ca, tf, rb, cb, tfb;
+    contract_index_perm(idxA, ra, ca, tf);
+    contract_index_perm(idxB, rb, cb, tfb);
+    DeviceTensor va = fuselegs(ctx, permutelegs(ctx, a, ca), 1, a.meta.N(), false);
+    DeviceTensor vb = fuselegs(ctx, permutelegs(ctx, b, cb), 1, b.meta.N(), true);
+    double s = 0.0;
+    if (va.meta.nblocks() && vb.meta.nblocks()) {
+      long ib = vb.meta.find(va.meta.sec.labels(0));
+      if (ib < 0) throw Error(kErrSpaceMismatch, "KeyError in SymVector product");
+      int64_t n = va.meta.sec.numel(0);
+      launch_dot(ctx, n, va.data() + va.meta.off[0], vb.data() + vb.meta.off[ib],
+                 ctx->d_partials + ctx->num_sms * 4);
+      MPSG_CUDA(cudaMemcpyAsync(ctx->h_pinned, ctx->d_partials + ctx->num_sms * 4,
+                                sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+      s = ctx->h_pinned[0];
+    }
+    if (scalar) *scalar = s;
+    return DeviceTensor();
+  }
+  std::shared_ptr<Buffer> fa, fb, fc;
+  const double* pa = a.data();
+  const double* pb = b.data();
+  if (!p->fa.identity) {
+    fa = alloc_buffer(ctx, p->host->fa.out.total);
+    launch_copy(ctx, p->fa, a.data(), fa->ptr);
+    pa = fa->ptr;
+  }
+  if (!p->fb.identity) {
+    fb = alloc_buffer(ctx, p->host->fb.out.total);
+    launch_copy(ctx, p->fb, b.data(), fb->ptr);
+    pb = fb->ptr;
+  }
+  DeviceTensor t;
+  t.ctx = ctx;
+  t.meta = p->host->split.out;
+  fc = alloc_buffer(ctx, p->host->mm.out.total);
+  run_gemm(ctx, p->mm, pa, pb, fc->ptr, precision);
+  if (p->split.identity) {
+    t.buf = fc;
+  } else {
+    t.buf = alloc_buffer(ctx, t.meta.total);
+    launch_copy(ctx, p->split, fc->ptr, t.data());
+  }
+  return t;
+}
+
+// ------------------------------------------------------------------------------------------
+// effective Hamiltonian and environments (apply.jl:17-25, 49-58, 93-105)
+// ------------------------------------------------------------------------------------------
+static const std::vector<int> kH1A = {-1, 2, 1}, kH1B = {-1, 3, 4, 5};
+static const std::vector<int> kH2A = {1, -1, -2, 4, 5}, kH2B = {-1, 2, 3, -2};
+static const std::vector<int> kH3A = {1, 2, -1, -2, 5}, kH3B = {-1, 3, 4, -2};
+static const std::vector<int> kH4A = {1, 2, 3, -1, -2}, kH4B = {-2, -1, 4};
+
+DeviceTensor applymps2site(Context* ctx, const DeviceTensor& v, const DeviceTensor& envL,
+                           const DeviceTensor& envR, const DeviceTensor& W1,
+                           const DeviceTensor& W2, int precision) {
+  DeviceTensor t1 = contract(ctx, envL, kH1A, v, kH1B, precision, nullptr);
+  DeviceTensor t2 = contract(ctx, t1, kH2A, W1, kH2B, precision, nullptr);
+  t1 = DeviceTensor();
+  DeviceTensor t3 = contract(ctx, t2, kH3A, W2, kH3B, precision, nullptr);
+  t2 = DeviceTensor();
+  return contract(ctx, t3, kH4A, envR, kH4B, precision, nullptr);
+}
+
+double applymps2site_flops(Context* ctx, const TensorMeta& v, const TensorMeta& envL,
+                           const TensorMeta& envR, const TensorMeta& W1, const TensorMeta& W2) {
+  auto p1 = get_contract_plan(ctx, envL, kH1A, v, kH1B);
+  auto p2 = get_contract_plan(ctx, p1->host->split.out, kH2A, W1, kH2B);
+  auto p3 = get_contract_plan(ctx, p2->host->split.out, kH3A, W2, kH3B);
+  auto p4 = get_contract_plan(ctx, p3->host->split.out, kH4A, envR, kH4B);
+  return p1->host->flops + p2->host->flops + p3->host->flops + p4->host->flops;
+}
+
+DeviceTensor mpsupdateleft(Context* ctx, const DeviceTensor& env, const DeviceTensor& A,
+                           const DeviceTensor& W, int precision) {
+  DeviceTensor t = contract(ctx, env, {-1, 3, 4}, A, {-1, 2, 1}, precision, nullptr);
+  t = contract(ctx, t, {1, -1, -2, 4}, W, {-2, 2, 3, -1}, precision, nullptr);
+  return contract(ctx, t, {1, -1, 2, -2}, dual_view(A), {-2, -1, 3}, precision, nullptr);
+}
+
+DeviceTensor mpsupdateright(Context* ctx, const DeviceTensor& env, const DeviceTensor& A,
+                            const DeviceTensor& W, int precision) {
+  DeviceTensor t = contract(ctx, env, {-1, 3, 4}, A, {1, 2, -1}, precision, nullptr);
+  t = contract(ctx, t, {1, -1, -2, 4}, W, {3, 2, -2, -1}, precision, nullptr);
+  return contract(ctx, t, {1, -1, 2, -2}, dual_view(A), {3, -1, -2}, precision, nullptr);
+}
+
+// ------------------------------------------------------------------------------------------
+// reductions
+// ------------------------------------------------------------------------------------------
+double dot(Context* ctx, const DeviceTensor& a, const DeviceTensor& b) {
+  double* d_out = ctx->d_partials + ctx->num_sms * 4;
+  launch_dot(ctx, a.meta.total, a.data(), b.data(), d_out);
+  MPSG_CUDA(cudaMemcpyAsync(ctx->h_pinned, d_out, sizeof(double), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return ctx->h_pinned[0];
+}
+
+}  // namespace mpsg

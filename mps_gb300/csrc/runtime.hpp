@@ -1,0 +1,131 @@
+// Device runtime: context (device, stream, plan cache), device tensors and the launchers of the
+// CUDA kernels.  Everything here is called from the C ABI in capi.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "planner.hpp"
+
+namespace mpsg {
+
+#define MPSG_CUDA(call)                                                                     \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      throw ::mpsg::Error(::mpsg::kErrCuda, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct Context;
+
+// Stream-ordered device allocation owned by a context.
+struct Buffer {
+  Context* ctx = nullptr;
+  double* ptr = nullptr;
+  int64_t n = 0;
+  ~Buffer();
+};
+std::shared_ptr<Buffer> alloc_buffer(Context* ctx, int64_t n);
+
+struct DeviceTensor {
+  Context* ctx = nullptr;
+  TensorMeta meta;
+  std::shared_ptr<Buffer> buf;  // shared by views (dual) of the same data
+  bool diag = false;            // singular values stored as dense diagonal blocks
+  double* data() const { return buf ? buf->ptr : nullptr; }
+};
+
+// Copy-task list on the device with per-task tile prefix sums.
+struct DevCopyPlan {
+  int ntasks = 0;
+  int64_t ntiles = 0;
+  int64_t elems = 0;
+  bool identity = false;
+  CopyTask* d_tasks = nullptr;
+  int64_t* d_prefix = nullptr;   // ntasks+1 tile prefix
+  int32_t* d_mode = nullptr;     // per task: packed (mode, axis a, axis b)
+  void upload(const std::vector<CopyTask>& tasks, bool identity_);
+  void release();
+};
+
+struct DevGemmPlan {
+  int n = 0;
+  int64_t ntiles = 0;
+  double flops = 0;
+  GemmTask* d_tasks = nullptr;
+  int64_t* d_prefix = nullptr;
+  int64_t max_ld = 0;
+  std::vector<GemmTask> host;
+  void upload(const std::vector<GemmTask>& g, double flops_);
+  void release();
+};
+
+struct DevContract {
+  std::shared_ptr<ContractPlan> host;
+  DevCopyPlan fa, fb, split;
+  DevGemmPlan mm;
+  ~DevContract();
+};
+
+struct DevReleg {
+  RelegPlan host;
+  DevCopyPlan cp;
+  ~DevReleg();
+};
+
+struct Context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  double* d_partials = nullptr;   // reduction partials (one per CTA of a reduction launch)
+  double* h_pinned = nullptr;     // small pinned host scratch for scalar results
+  std::unordered_map<std::string, std::shared_ptr<DevContract>> contract_cache;
+  std::unordered_map<std::string, std::shared_ptr<DevReleg>> releg_cache;
+  std::unordered_map<std::string, std::shared_ptr<DevGemmPlan>> matmul_cache;
+  int64_t kernel_launches = 0;    // launches of this library's kernels
+  double gemm_flops = 0;          // algorithmic flops issued through block GEMMs
+  void* solver = nullptr;         // cusolverDnHandle_t, created on first SVD
+  // optional per-kernel-class event timing (see mpsg_ctx_set_timing)
+  static constexpr int kKinds = 5;
+  bool timing = false;
+  struct TimedLaunch {
+    cudaEvent_t a, b;
+    double flops;
+  };
+  std::vector<TimedLaunch> events[kKinds];
+  std::vector<cudaEvent_t> event_pool;
+  double timed_ms[kKinds] = {0, 0, 0, 0, 0};
+  int64_t timed_launches[kKinds] = {0, 0, 0, 0, 0};
+  double timed_flops[kKinds] = {0, 0, 0, 0, 0};
+  ~Context();
+};
+
+enum KernelKind { kKindCopy = 0, kKindGemmF64 = 1, kKindGemmSplit = 2, kKindPack = 3, kKindVec = 4 };
+
+// RAII bracket of one launch with events when timing is enabled.
+struct KernelTimer {
+  Context* ctx;
+  int kind;
+  double flops;
+  cudaEvent_t a = nullptr, b = nullptr;
+  KernelTimer(Context* c, int k, double f = 0.0);
+  ~KernelTimer();
+};
+void collect_kernel_times(Context* ctx);
+
+// ---- kernel launchers (kernels_*.cu) ----
+void launch_copy(Context* ctx, const DevCopyPlan& p, const double* src, double* dst);
+void launch_gemm_f64(Context* ctx, const DevGemmPlan& p, const double* A, const double* B,
+                     double* C);
+void launch_fill(Context* ctx, double* x, int64_t n, double v);
+void launch_axpby(Context* ctx, int64_t n, double a, const double* x, double b, double* y);
+void launch_scale(Context* ctx, int64_t n, double a, const double* x, double* y);
+// sum_i x_i*y_i into *out (device), deterministic two-pass reduction
+void launch_dot(Context* ctx, int64_t n, const double* x, const double* y, double* d_out);
+
+}  // namespace mpsg

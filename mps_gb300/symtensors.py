@@ -1,0 +1,575 @@
+"""Host-side mirror of the SymTensors API of amiragha/mps, backed by the GB300 C ABI.
+
+Names, argument meaning (1-based leg positions, ncon-style index tuples) and error behaviour
+follow the reference (src/SymTensors.jl:26-81); every tensor lives on the device and every
+operation runs as CUDA kernels of ``libmpsgb300.so``.  The only host work is bookkeeping
+metadata and copying flat arrays in or out.
+
+``precision`` arguments select the block-GEMM arithmetic: 0 = FP64 (the reference's Float64
+path), s >= 2 = split precision with s bf16 slices (FP32 accumulation, FP64 epilogue).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import call, i32arr, i64arr, SpaceMismatch, MPSGError
+
+__all__ = [
+    "VectorSpace", "U1Space", "Context", "get_context", "SymTensor", "dual", "zeros", "fill",
+    "from_flat", "from_blocks", "meta", "permutelegs", "fuselegs", "splitleg", "SymMatrix",
+    "matmul", "contract", "contract_flops", "dot", "norm", "axpy", "axpby", "rmul", "mul",
+    "similar", "copy", "fill_", "applymps2site", "applymps2site_flops", "mpsupdateleft",
+    "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision",
+]
+
+
+# ---------------------------------------------------------------------------------------------
+# spaces (src/vspace.jl)
+# ---------------------------------------------------------------------------------------------
+class VectorSpace:
+    """Graded space charge -> dim with an ``isdual`` flag (value type; src/vspace.jl:5-18)."""
+
+    __slots__ = ("sectors", "isdual")
+
+    def __init__(self, pairs, isdual: bool = False):
+        pairs = sorted((int(c), int(d)) for c, d in pairs)
+        for i in range(1, len(pairs)):
+            if pairs[i][0] == pairs[i - 1][0]:
+                raise SpaceMismatch(_lib.ERR_SPACE_MISMATCH, f"duplicate charges! {pairs}")
+        for _, d in pairs:
+            if d <= 0:
+                raise SpaceMismatch(_lib.ERR_SPACE_MISMATCH, "space dimension can only be positive!")
+        self.sectors = tuple(pairs)
+        self.isdual = bool(isdual)
+
+    def charges(self):
+        return [c for c, _ in self.sectors]
+
+    def dims(self):
+        return [d for _, d in self.sectors]
+
+    def dim(self, charge=None) -> int:
+        if charge is None:
+            return sum(self.dims())
+        for c, d in self.sectors:
+            if c == charge:
+                return d
+        return 0
+
+    def __len__(self):
+        return len(self.sectors)
+
+    def __iter__(self):
+        return iter(self.sectors)
+
+    def __eq__(self, other):
+        return (isinstance(other, VectorSpace) and self.sectors == other.sectors
+                and self.isdual == other.isdual)
+
+    def __hash__(self):
+        return hash((self.sectors, self.isdual))
+
+    def __repr__(self):
+        tag = "'" if self.isdual else ""
+        inner = ", ".join(f"{c}{tag}=>{d}" for c, d in self.sectors)
+        return f"U1Space{'†' if self.isdual else ''}({inner})"
+
+
+def U1Space(*pairs, isdual: bool = False) -> VectorSpace:
+    """``U1Space(c=>d, ...)`` (src/vspace.jl:75-76): ``U1Space((0, 1), (1, 2))``."""
+    if len(pairs) == 1 and not isinstance(pairs[0], tuple):
+        pairs = tuple(pairs[0])
+    return VectorSpace(pairs, isdual)
+
+
+def _space_args(spaces):
+    spaces = list(spaces)
+    nsect = [len(V) for V in spaces]
+    charges = [c for V in spaces for c in V.charges()]
+    dims = [d for V in spaces for d in V.dims()]
+    isd = [int(V.isdual) for V in spaces]
+    return len(spaces), i32arr(nsect), i32arr(charges), i64arr(dims), i32arr(isd)
+
+
+# ---------------------------------------------------------------------------------------------
+# context
+# ---------------------------------------------------------------------------------------------
+_DEFAULT_PRECISION = 0
+
+
+def set_default_precision(p: int):
+    """Default block-GEMM arithmetic for calls that do not pass ``precision``."""
+    global _DEFAULT_PRECISION
+    _DEFAULT_PRECISION = int(p)
+
+
+def _prec(p):
+    return _DEFAULT_PRECISION if p is None else int(p)
+
+
+class Context:
+    """One GPU, one CUDA stream and the plan caches of the library."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        call("mpsg_ctx_create", device, C.byref(h))
+        self._h = h
+        self.device = device
+        self._free = _lib.lib.mpsg_ctx_destroy
+
+    @property
+    def handle(self):
+        return self._h
+
+    def synchronize(self):
+        call("mpsg_ctx_synchronize", self._h)
+
+    def counters(self):
+        """(kernel launches, algorithmic GEMM flops) issued so far on this context."""
+        n = C.c_int64()
+        f = C.c_double()
+        call("mpsg_ctx_counters", self._h, C.byref(n), C.byref(f))
+        return n.value, f.value
+
+    def clear_caches(self):
+        call("mpsg_ctx_clear_caches", self._h)
+
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer."""
+        s = C.c_void_p()
+        call("mpsg_ctx_stream", self._h, C.byref(s))
+        return s.value or 0
+
+    KERNEL_KINDS = {"copy": 0, "gemm_f64": 1, "gemm_split": 2, "pack": 3, "vec": 4}
+
+    def set_timing(self, enable: bool):
+        """Bracket every kernel launch with CUDA events (resets the accumulated times)."""
+        call("mpsg_ctx_set_timing", self._h, int(bool(enable)))
+
+    def kernel_time(self, kind: str):
+        """(summed milliseconds, launches, algorithmic flops) of one kernel class since timing
+        was enabled."""
+        ms = C.c_double()
+        n = C.c_int64()
+        f = C.c_double()
+        call("mpsg_ctx_kernel_time", self._h, self.KERNEL_KINDS[kind], C.byref(ms), C.byref(n),
+             C.byref(f))
+        return ms.value, n.value, f.value
+
+    def close(self):
+        if self._h:
+            self._free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_contexts: dict[int, Context] = {}
+
+
+def get_context(device: int = 0) -> Context:
+    if device not in _contexts:
+        _contexts[device] = Context(device)
+    return _contexts[device]
+
+
+# ---------------------------------------------------------------------------------------------
+# tensors (src/symtensor.jl)
+# ---------------------------------------------------------------------------------------------
+class SymTensor:
+    """Device-resident block-sparse tensor.  ``ctx is None`` marks a structure-only tensor
+    (sector table without data), which the planning functions accept on any host."""
+
+    __slots__ = ("_h", "ctx", "_space", "_charge", "_sect", "__weakref__")
+
+    def __init__(self, handle, ctx):
+        self._h = handle
+        self.ctx = ctx
+        self._space = None
+        self._charge = None
+        self._sect = None
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.lib.mpsg_tensor_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def is_meta(self) -> bool:
+        return self.ctx is None
+
+    @property
+    def charge(self) -> int:
+        if self._charge is None:
+            c = C.c_int32()
+            call("mpsg_tensor_charge", self._h, C.byref(c))
+            self._charge = c.value
+        return self._charge
+
+    @property
+    def rank(self) -> int:
+        n = C.c_int32()
+        call("mpsg_tensor_rank", self._h, C.byref(n))
+        return n.value
+
+    @property
+    def space(self):
+        if self._space is None:
+            sp = []
+            for leg in range(1, self.rank + 1):
+                n = C.c_int32()
+                d = C.c_int32()
+                call("mpsg_tensor_space", self._h, leg, C.byref(n), None, None, C.byref(d))
+                ch = (C.c_int32 * n.value)()
+                dm = (C.c_int64 * n.value)()
+                call("mpsg_tensor_space", self._h, leg, None, ch, dm, None)
+                sp.append(VectorSpace(zip(list(ch), list(dm)), bool(d.value)))
+            self._space = tuple(sp)
+        return self._space
+
+    def numel(self) -> int:
+        ne = C.c_int64()
+        call("mpsg_tensor_numel", self._h, None, C.byref(ne))
+        return ne.value
+
+    def nblocks(self) -> int:
+        nb = C.c_int64()
+        call("mpsg_tensor_numel", self._h, C.byref(nb), None)
+        return nb.value
+
+    def size(self):
+        return tuple(V.dim() for V in self.space)
+
+    def _sector_table(self):
+        if self._sect is None:
+            nb, N = self.nblocks(), self.rank
+            lab = (C.c_int32 * max(1, nb * N))()
+            sz = (C.c_int64 * max(1, nb * N))()
+            off = (C.c_int64 * max(1, nb))()
+            call("mpsg_tensor_sectors", self._h, lab, sz, off)
+            L = np.ctypeslib.as_array(lab)[: nb * N].reshape(nb, N) if nb else np.zeros((0, N), int)
+            Z = np.ctypeslib.as_array(sz)[: nb * N].reshape(nb, N) if nb else np.zeros((0, N), int)
+            O = np.ctypeslib.as_array(off)[:nb].copy() if nb else np.zeros(0, int)
+            self._sect = ([tuple(int(x) for x in r) for r in L],
+                          [tuple(int(x) for x in r) for r in Z], [int(o) for o in O])
+        return self._sect
+
+    def sectors(self):
+        """Sector labels in reference order (src/symtensor.jl:87)."""
+        return list(self._sector_table()[0])
+
+    def block_sizes(self):
+        return list(self._sector_table()[1])
+
+    def offsets(self):
+        return list(self._sector_table()[2])
+
+    def isdiagonal(self) -> bool:
+        d = C.c_int32()
+        call("mpsg_tensor_is_diagonal", self._h, C.byref(d))
+        return bool(d.value)
+
+    # -- data movement -------------------------------------------------------------------
+    def to_flat(self) -> np.ndarray:
+        if self.is_meta:
+            raise MPSGError(_lib.ERR_ARGUMENT, "structure-only tensor has no data")
+        n = self.numel()
+        out = np.empty(n, dtype=np.float64)
+        call("mpsg_tensor_download", self._h, out.ctypes.data_as(_lib.PF64), n)
+        return out
+
+    def upload(self, flat):
+        flat = np.ascontiguousarray(flat, dtype=np.float64)
+        call("mpsg_tensor_upload", self._h, flat.ctypes.data_as(_lib.PF64), flat.size)
+        return self
+
+    @property
+    def blocks(self):
+        """Sector -> block (column-major numpy arrays), downloaded from the device."""
+        flat = self.to_flat()
+        out = {}
+        for s, z, o in zip(*self._sector_table()):
+            n = int(np.prod(z))
+            out[s] = flat[o:o + n].reshape(z, order="F")
+        return out
+
+    def __getitem__(self, sector):
+        return self.blocks[tuple(sector)]
+
+    def device_ptr(self) -> int:
+        p = C.c_void_p()
+        call("mpsg_tensor_device_ptr", self._h, C.byref(p))
+        return p.value or 0
+
+    def issimilar(self, other) -> bool:
+        return self.charge == other.charge and self.space == other.space
+
+    # -- operators -----------------------------------------------------------------------
+    def __mul__(self, other):
+        if isinstance(other, SymTensor):
+            return matmul(self, other)
+        out = copy(self)
+        rmul(out, float(other))
+        return out
+
+    __rmul__ = __mul__
+
+    def __repr__(self):
+        kind = "meta " if self.is_meta else ""
+        return f"<{kind}SymTensor charge={self.charge} space={self.space} blocks={self.nblocks()}>"
+
+
+def _wrap(h, ctx):
+    if not h:
+        return None
+    return SymTensor(h, ctx)
+
+
+def _ctx(ctx):
+    return ctx if ctx is not None else get_context()
+
+
+def zeros(charge, space, ctx=None) -> SymTensor:
+    """Zero tensor holding every allowed sector (``fill(0.0, charge, space)``)."""
+    ctx = _ctx(ctx)
+    h = C.c_void_p()
+    call("mpsg_tensor_create", ctx.handle, int(charge), *_space_args(space), C.byref(h))
+    return SymTensor(h, ctx)
+
+
+def fill(x, charge, space, ctx=None) -> SymTensor:
+    """``fill(x, charge, space)`` (src/symtensor.jl:157-164)."""
+    t = zeros(charge, space, ctx)
+    if x != 0:
+        call("mpsg_fill", t.ctx.handle, t.handle, float(x))
+    return t
+
+
+def fill_(A: SymTensor, x) -> SymTensor:
+    """``fill!(A, x)`` (src/symtensor.jl:166-171)."""
+    call("mpsg_fill", A.ctx.handle, A.handle, float(x))
+    return A
+
+
+def meta(charge, space) -> SymTensor:
+    """Structure-only tensor: sector table without data (works without a GPU)."""
+    h = C.c_void_p()
+    call("mpsg_meta_create", int(charge), *_space_args(space), C.byref(h))
+    return SymTensor(h, None)
+
+
+def from_flat(charge, space, flat, ctx=None) -> SymTensor:
+    t = zeros(charge, space, ctx)
+    return t.upload(flat)
+
+
+def from_blocks(charge, space, blocks, ctx=None) -> SymTensor:
+    """Upload a sector -> block mapping; every allowed sector must be present
+    (the SymTensor constructor check, src/symtensor.jl:17-28)."""
+    t = zeros(charge, space, ctx)
+    sects, sizes, offs = t._sector_table()
+    if len(blocks) != len(sects):
+        raise SpaceMismatch(_lib.ERR_SPACE_MISMATCH,
+                            f"SectorMismatch(): {len(blocks)} blocks vs {len(sects)} sectors")
+    flat = np.empty(t.numel(), dtype=np.float64)
+    for s, z, o in zip(sects, sizes, offs):
+        if s not in blocks:
+            raise SpaceMismatch(_lib.ERR_SPACE_MISMATCH, f"SectorMismatch(): missing {s}")
+        b = np.asarray(blocks[s], dtype=np.float64)
+        if tuple(b.shape) != tuple(z):
+            raise SpaceMismatch(_lib.ERR_SPACE_MISMATCH, f"SizeMismatch() at {s}")
+        flat[o:o + b.size] = b.ravel(order="F")
+    return t.upload(flat)
+
+
+def dual(x):
+    """``dual`` of a space or of a tensor (src/vspace.jl:53, src/symtensor.jl:201-212)."""
+    if isinstance(x, VectorSpace):
+        return VectorSpace(x.sectors, not x.isdual)
+    h = C.c_void_p()
+    if x.is_meta:
+        sp = tuple(VectorSpace(V.sectors, not V.isdual) for V in x.space)
+        return meta(-x.charge, sp)
+    call("mpsg_dual", x.ctx.handle, x.handle, C.byref(h))
+    return SymTensor(h, x.ctx)
+
+
+def copy(A: SymTensor) -> SymTensor:
+    h = C.c_void_p()
+    call("mpsg_tensor_copy", A.ctx.handle, A.handle, C.byref(h))
+    return SymTensor(h, A.ctx)
+
+
+def similar(A: SymTensor) -> SymTensor:
+    """``similar(A)`` (src/symtensor.jl:252-255); contents are zero here."""
+    return zeros(A.charge, A.space, A.ctx)
+
+
+# ---------------------------------------------------------------------------------------------
+# releg (src/symreleg.jl) and contraction (src/contract.jl)
+# ---------------------------------------------------------------------------------------------
+def permutelegs(A: SymTensor, perm) -> SymTensor:
+    perm = [int(p) for p in perm]
+    h = C.c_void_p()
+    if A.is_meta:
+        call("mpsg_plan_permutelegs", A.handle, i32arr(perm), C.byref(h))
+    else:
+        call("mpsg_permutelegs", A.ctx.handle, A.handle, i32arr(perm), C.byref(h))
+    return SymTensor(h, A.ctx)
+
+
+def fuselegs(A: SymTensor, l: int, n: int = 2, _dual: bool = False) -> SymTensor:
+    h = C.c_void_p()
+    if A.is_meta:
+        call("mpsg_plan_fuselegs", A.handle, int(l), int(n), int(_dual), C.byref(h))
+    else:
+        call("mpsg_fuselegs", A.ctx.handle, A.handle, int(l), int(n), int(_dual), C.byref(h))
+    return SymTensor(h, A.ctx)
+
+
+def splitleg(A: SymTensor, l: int, space) -> SymTensor:
+    if isinstance(space, VectorSpace):
+        space = (space,)
+    h = C.c_void_p()
+    args = _space_args(space)
+    if A.is_meta:
+        call("mpsg_plan_splitleg", A.handle, int(l), *args, C.byref(h))
+    else:
+        call("mpsg_splitleg", A.ctx.handle, A.handle, int(l), *args, C.byref(h))
+    return SymTensor(h, A.ctx)
+
+
+def SymMatrix(A: SymTensor, rowidxs, colidxs) -> SymTensor:
+    """Permute-fuse into a block-diagonal matrix (src/contract.jl:112-171)."""
+    r = [int(x) for x in rowidxs]
+    c_ = [int(x) for x in colidxs]
+    h = C.c_void_p()
+    if A.is_meta:
+        call("mpsg_plan_symmatrix", A.handle, len(r), i32arr(r), len(c_), i32arr(c_), C.byref(h))
+    else:
+        call("mpsg_symmatrix", A.ctx.handle, A.handle, len(r), i32arr(r), len(c_), i32arr(c_),
+             C.byref(h))
+    return SymTensor(h, A.ctx)
+
+
+def matmul(A: SymTensor, B: SymTensor, precision=None) -> SymTensor:
+    """``A * B`` of two SymMatrix (src/contract.jl:234-298)."""
+    h = C.c_void_p()
+    if A.is_meta:
+        f = C.c_double()
+        call("mpsg_plan_matmul", A.handle, B.handle, C.byref(h), C.byref(f))
+    else:
+        call("mpsg_matmul", A.ctx.handle, A.handle, B.handle, _prec(precision), C.byref(h))
+    return SymTensor(h, A.ctx)
+
+
+def contract(A: SymTensor, idxA, B: SymTensor, idxB, precision=None):
+    """``contract(A, idxA, B, idxB)`` with ncon-style index tuples (src/contract.jl:11-47).
+    Returns a number when every leg is contracted."""
+    ia, ib = i32arr(idxA), i32arr(idxB)
+    if len(idxA) != A.rank or len(idxB) != B.rank:
+        raise MPSGError(_lib.ERR_ARGUMENT, "index tuple length differs from tensor rank")
+    h = C.c_void_p()
+    if A.is_meta:
+        f = C.c_double()
+        call("mpsg_plan_contract", A.handle, ia, B.handle, ib, C.byref(h), C.byref(f))
+        return _wrap(h.value, None)
+    s = C.c_double()
+    call("mpsg_contract", A.ctx.handle, A.handle, ia, B.handle, ib, _prec(precision), C.byref(h),
+         C.byref(s))
+    if not h.value:
+        return s.value
+    return SymTensor(h, A.ctx)
+
+
+def contract_flops(A: SymTensor, idxA, B: SymTensor, idxB) -> float:
+    h = C.c_void_p()
+    f = C.c_double()
+    call("mpsg_plan_contract", A.handle, i32arr(idxA), B.handle, i32arr(idxB), C.byref(h),
+         C.byref(f))
+    _wrap(h.value, None)
+    return f.value
+
+
+# ---------------------------------------------------------------------------------------------
+# effective Hamiltonian and environments (src/apply.jl)
+# ---------------------------------------------------------------------------------------------
+def applymps2site(v, envL, envR, W1, W2, precision=None) -> SymTensor:
+    """``_applymps2site`` (src/apply.jl:93-105)."""
+    h = C.c_void_p()
+    call("mpsg_applymps2site", v.ctx.handle, v.handle, envL.handle, envR.handle, W1.handle,
+         W2.handle, _prec(precision), C.byref(h))
+    return SymTensor(h, v.ctx)
+
+
+def applymps2site_flops(v, envL, envR, W1, W2) -> float:
+    f = C.c_double()
+    call("mpsg_applymps2site_flops", v.ctx.handle, v.handle, envL.handle, envR.handle,
+         W1.handle, W2.handle, C.byref(f))
+    return f.value
+
+
+def mpsupdateleft(env, A, W, precision=None) -> SymTensor:
+    """``_mpsupdateleft`` (src/apply.jl:49-58)."""
+    h = C.c_void_p()
+    call("mpsg_mpsupdateleft", env.ctx.handle, env.handle, A.handle, W.handle, _prec(precision),
+         C.byref(h))
+    return SymTensor(h, env.ctx)
+
+
+def mpsupdateright(env, A, W, precision=None) -> SymTensor:
+    """``_mpsupdateright`` (src/apply.jl:17-25)."""
+    h = C.c_void_p()
+    call("mpsg_mpsupdateright", env.ctx.handle, env.handle, A.handle, W.handle,
+         _prec(precision), C.byref(h))
+    return SymTensor(h, env.ctx)
+
+
+# ---------------------------------------------------------------------------------------------
+# vector operations (src/symtensor.jl:266-323)
+# ---------------------------------------------------------------------------------------------
+def dot(A, B) -> float:
+    out = C.c_double()
+    call("mpsg_dot", A.ctx.handle, A.handle, B.handle, C.byref(out))
+    return out.value
+
+
+def norm(A) -> float:
+    out = C.c_double()
+    call("mpsg_norm", A.ctx.handle, A.handle, C.byref(out))
+    return out.value
+
+
+def axpy(alpha, A, B):
+    call("mpsg_axpy", A.ctx.handle, float(alpha), A.handle, B.handle)
+    return B
+
+
+def axpby(alpha, A, beta, B):
+    call("mpsg_axpby", A.ctx.handle, float(alpha), A.handle, float(beta), B.handle)
+    return B
+
+
+def rmul(A, alpha):
+    call("mpsg_rmul", A.ctx.handle, A.handle, float(alpha))
+    return A
+
+
+def mul(B, A, alpha):
+    call("mpsg_mul", A.ctx.handle, B.handle, A.handle, float(alpha))
+    return B
