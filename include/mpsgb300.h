@@ -121,6 +121,32 @@ int mpsg_mpsupdateleft(mpsg_ctx* ctx, const mpsg_tensor* env, const mpsg_tensor*
 int mpsg_mpsupdateright(mpsg_ctx* ctx, const mpsg_tensor* env, const mpsg_tensor* a,
                         const mpsg_tensor* w, int32_t precision, mpsg_tensor** out); /* :17-25 */
 
+/* ---- factorisations and the Krylov solver -------------------------------------------------- */
+/* _svd_(A) on a rank-2 tensor (src/symtools.jl:1-35): per-sector thin SVD; S is returned as a
+ * diagonal tensor (dense diagonal blocks, mpsg_tensor_is_diagonal = 1). */
+int mpsg_svd(mpsg_ctx* ctx, const mpsg_tensor* a, mpsg_tensor** u, mpsg_tensor** s,
+             mpsg_tensor** v);
+/* svdtrunc(A; maxdim, tol) (src/mpsutils.jl:116-179): keeps the maxdim largest singular values
+ * above the ABSOLUTE tol across all sectors, ties to the first sector (:89-112); tieband > 0
+ * treats values within tieband*max as equal (0 = the reference rule). */
+int mpsg_svdtrunc(mpsg_ctx* ctx, const mpsg_tensor* a, int64_t maxdim, double tol,
+                  double tieband, mpsg_tensor** u, mpsg_tensor** s, mpsg_tensor** v);
+/* truncatedsizes (src/mpsutils.jl:89-112) on host arrays: nsect sectors, lens[i] descending values
+ * each, concatenated in `values`; writes the kept count per sector to ns. */
+int mpsg_truncatedsizes(int32_t nsect, const int64_t* lens, const double* values, int64_t maxdim,
+                        double tol, double tieband, int64_t* ns);
+/* Symmetric eigen-decomposition of a small dense column-major n x n matrix (ascending). */
+int mpsg_small_eigh(int32_t n, const double* a, double* evals, double* evecs);
+/* eigsolve(v -> _applymps2site(v, envL, envR, W1, W2), x0, 1, :SR, ishermitian=true; tol,
+ * krylovdim, maxiter) (src/dmrg.jl:77-82, KrylovKit Lanczos): lowest eigenpair.  Returns
+ * MPSG_OK also when not converged after maxiter restarts (the reference only warns);
+ * *converged reports it. */
+int mpsg_eigsolve_heff2(mpsg_ctx* ctx, const mpsg_tensor* x0, const mpsg_tensor* envl,
+                        const mpsg_tensor* envr, const mpsg_tensor* w1, const mpsg_tensor* w2,
+                        int32_t krylovdim, int32_t maxiter, double tol, int32_t precision,
+                        double* eigenvalue, mpsg_tensor** eigenvector, double* normres,
+                        int32_t* numiter, int32_t* numops, int32_t* converged);
+
 /* ---- structure-only planning (no device memory; usable on hosts without a GPU) ---------- */
 /* A structure-only tensor carries charge, spaces and the sector table but no data; every
  * mpsg_plan_* call returns the structure the matching operation would produce, computed by the

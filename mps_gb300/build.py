@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmpsgb300.so")
 
-SOURCES = ["planner.cpp", "ops.cu", "capi.cu", "kernels_copy.cu", "kernels_f64.cu"]
+SOURCES = ["planner.cpp", "ops.cu", "capi.cu", "kernels_copy.cu", "kernels_f64.cu", "linalg.cu",
+           "krylov.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr", "-I", CSRC]

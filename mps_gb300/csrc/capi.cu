@@ -4,10 +4,14 @@
 #include <sstream>
 
 #include "../../include/mpsgb300.h"
-#include "ops.hpp"
+#include "linalg.hpp"
 
+// The handle holds one reference to the context; device buffers hold the others, so
+// mpsg_ctx_destroy never leaves a live tensor with a dangling stream.
 struct mpsg_ctx {
-  mpsg::Context c;
+  std::shared_ptr<mpsg::Context> owner;
+  mpsg::Context& c;
+  explicit mpsg_ctx(std::shared_ptr<mpsg::Context> p) : owner(std::move(p)), c(*owner) {}
 };
 struct mpsg_tensor {
   mpsg::DeviceTensor t;
@@ -76,14 +80,9 @@ const char* mpsg_last_error(void) { return g_last_error.c_str(); }
 int mpsg_ctx_create(int device, mpsg_ctx** out) {
   return guarded([&] {
     need(out, "out");
-    auto* h = new mpsg_ctx;
-    try {
-      mpsg::context_init(&h->c, device);
-    } catch (...) {
-      delete h;
-      throw;
-    }
-    *out = h;
+    auto c = std::make_shared<mpsg::Context>();
+    mpsg::context_init(c.get(), device);
+    *out = new mpsg_ctx(c);
   });
 }
 
@@ -421,6 +420,90 @@ int mpsg_mpsupdateright(mpsg_ctx* ctx, const mpsg_tensor* env, const mpsg_tensor
     need(w, "w");
     need(out, "out");
     *out = wrap(mpsg::mpsupdateright(&ctx->c, env->t, a->t, w->t, precision));
+  });
+}
+
+int mpsg_svd(mpsg_ctx* ctx, const mpsg_tensor* a, mpsg_tensor** u, mpsg_tensor** s,
+             mpsg_tensor** v) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(u, "u");
+    need(s, "s");
+    need(v, "v");
+    auto R = mpsg::svd_blocks(&ctx->c, a->t, false, 0, 0.0, 0.0);
+    *u = wrap(std::move(R.u));
+    *s = wrap(std::move(R.s));
+    *v = wrap(std::move(R.v));
+  });
+}
+
+int mpsg_svdtrunc(mpsg_ctx* ctx, const mpsg_tensor* a, int64_t maxdim, double tol,
+                  double tieband, mpsg_tensor** u, mpsg_tensor** s, mpsg_tensor** v) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(u, "u");
+    need(s, "s");
+    need(v, "v");
+    auto R = mpsg::svd_blocks(&ctx->c, a->t, true, maxdim, tol, tieband);
+    *u = wrap(std::move(R.u));
+    *s = wrap(std::move(R.s));
+    *v = wrap(std::move(R.v));
+  });
+}
+
+int mpsg_truncatedsizes(int32_t nsect, const int64_t* lens, const double* values, int64_t maxdim,
+                        double tol, double tieband, int64_t* ns) {
+  return guarded([&] {
+    need(lens, "lens");
+    need(values, "values");
+    need(ns, "ns");
+    if (nsect < 1) throw mpsg::Error(mpsg::kErrArgument, "no sectors");
+    std::vector<std::vector<double>> S(nsect);
+    int64_t p = 0;
+    for (int i = 0; i < nsect; ++i) {
+      if (lens[i] < 1) throw mpsg::Error(mpsg::kErrArgument, "empty sector");
+      S[i].assign(values + p, values + p + lens[i]);
+      p += lens[i];
+    }
+    auto r = mpsg::truncatedsizes(S, maxdim, tol, tieband);
+    for (int i = 0; i < nsect; ++i) ns[i] = r[i];
+  });
+}
+
+int mpsg_small_eigh(int32_t n, const double* a, double* evals, double* evecs) {
+  return guarded([&] {
+    need(a, "a");
+    need(evals, "evals");
+    need(evecs, "evecs");
+    if (n < 1) throw mpsg::Error(mpsg::kErrArgument, "n < 1");
+    mpsg::small_eigh(n, a, evals, evecs);
+  });
+}
+
+int mpsg_eigsolve_heff2(mpsg_ctx* ctx, const mpsg_tensor* x0, const mpsg_tensor* envl,
+                        const mpsg_tensor* envr, const mpsg_tensor* w1, const mpsg_tensor* w2,
+                        int32_t krylovdim, int32_t maxiter, double tol, int32_t precision,
+                        double* eigenvalue, mpsg_tensor** eigenvector, double* normres,
+                        int32_t* numiter, int32_t* numops, int32_t* converged) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(x0, "x0");
+    need(envl, "envl");
+    need(envr, "envr");
+    need(w1, "w1");
+    need(w2, "w2");
+    need(eigenvalue, "eigenvalue");
+    need(eigenvector, "eigenvector");
+    auto R = mpsg::eigsolve_heff2(&ctx->c, x0->t, envl->t, envr->t, w1->t, w2->t, krylovdim,
+                                  maxiter, tol, precision);
+    *eigenvalue = R.value;
+    *eigenvector = wrap(std::move(R.vec));
+    if (normres) *normres = R.normres;
+    if (numiter) *numiter = R.numiter;
+    if (numops) *numops = R.numops;
+    if (converged) *converged = R.converged ? 1 : 0;
   });
 }
 

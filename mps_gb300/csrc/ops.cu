@@ -10,12 +10,12 @@ namespace mpsg {
 // context and buffers
 // ------------------------------------------------------------------------------------------
 Buffer::~Buffer() {
-  if (ptr) cudaFreeAsync(ptr, ctx->stream);
+  if (ptr) cudaFreeAsync(ptr, owner->stream);
 }
 
 std::shared_ptr<Buffer> alloc_buffer(Context* ctx, int64_t n) {
   auto b = std::make_shared<Buffer>();
-  b->ctx = ctx;
+  b->owner = ctx->shared_from_this();
   b->n = n;
   if (n > 0) MPSG_CUDA(cudaMallocAsync((void**)&b->ptr, sizeof(double) * n, ctx->stream));
   return b;
@@ -85,6 +85,7 @@ Context::~Context() {
       cudaEventDestroy(ev.b);
     }
   for (auto e : event_pool) cudaEventDestroy(e);
+  if (solver && solver_destroy) solver_destroy(solver);
   if (d_partials) cudaFree(d_partials);
   if (h_pinned) cudaFreeHost(h_pinned);
   if (stream) cudaStreamDestroy(stream);

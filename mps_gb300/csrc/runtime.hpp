@@ -23,9 +23,10 @@ namespace mpsg {
 
 struct Context;
 
-// Stream-ordered device allocation owned by a context.
+// Stream-ordered device allocation.  Every buffer co-owns its context, so the context (stream,
+// caches) outlives the last tensor whatever order a caller releases handles in.
 struct Buffer {
-  Context* ctx = nullptr;
+  std::shared_ptr<Context> owner;
   double* ptr = nullptr;
   int64_t n = 0;
   ~Buffer();
@@ -78,7 +79,7 @@ struct DevReleg {
   ~DevReleg();
 };
 
-struct Context {
+struct Context : std::enable_shared_from_this<Context> {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
@@ -90,6 +91,7 @@ struct Context {
   int64_t kernel_launches = 0;    // launches of this library's kernels
   double gemm_flops = 0;          // algorithmic flops issued through block GEMMs
   void* solver = nullptr;         // cusolverDnHandle_t, created on first SVD
+  void (*solver_destroy)(void*) = nullptr;
   // optional per-kernel-class event timing (see mpsg_ctx_set_timing)
   static constexpr int kKinds = 5;
   bool timing = false;

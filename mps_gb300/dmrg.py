@@ -148,6 +148,180 @@ def heff_problem(chi: int, delta: float = 0.5, seed: int = 1911, ctx=None, meta_
     return v, eL, eR, W, W
 
 
+# ---------------------------------------------------------------------------------------------
+# MPS (src/symmps.jl) and the 2-site DMRG sweep (src/dmrg.jl) on device tensors
+# ---------------------------------------------------------------------------------------------
+class MPState:
+    """``MPState``: site tensors (Vl, d, dual(Vr)) and the orthogonality center (symmps.jl:1-4)."""
+
+    def __init__(self, As, center: int = 0):
+        self.As = list(As)
+        self.center = center
+
+    def __len__(self):
+        return len(self.As)
+
+
+def bond_dims(lx, site, M, chimax):
+    """Charges of the bond right of ``site`` as in src/symmps.jl:59-62 (d = 2), each with
+    dimension min(chimax, #left states, #right states)."""
+    cmin = max(0, M - (lx - site))
+    cmax = min(M, site)
+    return [(c, max(1, min(chimax, math.comb(site, c), math.comb(lx - site, M - c))))
+            for c in range(cmin, cmax + 1)]
+
+
+def random_mps_host(lx: int, M: int, chimax: int, seed: int = 1911):
+    """(charge, spaces, flat) per site of a random U(1) MPS with total charge M: blocks N(0,1)
+    from a Philox stream in reference block order."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    d = U1Space(*SITE)
+    Vl = U1Space((0, 1))
+    out = []
+    for site in range(1, lx + 1):
+        Vr = VectorSpace(bond_dims(lx, site, M, chimax))
+        sp = (Vl, d, dual(Vr))
+        n = mg.meta(0, sp).numel()
+        out.append((0, sp, rng.standard_normal(n)))
+        Vl = Vr
+    return out
+
+
+def mps_from_host(sites, ctx=None) -> MPState:
+    return MPState([mg.from_flat(c, sp, f, ctx) for c, sp, f in sites], center=0)
+
+
+def _pushleft(mps: MPState, l: int):
+    """``_pushleft!`` (src/symmps.jl:167-174), 1-based ``l``."""
+    A = mps.As[l - 1]
+    u, s, v = mg._svd_(mg.fuselegs(A, 2, 2))
+    mps.As[l - 1] = mg.splitleg(v, 2, A.space[1:3])
+    mps.As[l - 2] = mg.contract(mps.As[l - 2], (1, 2, -1), mg.matmul(u, s, precision=0), (-1, 3),
+                                precision=0)
+
+
+def _pushright(mps: MPState, l: int):
+    """``_pushright!`` (src/symmps.jl:176-183)."""
+    A = mps.As[l - 1]
+    u, s, v = mg._svd_(mg.fuselegs(A, 1, 2))
+    mps.As[l - 1] = mg.splitleg(u, 1, A.space[0:2])
+    mps.As[l] = mg.contract(mg.matmul(s, v, precision=0), (1, -1), mps.As[l], (-1, 2, 3),
+                            precision=0)
+
+
+def center_at(mps: MPState, center: int) -> MPState:
+    """``center_at!`` (src/symmps.jl:185-200)."""
+    x1, xL = 1, len(mps)
+    if mps.center > 0:
+        x1 = xL = mps.center
+    for p in range(x1, center):
+        _pushright(mps, p)
+    for p in range(xL, center, -1):
+        _pushleft(mps, p)
+    mps.center = center
+    return mps
+
+
+def initialenv(mps: MPState, Ws, at: int = 1, precision: int = 0):
+    """``initialenv`` (src/dmrg.jl:9-36): boundary environments of ones, then right updates."""
+    if mps.center != at:
+        raise mg.SpaceMismatch(2, f"MPS center has to be {at}")
+    lx = len(mps)
+    ctx = mps.As[0].ctx
+    env = [None] * (lx + 2)
+    lVa = mps.As[0].space[0]
+    rVa = dual(mps.As[-1].space[2])
+    lVw = Ws[0].space[0]
+    rVw = dual(Ws[-1].space[2])
+    env[0] = mg.fill(1.0, 0, (dual(lVa), dual(lVw), lVa), ctx)
+    env[lx + 1] = mg.fill(1.0, 0, (rVa, rVw, dual(rVa)), ctx)
+    for l in range(lx, at - 1, -1):
+        env[l] = mg.mpsupdateright(env[l + 1], mps.As[l - 1], Ws[l - 1], precision=precision)
+    for l in range(1, at):
+        env[l] = mg.mpsupdateleft(env[l - 1], mps.As[l - 1], Ws[l - 1], precision=precision)
+    return env
+
+
+class SweepOptions:
+    """Keyword arguments of ``dmrg2sitesweep!`` (src/dmrg.jl:58-66) plus the precision split:
+    ``precision`` for the Krylov matvecs, ``energy_precision`` for the post-truncation energy
+    matvec (dmrg.jl:92-93) and ``env_precision`` for environment updates."""
+
+    def __init__(self, maxdim=200, tol=1e-9, lanczostol=1e-7, krylovdim=5, krylovmaxiter=8,
+                 tieband=0.0, precision=0, energy_precision=0, env_precision=0):
+        self.maxdim = maxdim
+        self.tol = tol
+        self.lanczostol = lanczostol
+        self.krylovdim = krylovdim
+        self.krylovmaxiter = krylovmaxiter
+        self.tieband = tieband
+        self.precision = precision
+        self.energy_precision = energy_precision
+        self.env_precision = env_precision
+
+
+def _truncate_and_energy(v, AA, env, Ws, l, o: SweepOptions):
+    u, s, vt = mg.svdtrunc(mg.SymMatrix(v, [1, 2], [3, 4]), maxdim=o.maxdim, tol=o.tol,
+                           tieband=o.tieband)
+    ns = mg.norm(s)
+    truncerr = 1.0 - ns
+    mg.rmul(s, 1.0 / ns)
+    usv = mg.matmul(mg.matmul(u, s, precision=0), vt, precision=0)
+    AA = mg.splitleg(mg.splitleg(usv, 2, AA.space[2:4]), 1, AA.space[0:2])
+    e = mg.dot(AA, mg.applymps2site(AA, env[l - 1], env[l + 2], Ws[l - 1], Ws[l],
+                                    precision=o.energy_precision))
+    return u, s, vt, AA, e, truncerr
+
+
+def _eig(AA, env, Ws, l, o: SweepOptions, stats):
+    e, v, info = mg.eigsolve_heff2(AA, env[l - 1], env[l + 2], Ws[l - 1], Ws[l],
+                                   krylovdim=o.krylovdim, maxiter=o.krylovmaxiter,
+                                   tol=o.lanczostol, precision=o.precision)
+    if stats is not None:
+        stats.append(info)
+    return v
+
+
+def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stats=None, **kw):
+    """``dmrg2sitesweep!`` (src/dmrg.jl:58-179): one left-to-right-to-left sweep on the GPU.
+    Returns the reference's energy list (3L-5 post-truncation energies; the right-to-left loop
+    pushes each energy twice, dmrg.jl:132,156)."""
+    o = opts or SweepOptions(**kw)
+    lx = len(mps)
+    if mps.center != 1:
+        raise mg.SpaceMismatch(2, "The center of MPS has to be 1 for dmrg L->R->L")
+    energies = []
+    A = mps.As[0]
+    for l in range(1, lx - 1):
+        AA = mg.contract(A, (1, 2, -1), mps.As[l], (-1, 3, 4), precision=0)
+        v = _eig(AA, env, Ws, l, o, stats)
+        u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o)
+        energies.append(e)
+        mps.As[l - 1] = mg.splitleg(u, 1, A.space[0:2])
+        env[l] = mg.mpsupdateleft(env[l - 1], mps.As[l - 1], Ws[l - 1], precision=o.env_precision)
+        A = mg.splitleg(mg.matmul(s, vt, precision=0), 2, AA.space[2:4])
+    l = lx - 1
+    AA = mg.contract(A, (1, 2, -1), mps.As[l], (-1, 3, 4), precision=0)
+    v = _eig(AA, env, Ws, l, o, stats)
+    e = None
+    for l in range(lx - 1, 1, -1):
+        u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o)
+        energies.append(e)
+        mps.As[l] = mg.splitleg(vt, 2, AA.space[2:4])
+        env[l + 1] = mg.mpsupdateright(env[l + 2], mps.As[l], Ws[l], precision=o.env_precision)
+        A = mg.splitleg(mg.matmul(u, s, precision=0), 1, AA.space[0:2])
+        AA = mg.contract(mps.As[l - 2], (1, 2, -1), A, (-1, 3, 4), precision=0)
+        v = _eig(AA, env, Ws, l - 1, o, stats)
+        energies.append(e)
+    l = 1
+    u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o)
+    energies.append(e)
+    mps.As[1] = mg.splitleg(vt, 2, AA.space[2:4])
+    env[2] = mg.mpsupdateright(env[3], mps.As[1], Ws[1], precision=o.env_precision)
+    mps.As[0] = mg.splitleg(mg.matmul(u, s, precision=0), 1, AA.space[0:2])
+    return energies
+
+
 HEFF_STEPS = (((-1, 2, 1), (-1, 3, 4, 5)), ((1, -1, -2, 4, 5), (-1, 2, 3, -2)),
               ((1, 2, -1, -2, 5), (-1, 3, 4, -2)), ((1, 2, 3, -1, -2), (-2, -1, 4)))
 

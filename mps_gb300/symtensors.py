@@ -23,7 +23,8 @@ __all__ = [
     "from_flat", "from_blocks", "meta", "permutelegs", "fuselegs", "splitleg", "SymMatrix",
     "matmul", "contract", "contract_flops", "dot", "norm", "axpy", "axpby", "rmul", "mul",
     "similar", "copy", "fill_", "applymps2site", "applymps2site_flops", "mpsupdateleft",
-    "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision",
+    "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision", "_svd_",
+    "svdtrunc", "truncatedsizes", "small_eigh", "eigsolve_heff2", "EigInfo",
 ]
 
 
@@ -538,6 +539,76 @@ def mpsupdateright(env, A, W, precision=None) -> SymTensor:
     call("mpsg_mpsupdateright", env.ctx.handle, env.handle, A.handle, W.handle,
          _prec(precision), C.byref(h))
     return SymTensor(h, env.ctx)
+
+
+# ---------------------------------------------------------------------------------------------
+# factorisations and the Krylov solver (src/symtools.jl, src/mpsutils.jl, KrylovKit boundary)
+# ---------------------------------------------------------------------------------------------
+def _svd_(A: SymTensor):
+    """Per-sector thin SVD of a rank-2 tensor (src/symtools.jl:1-35): (u, s, v)."""
+    u, s, v = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    call("mpsg_svd", A.ctx.handle, A.handle, C.byref(u), C.byref(s), C.byref(v))
+    return SymTensor(u, A.ctx), SymTensor(s, A.ctx), SymTensor(v, A.ctx)
+
+
+def svdtrunc(A: SymTensor, maxdim=None, tol: float = 1e-12, tieband: float = 0.0):
+    """``svdtrunc(A; maxdim, tol)`` (src/mpsutils.jl:116-179): absolute ``tol``, global greedy
+    ``maxdim``; ``tieband`` > 0 widens ties (0 = the reference rule)."""
+    if maxdim is None:
+        maxdim = max(A.size())
+    u, s, v = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    call("mpsg_svdtrunc", A.ctx.handle, A.handle, int(maxdim), float(tol), float(tieband),
+         C.byref(u), C.byref(s), C.byref(v))
+    return SymTensor(u, A.ctx), SymTensor(s, A.ctx), SymTensor(v, A.ctx)
+
+
+def truncatedsizes(S, maxdim: int = 200, tol: float = 1e-14, tieband: float = 0.0):
+    """``truncatedsizes`` (src/mpsutils.jl:89-112) of a list of descending value lists."""
+    lens = [len(s) for s in S]
+    vals = [float(x) for s in S for x in s]
+    out = (C.c_int64 * len(S))()
+    call("mpsg_truncatedsizes", len(S), i64arr(lens), (C.c_double * max(1, len(vals)))(*vals),
+         int(maxdim), float(tol), float(tieband), out)
+    return list(out)
+
+
+def small_eigh(A):
+    """Eigen-decomposition of a small symmetric matrix on the host (FP64 Jacobi), ascending."""
+    A = np.asarray(A, dtype=np.float64)
+    n = A.shape[0]
+    a = np.asfortranarray(A)
+    w = np.empty(n)
+    v = np.empty((n, n), order="F")
+    call("mpsg_small_eigh", n, a.ctypes.data_as(_lib.PF64), w.ctypes.data_as(_lib.PF64),
+         v.ctypes.data_as(_lib.PF64))
+    return w, v
+
+
+class EigInfo:
+    """Convergence report of ``eigsolve`` (KrylovKit's ``info``: normres, numiter, numops)."""
+
+    def __init__(self, normres, numiter, numops, converged):
+        self.normres = normres
+        self.numiter = numiter
+        self.numops = numops
+        self.converged = converged
+
+    def __repr__(self):
+        return (f"EigInfo(normres={self.normres:.3e}, numiter={self.numiter}, "
+                f"numops={self.numops}, converged={self.converged})")
+
+
+def eigsolve_heff2(x0, envL, envR, W1, W2, krylovdim=5, maxiter=8, tol=1e-7, precision=None):
+    """``eigsolve(v -> _applymps2site(v, envL, envR, W1, W2), x0, 1, :SR, ishermitian=true)``
+    (src/dmrg.jl:77-82): returns (eigenvalue, eigenvector, info)."""
+    e = C.c_double()
+    x = C.c_void_p()
+    nr = C.c_double()
+    ni, no, cv = C.c_int32(), C.c_int32(), C.c_int32()
+    call("mpsg_eigsolve_heff2", x0.ctx.handle, x0.handle, envL.handle, envR.handle, W1.handle,
+         W2.handle, int(krylovdim), int(maxiter), float(tol), _prec(precision), C.byref(e),
+         C.byref(x), C.byref(nr), C.byref(ni), C.byref(no), C.byref(cv))
+    return e.value, SymTensor(x, x0.ctx), EigInfo(nr.value, ni.value, no.value, bool(cv.value))
 
 
 # ---------------------------------------------------------------------------------------------

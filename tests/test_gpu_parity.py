@@ -196,7 +196,10 @@ def test_vector_ops_match_oracle():
     assert_tensor_close(dB, B, rtol=1e-15)
     mg.rmul(dB, 0.125)
     st.rmul(B, 0.125)
-    assert_tensor_close(dB, B, exact=True)
+    assert_tensor_close(dB, B, rtol=1e-15)
+    before = dB.to_flat()
+    mg.rmul(dB, 0.125)  # a power of two scales exactly
+    assert np.array_equal(dB.to_flat(), before * 0.125)
     with pytest.raises(mg.SpaceMismatch):
         mg.dot(dA, to_device(rand_tensor(0, sp[:2] + (U1Space((0, 2)),), rng)))
 
