@@ -32,6 +32,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "H_eff matvec GFLOP/s at chi=2048 (2-site DMRG hot path)"
 UNIT = "GFLOP/s"
+DEFAULT_SLICES = 3  # split precision used for the headline (0 = FP64)
 
 
 def parse():
@@ -204,7 +205,7 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(ctx.stream())
     prob = gd.heff_problem(args.chi, ctx=ctx)
     flops = mg.applymps2site_flops(*prob)
-    precision = 0 if args.precision is None else args.precision
+    S = DEFAULT_SLICES if args.precision is None else args.precision
     flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     def barrier():
@@ -212,7 +213,15 @@ def run_ours(args):
         if ws > 1:
             torch.distributed.barrier()
 
-    def timed_steps(k, with_kernel_timing=False):
+    # prepared operators (built once per bond in a DMRG sweep); build time reported separately
+    t0 = time.perf_counter()
+    op = mg.Heff2(*prob, precision=S)
+    ctx.synchronize()
+    op_build_ms = (time.perf_counter() - t0) * 1e3
+    op64 = mg.Heff2(*prob, precision=0) if S != 0 else op
+    v = prob[0]
+
+    def timed_steps(o, k, with_kernel_timing=False):
         starts = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
         ends = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
         ctx.set_timing(with_kernel_timing)
@@ -220,21 +229,20 @@ def run_ours(args):
             for i in range(k):
                 flush.zero_()
                 starts[i].record(stream)
-                out = mg.applymps2site(*prob, precision=precision)
+                out = o(v)
                 ends[i].record(stream)
                 del out
         torch.cuda.synchronize()
-        ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-        return ms
+        return [s.elapsed_time(e) for s, e in zip(starts, ends)]
 
-    with torch.cuda.stream(stream):
+    for o in (op, op64):
         for _ in range(args.warmup):
-            out = mg.applymps2site(*prob, precision=precision)
-            del out
+            del_out = o(v)
+            del del_out
     barrier()
     launches0, _ = ctx.counters()
     with ClockSampler(local) as cs:
-        ms = timed_steps(args.steps)
+        ms = timed_steps(op, args.steps)
     launches = ctx.counters()[0] - launches0
     clocks = cs.summary()
     t_local = sum(ms) / len(ms) / 1e3
@@ -245,12 +253,22 @@ def run_ours(args):
         t = float(tt.item())
     value = ws * flops / t / 1e9
 
+    # the plain FP64 drop-in on the same inputs
+    ms64 = timed_steps(op64, max(3, min(args.steps, 10))) if S != 0 else ms
+    t64 = sum(ms64) / len(ms64) / 1e3
+
+    # accuracy of this step against the FP64 drop-in
+    y = op(v).to_flat()
+    y64 = op64(v).to_flat()
+    rel_err = float(np.linalg.norm(y - y64) / np.linalg.norm(y64))
+
     # per-kernel CUDA-event times (second pass over the same steps)
-    timed_steps(args.steps, with_kernel_timing=True)
+    timed_steps(op, args.steps, with_kernel_timing=True)
     kinds = {k: ctx.kernel_time(k) for k in ("copy", "gemm_f64", "gemm_split", "pack")}
     ctx.set_timing(False)
 
-    # end to end through the C ABI with host buffers: H2D of all five inputs, D2H of v'
+    # end to end through the C ABI with host buffers: H2D of all five inputs, the reference-facing
+    # _applymps2site call (operator preparation included), D2H of v'
     host_in = [torch.from_numpy(x.to_flat()).pin_memory() for x in prob]
     host_out = torch.empty(prob[0].numel(), dtype=torch.float64).pin_memory()
     dev = [mg.zeros(x.charge, x.space, ctx) for x in prob]
@@ -263,7 +281,7 @@ def run_ours(args):
         for d, h in zip(dev, host_in):
             mg._lib.call("mpsg_tensor_upload", d.handle,
                          mg._lib.C.cast(h.data_ptr(), mg._lib.PF64), h.numel())
-        r = mg.applymps2site(*dev, precision=precision)
+        r = mg.applymps2site(*dev, precision=S)
         mg._lib.call("mpsg_tensor_download", r.handle,
                      mg._lib.C.cast(host_out.data_ptr(), mg._lib.PF64), host_out.numel())
         t1 = time.perf_counter()
@@ -273,9 +291,9 @@ def run_ours(args):
     e2e_value = ws * flops / statistics.mean(e2e_t) / 1e9
 
     peaks = measured_peaks()
-    if precision == 0:
+    step_ms = sum(ms) / len(ms)
+    if S == 0:
         gem_ms, gem_n, gem_f = kinds["gemm_f64"]
-        # FP64 peak: cuBLAS DGEMM measured now on this GPU (the driver's peaks file has none)
         a = torch.randn(8192, 8192, dtype=torch.float64, device=f"cuda:{local}")
         torch.matmul(a, a)
         torch.cuda.synchronize()
@@ -288,23 +306,26 @@ def run_ours(args):
         peak = 3 * 2 * 8192 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
         peak_src = "cuBLAS DGEMM 8192^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)"
         del a
-        pipe = "fp64"
-        dtype = "f64"
+        pipe, dtype = "fp64", "f64"
+        achieved = gem_f / (gem_ms / 1e3) / 1e12 if gem_n else None
+        kernel_desc = "grouped FP64 block GEMM (one launch per contraction)"
     else:
         gem_ms, gem_n, gem_f = kinds["gemm_split"]
         peak = peaks["bf16_tflops"] if peaks else 1900.0
         peak_src = "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback 1.9 PFLOP/s"
-        pipe = "bf16-tensor"
-        dtype = f"bf16x{precision}-split (fp32 accumulate, f64 epilogue)"
-    # algorithmic flops of the timed GEMM launches / their summed CUDA-event durations
-    achieved = gem_f / (gem_ms / 1e3) / 1e12 if gem_n else None
-    roof = {"bound": "tensor", "pipe": pipe, "kernel": "grouped block GEMM (one launch per "
-            "contraction)", "launches_timed": gem_n,
+        pipe = "bf16-tensor (tcgen05)"
+        dtype = f"f64 via {S} bf16 slices ({S * (S + 1) // 2} tcgen05 products, fp32 TMEM accumulate)"
+        # achieved counts ALGORITHMIC flops (the reference's contraction order), not the
+        # executed slice products
+        achieved = flops * args.steps / (gem_ms / 1e3) / 1e12 if gem_n else None
+        kernel_desc = ("split-precision grouped block GEMM (2 launches per H_eff application; "
+                       "achieved = reference-order algorithmic flops / summed GEMM time)")
+    roof = {"bound": "tensor", "pipe": pipe, "kernel": kernel_desc, "launches_timed": gem_n,
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": (achieved / peak) if achieved else None, "peak_source": peak_src,
-            "traffic": profile_traffic(f"gemm_p{precision}_chi{args.chi}")}
-    step_ms = sum(ms) / len(ms)
-    share = {k: round(v[0] / args.steps / step_ms, 4) for k, v in kinds.items() if v[1]}
+            "frac": (achieved / peak) if achieved else None, "peak_source": peak_src + " (of measured)"
+            if peaks else peak_src,
+            "traffic": profile_traffic(f"gemm_p{S}_chi{args.chi}")}
+    share = {k: round(v_[0] / args.steps / step_ms, 4) for k, v_ in kinds.items() if v_[1]}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -313,9 +334,13 @@ def run_ours(args):
         "data": "synthetic (seeded Philox N(0,1) blocks)",
         "config": {"workload": f"H_eff matvec, XXZ Delta=0.5, chi={args.chi} on both bonds, "
                                "25 charges binomial profile, d=2, MPO bond 5",
-                   "chi": args.chi, "precision": precision, "gflop_per_step": flops / 1e9,
+                   "chi": args.chi, "precision_slices": S, "gflop_per_step": flops / 1e9,
+                   "op_build_ms": op_build_ms,
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "flushed before every timed step (512 MiB write)"},
+        "fp64": {"value": ws * flops / t64 / 1e9, "unit": UNIT, "ms_per_step": t64 * 1e3,
+                 "speedup_mixed_vs_fp64": t64 / t},
+        "rel_err_vs_fp64": rel_err,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
@@ -325,8 +350,8 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
         os.environ.setdefault("OPENBLAS_NUM_THREADS", str(os.cpu_count() or 1))
-        v, n, tm, cores = cpu_heff_rate(args.chi, flops)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+        vv, n, tm, cores = cpu_heff_rate(args.chi, flops)
+        line["cpu_baseline"] = {"value": vv, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"{n} full H_eff matvecs of the same workload "
                                           f"({tm:.2f} s each), NumPy/OpenBLAS oracle"}
     if rank == 0:

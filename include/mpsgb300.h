@@ -170,6 +170,20 @@ int mpsg_plan_contract(const mpsg_tensor* a, const int32_t* idxa, const mpsg_ten
 int mpsg_plan_contract_tasks(const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
                              const int32_t* idxb, int64_t* copy_tasks, int64_t* gemm_tasks);
 
+/* ---- prepared two-site effective Hamiltonian ---------------------------------------------- */
+/* The matvec closure v -> _applymps2site(v, envL, envR, W1, W2) of src/dmrg.jl:77 as an object
+ * that is built once per bond and applied many times.  precision 0 runs the reference's four
+ * FP64 contractions; precision S >= 2 folds W1 into envL and W2 into envR once and applies
+ * H_eff as two split-precision tensor-core GEMMs whose constant operands are sliced once. */
+typedef struct mpsg_heff mpsg_heff;
+int mpsg_heff2_create(mpsg_ctx* ctx, const mpsg_tensor* v_like, const mpsg_tensor* envl,
+                      const mpsg_tensor* envr, const mpsg_tensor* w1, const mpsg_tensor* w2,
+                      int32_t precision, mpsg_heff** out);
+int mpsg_heff2_apply(mpsg_ctx* ctx, mpsg_heff* op, const mpsg_tensor* v, mpsg_tensor** out);
+/* Algorithmic flops of one application in the reference contraction order. */
+int mpsg_heff2_flops(const mpsg_heff* op, double* flops);
+int mpsg_heff2_free(mpsg_heff* op);
+
 /* ---- vector operations used by the Krylov solver (src/symtensor.jl:252-323) -------------- */
 int mpsg_fill(mpsg_ctx* ctx, mpsg_tensor* a, double x);                          /* :166-171 */
 int mpsg_rmul(mpsg_ctx* ctx, mpsg_tensor* a, double alpha);                      /* :280-285 */

@@ -89,6 +89,10 @@ SIGNATURES = {
     "mpsg_small_eigh": [I32, PF64, PF64, PF64],
     "mpsg_eigsolve_heff2": [P, P, P, P, P, P, I32, I32, F64, I32, PF64, PP, PF64, PI32, PI32,
                             PI32],
+    "mpsg_heff2_create": [P, P, P, P, P, P, I32, PP],
+    "mpsg_heff2_apply": [P, P, P, PP],
+    "mpsg_heff2_flops": [P, PF64],
+    "mpsg_heff2_free": [P],
     "mpsg_meta_create": [I32, I32, PI32, PI32, PI64, PI32, PP],
     "mpsg_plan_permutelegs": [P, PI32, PP],
     "mpsg_plan_fuselegs": [P, I32, I32, I32, PP],

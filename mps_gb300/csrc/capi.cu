@@ -507,6 +507,55 @@ int mpsg_eigsolve_heff2(mpsg_ctx* ctx, const mpsg_tensor* x0, const mpsg_tensor*
   });
 }
 
+struct mpsg_heff {
+  std::shared_ptr<mpsg::HeffOp> op;
+};
+
+int mpsg_heff2_create(mpsg_ctx* ctx, const mpsg_tensor* v_like, const mpsg_tensor* envl,
+                      const mpsg_tensor* envr, const mpsg_tensor* w1, const mpsg_tensor* w2,
+                      int32_t precision, mpsg_heff** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(v_like, "v_like");
+    need(envl, "envl");
+    need(envr, "envr");
+    need(w1, "w1");
+    need(w2, "w2");
+    need(out, "out");
+    auto h = new mpsg_heff;
+    try {
+      h->op = mpsg::heff_create(&ctx->c, v_like->t.meta, envl->t, envr->t, w1->t, w2->t,
+                                precision);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int mpsg_heff2_apply(mpsg_ctx* ctx, mpsg_heff* op, const mpsg_tensor* v, mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(op, "op");
+    need(v, "v");
+    need(out, "out");
+    *out = wrap(mpsg::heff_apply(*op->op, v->t));
+  });
+}
+
+int mpsg_heff2_flops(const mpsg_heff* op, double* flops) {
+  return guarded([&] {
+    need(op, "op");
+    need(flops, "flops");
+    *flops = op->op->ref_flops;
+  });
+}
+
+int mpsg_heff2_free(mpsg_heff* op) {
+  return guarded([&] { delete op; });
+}
+
 static mpsg_tensor* meta_only(const mpsg::TensorMeta& m) {
   mpsg::DeviceTensor t;
   t.meta = m;

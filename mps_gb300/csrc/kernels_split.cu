@@ -1,0 +1,807 @@
+// Split-precision grouped block GEMM on the 5th-generation tensor cores (tcgen05 + TMEM + TMA).
+//
+// C (FP64) = A (FP64) * B (FP64) for every sector GEMM of a contraction, computed from bf16
+// slices of the operands (an error-free splitting in the style of Ozaki et al.):
+//
+//   * Packing.  Every row i of A (and every column j of B) is cut into K-chunks of `chunk`
+//     columns.  With e(i,c) the power-of-two bound of row i in chunk c and R(i) = max_c e(i,c),
+//     the chunk is written as a fixed-point integer F with beta*S fraction bits relative to
+//     2^e(i,c), and F is split into S balanced base-2^beta digits t_0..t_{S-1}
+//     (|t_0| <= 2^beta, |t_p| <= 2^(beta-1)); slice p stores t_p * 2^(e(i,c)-R(i)-beta(p+1)),
+//     exactly representable in bf16.  All of this is integer arithmetic on the FP64 bit
+//     pattern: GB300 executes FP64 at a small fraction of its FP32 rate.
+//   * MMA.  For every slice pair (p, q) with p + q < S, tcgen05.mma (M=128, N=64, K=16, bf16
+//     in, FP32 out) accumulates into TMEM accumulator g = p + q.  Within one chunk every product
+//     of group g is an integer multiple of one power of two and the sum stays below 2^24 units
+//     (pairs(g) * chunk * 2^(2 beta) <= 2^24), so the FP32 accumulation is exact.
+//   * Epilogue.  After each chunk the 4 epilogue warps drain the S accumulators (tcgen05.ld)
+//     into a double-single (hi, lo) FP32 pair per output element (TwoSum, exact up to 2^-48),
+//     release TMEM to the MMA warp (double-buffered), and after the last chunk assemble
+//     (hi + lo) * 2^(R(i) + C(j)) as an FP64 number with integer instructions only.
+//
+// Accuracy: slicing error <= 2^(-beta*S) relative to the row/column scale, so S = 2 is the
+// classic "bf16x3" (3 products), S = 3 gives about 21 bits (6 products), S = 4 about 28 bits.
+//
+// Kernel layout: persistent, one CTA per SM, 6 warps: warp 0 = TMA producer (one elected
+// thread, cp.async.bulk.tensor 3-d loads of pre-packed K-major tiles with 128B swizzle), warp 1
+// = TMEM allocator + MMA issuer (one thread), warps 2-5 = epilogue (one TMEM lane per thread).
+// Every mbarrier wait is bounded (clock64 budget); on timeout the kernel records an error code,
+// stops issuing work, waits for its own MMAs and frees TMEM before returning.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "split.hpp"
+
+namespace mpsg {
+namespace split {
+
+// ------------------------------------------------------------------------------------------
+// device helpers (inline PTX)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok;
+}
+
+constexpr long long kWaitCycles = 4000000000LL;  // about 2 s at the maximum SM clock
+
+// Bounded wait on a barrier phase; returns false (and raises the abort flag) on timeout or when
+// another role already aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          int* err, int code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (clock64() - t0 > kWaitCycles) {
+      *abort_flag = 1;
+      atomicCAS(err, 0, code);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// 32 consecutive FP32 columns of one TMEM lane per thread (shape 32x32b, 32 repetitions)
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand tile, 128-byte swizzle, 8-row groups 1024 B
+// apart (stride byte offset), base 1024-byte aligned.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset
+  d |= (uint64_t)1 << 46;                    // descriptor version
+  d |= (uint64_t)2 << 61;                    // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, bf16 A and B, both K-major.
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+// (hi + lo) * 2^E as FP64 using integer instructions only (hi, lo normal or zero FP32 values
+// with |lo| <= |hi|).  Bits below 2^-62 of |hi| are truncated.
+__device__ __forceinline__ double ds_to_f64(float hi, float lo, int E) {
+  if (hi == 0.f) {
+    hi = lo;
+    lo = 0.f;
+    if (hi == 0.f) return 0.0;
+  }
+  const uint32_t uh = __float_as_uint(hi), ul = __float_as_uint(lo);
+  const int eh = (int)((uh >> 23) & 0xff);
+  const int el = (int)((ul >> 23) & 0xff);
+  long long mh = (long long)((uh & 0x7fffffu) | (eh ? 0x800000u : 0u));
+  if (uh >> 31) mh = -mh;
+  long long I = mh << 38;  // value = I * 2^(eh - 150 - 38)
+  if (lo != 0.f) {
+    long long ml = (long long)((ul & 0x7fffffu) | (el ? 0x800000u : 0u));
+    if (ul >> 31) ml = -ml;
+    const int d = 38 - (eh - el);
+    if (d >= 0) I += ml << d;
+    else if (d > -63) I += ml >> (-d);
+  }
+  if (I == 0) return 0.0;
+  const unsigned long long sign = I < 0 ? (1ull << 63) : 0ull;
+  unsigned long long A = I < 0 ? (unsigned long long)(-I) : (unsigned long long)I;
+  const int lz = __clzll((long long)A);
+  A <<= lz;  // bit 63 set
+  unsigned long long mant = A >> 11;
+  const unsigned long long rest = A & 0x7ffull;
+  if ((rest > 0x400ull) || (rest == 0x400ull && (mant & 1ull))) mant += 1;  // round to nearest
+  int shift = 0;
+  if (mant >> 53) {
+    mant >>= 1;
+    shift = 1;
+  }
+  // value = mant * 2^(63 - lz - 52 + shift) * 2^(eh - 188 + E - 11 + 11)
+  const long long bexp = (long long)63 - lz + shift + (eh - 188) + E + 1023;
+  if (bexp <= 0) return 0.0;  // below the normal range: negligible at this accuracy
+  if (bexp >= 2047) return __longlong_as_double((long long)(sign | (0x7ffull << 52)));
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)bexp << 52) | (mant & ((1ull << 52) - 1))));
+}
+
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float bv = __fsub_rn(s, hi);
+  const float av = __fsub_rn(s, bv);
+  const float err = __fadd_rn(__fsub_rn(hi, av), __fsub_rn(x, bv));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+
+__device__ __forceinline__ int find_problem(const int64_t* __restrict__ prefix, int n, int64_t t) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ------------------------------------------------------------------------------------------
+// packing kernels
+// ------------------------------------------------------------------------------------------
+// Operand view: element (r, k) of problem p at base[off + r*rs + k*ks]; A uses rows = M,
+// (rs, ks) = (1, lda); B uses rows = N, (rs, ks) = (ldb, 1).
+__device__ __forceinline__ void operand_geom(const Problem& P, int is_b, int64_t& rows,
+                                             int64_t& off, int64_t& rs, int64_t& ks) {
+  if (!is_b) {
+    rows = P.M;
+    off = P.offA;
+    rs = 1;
+    ks = P.lda;
+  } else {
+    rows = P.N;
+    off = P.offB;
+    rs = P.ldb;
+    ks = 1;
+  }
+}
+
+__device__ __forceinline__ int exp_bound(unsigned long long absbits) {
+  // smallest e with |x| < 2^e for the largest |x| (0 when every value is 0)
+  if (absbits == 0) return 0;
+  const int eb = (int)(absbits >> 52);
+  return (eb == 0 ? -1022 : eb - 1023) + 1;
+}
+
+// One thread per operand row: chunk exponents e(r,c) and the row reference R(r) = max_c e(r,c).
+__global__ void pack_exponents_kernel(const Problem* __restrict__ probs,
+                                      const int64_t* __restrict__ row_prefix, int nprob,
+                                      int64_t nrows, int is_b, int chunk,
+                                      const double* __restrict__ X, int16_t* __restrict__ E,
+                                      int32_t* __restrict__ R) {
+  for (int64_t gr = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; gr < nrows;
+       gr += (int64_t)gridDim.x * blockDim.x) {
+    const int p = find_problem(row_prefix, nprob, gr);
+    const Problem P = probs[p];
+    const int64_t r = gr - row_prefix[p];
+    int64_t rows, off, rs, ks;
+    operand_geom(P, is_b, rows, off, rs, ks);
+    const int64_t rbase = is_b ? P.rB : P.rA;
+    const int64_t ebase = is_b ? P.eB : P.eA;
+    const int nch = P.nch;
+    int Rr = -100000;
+    bool any = false;
+    for (int c = 0; c < nch; ++c) {
+      unsigned long long m = 0;
+      const int64_t k0 = (int64_t)c * chunk, k1 = min((int64_t)(c + 1) * chunk, P.K);
+      for (int64_t k = k0; k < k1; ++k) {
+        const unsigned long long b =
+            (unsigned long long)__double_as_longlong(X[off + r * rs + k * ks]) &
+            0x7fffffffffffffffull;
+        m = b > m ? b : m;
+      }
+      const int e = exp_bound(m);
+      E[ebase + r * nch + c] = (int16_t)e;
+      if (m) {
+        Rr = any ? max(Rr, e) : e;
+        any = true;
+      }
+    }
+    R[rbase + r] = any ? Rr : 0;
+  }
+}
+
+// One CTA per packed tile (rows_per_tile x 64 K).  Writes S slices, row-major 128-byte rows.
+template <int S>
+__global__ void __launch_bounds__(256) pack_slices_kernel(
+    const Problem* __restrict__ probs, const int64_t* __restrict__ tile_prefix, int nprob,
+    int64_t ntiles, int is_b, int chunk, int rows_per_tile, int64_t rows_total,
+    const double* __restrict__ X, const int16_t* __restrict__ E, const int32_t* __restrict__ R,
+    __nv_bfloat16* __restrict__ out) {
+  constexpr int kBeta = kSliceBits;
+  extern __shared__ double pack_smem[];  // [128][65] doubles, dynamic (above the static limit)
+  double(*tile)[65] = reinterpret_cast<double(*)[65]>(pack_smem);
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int p = find_problem(tile_prefix, nprob, t);
+    const Problem P = probs[p];
+    const int64_t lt = t - tile_prefix[p];
+    const int64_t ri = lt / P.nks, kstep = lt % P.nks;
+    int64_t rows, off, rs, ks;
+    operand_geom(P, is_b, rows, off, rs, ks);
+    const int64_t r0 = ri * rows_per_tile, k0 = kstep * 64;
+    // stage the FP64 tile in shared memory, coalesced along the contiguous axis
+    if (rs == 1) {
+      for (int i = threadIdx.x; i < rows_per_tile * 64; i += 256) {
+        const int rr = i % rows_per_tile, kk = i / rows_per_tile;
+        const int64_t r = r0 + rr, k = k0 + kk;
+        tile[rr][kk] = (r < rows && k < P.K) ? X[off + r * rs + k * ks] : 0.0;
+      }
+    } else {
+      for (int i = threadIdx.x; i < rows_per_tile * 64; i += 256) {
+        const int kk = i % 64, rr = i / 64;
+        const int64_t r = r0 + rr, k = k0 + kk;
+        tile[rr][kk] = (r < rows && k < P.K) ? X[off + r * rs + k * ks] : 0.0;
+      }
+    }
+    __syncthreads();
+    const int64_t rbase = is_b ? P.rB : P.rA;
+    const int64_t ebase = is_b ? P.eB : P.eA;
+    const int c = (int)(k0 / chunk);
+    const int64_t tile_row0 = (is_b ? P.tB : P.tA) * rows_per_tile + lt * rows_per_tile;
+    for (int i = threadIdx.x; i < rows_per_tile * 8; i += 256) {
+      const int g8 = i % 8, rr = i / 8;
+      const int64_t r = r0 + rr;
+      int e = 0, Rr = 0;
+      if (r < rows) {
+        e = E[ebase + r * P.nch + c];
+        Rr = R[rbase + r];
+      }
+      uint32_t packed[S][4];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const long long bits = __double_as_longlong(tile[rr][g8 * 8 + j]);
+        long long F = 0;
+        const int eb = (int)((bits >> 52) & 0x7ff);
+        if (eb != 0 && r < rows) {
+          const unsigned long long mant = ((unsigned long long)bits & ((1ull << 52) - 1)) |
+                                          (1ull << 52);
+          const int sh = eb - 1075 + kBeta * S - e;
+          unsigned long long f;
+          if (sh >= 0) f = mant << sh;
+          else if (sh > -64) f = (mant + (1ull << (-sh - 1))) >> (-sh);
+          else f = 0;
+          F = bits < 0 ? -(long long)f : (long long)f;
+        }
+#pragma unroll
+        for (int q = 0; q < S; ++q) {
+          const int shq = kBeta * (S - 1 - q);
+          long long tq;
+          if (shq > 0) tq = (F + (1ll << (shq - 1))) >> shq;
+          else tq = F;
+          F -= tq << shq;
+          // slice value t_q * 2^(e - R - beta (q+1))
+          int k = e - Rr - kBeta * (q + 1);
+          float v = (float)tq;
+          if (k < -126) {
+            v *= 1.1754943508222875e-38f;  // 2^-126
+            k += 126;
+            k = max(k, -126);
+          }
+          v *= __uint_as_float((uint32_t)(k + 127) << 23);
+          const uint16_t h = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+          if (j & 1) packed[q][j >> 1] |= (uint32_t)h << 16;
+          else packed[q][j >> 1] = (uint32_t)h;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        uint4 w = make_uint4(packed[q][0], packed[q][1], packed[q][2], packed[q][3]);
+        const int64_t idx = ((int64_t)q * rows_total + tile_row0 + rr) * 64 + g8 * 8;
+        *reinterpret_cast<uint4*>(out + idx) = w;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// the GEMM kernel
+// ------------------------------------------------------------------------------------------
+template <int S>
+struct Cfg {
+  static constexpr int kPairs = S * (S + 1) / 2;
+  static constexpr int kChunkSteps = (1024 / S) / BK;
+  static constexpr int kABytes = BM * BK * 2;
+  static constexpr int kBBytes = BN * BK * 2;
+  static constexpr int kStageBytes = S * (kABytes + kBBytes);
+  static constexpr int kStages = (220 * 1024) / kStageBytes > 4 ? 4 : (220 * 1024) / kStageBytes;
+  static constexpr int kAccCols = S * BN;
+  static constexpr int kBufs = (2 * kAccCols <= 512) ? 2 : 1;
+  static constexpr int kTmemCols = (kBufs * kAccCols <= 128) ? 128
+                                   : (kBufs * kAccCols <= 256) ? 256 : 512;
+  static constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+};
+
+template <int S>
+__global__ void __launch_bounds__(192, 1) split_gemm_kernel(
+    const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+    const Problem* __restrict__ probs, const int64_t* __restrict__ tile_prefix, int nprob,
+    int64_t ntiles, const int32_t* __restrict__ RA, const int32_t* __restrict__ CB,
+    double* __restrict__ C, int* __restrict__ err) {
+  using CF = Cfg<S>;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = (uint64_t*)(smem + CF::kStages * CF::kStageBytes);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + CF::kStages;
+  uint64_t* tfull = bars + 2 * CF::kStages;
+  uint64_t* tempty = tfull + 2;
+  uint64_t* drain = tempty + 2;
+  uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < CF::kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 128);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, CF::kTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+        const int p = find_problem(tile_prefix, nprob, t);
+        const Problem& P = probs[p];
+        const int64_t lt = t - tile_prefix[p];
+        const int64_t mi = lt % P.mt, ni = lt / P.mt;
+        for (int ks = 0; ks < P.nks; ++ks) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) break;
+          uint8_t* sA = smem + stage * CF::kStageBytes;
+          uint8_t* sB = sA + S * CF::kABytes;
+          mbar_expect_tx(&full[stage], CF::kStageBytes);
+          const int rowA = (int)((P.tA + mi * P.nks + ks) * BM);
+          const int rowB = (int)((P.tB + ni * P.nks + ks) * BN);
+#pragma unroll
+          for (int s = 0; s < S; ++s) tma_load_3d(sA + s * CF::kABytes, &tmA, &full[stage], 0, rowA, s);
+#pragma unroll
+          for (int s = 0; s < S; ++s) tma_load_3d(sB + s * CF::kBBytes, &tmB, &full[stage], 0, rowB, s);
+          if (++stage == CF::kStages) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc = make_idesc(BM, BN);
+      int stage = 0;
+      uint32_t phase = 0;
+      int64_t use = 0;
+      bool issued = false;
+      for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+        const int p = find_problem(tile_prefix, nprob, t);
+        const Problem& P = probs[p];
+        for (int c0 = 0; c0 < P.nks && !*abort_flag; c0 += CF::kChunkSteps) {
+          const int buf = (int)(use % CF::kBufs);
+          const uint32_t bph = (uint32_t)((use / CF::kBufs) & 1);
+          if (!mbar_wait(&tempty[buf], bph ^ 1, abort_flag, err, 2)) break;
+          tc_fence_after();
+          uint32_t init = 0;  // bit g: accumulator g already written in this chunk
+          const int c1 = min(P.nks, c0 + CF::kChunkSteps);
+          for (int ks = c0; ks < c1; ++ks) {
+            if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) break;
+            tc_fence_after();
+            const uint32_t sA = smem_u32(smem + stage * CF::kStageBytes);
+            const uint32_t sB = sA + S * CF::kABytes;
+#pragma unroll
+            for (int pa = 0; pa < S; ++pa) {
+#pragma unroll
+              for (int qb = 0; qb < S - pa; ++qb) {
+                const int g = pa + qb;
+                const uint32_t dcol = tmem_base + (uint32_t)((buf * S + g) * BN);
+                const uint64_t ad = sw128_desc(sA + pa * CF::kABytes);
+                const uint64_t bd = sw128_desc(sB + qb * CF::kBBytes);
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                  umma_bf16(dcol, ad + 2 * kk, bd + 2 * kk, idesc, (init >> g) & 1u);
+                  init |= 1u << g;
+                }
+              }
+            }
+            umma_commit(&empty[stage]);
+            issued = true;
+            if (++stage == CF::kStages) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+          umma_commit(&tfull[buf]);
+          ++use;
+        }
+      }
+      if (issued) {  // make sure every MMA has retired before TMEM is released
+        umma_commit(drain);
+        volatile int no_abort = 0;
+        mbar_wait(drain, 0, &no_abort, err, 4);
+      }
+    }
+  } else {
+    // ---------------- epilogue: warps 2..5 ----------------
+    const int lrow = 32 * (warp & 3) + lane;
+    const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
+    int64_t use = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int p = find_problem(tile_prefix, nprob, t);
+      const Problem& P = probs[p];
+      const int64_t lt = t - tile_prefix[p];
+      const int64_t mi = lt % P.mt, ni = lt / P.mt;
+      float hi[BN], lo[BN];
+#pragma unroll
+      for (int j = 0; j < BN; ++j) {
+        hi[j] = 0.f;
+        lo[j] = 0.f;
+      }
+      bool ok = true;
+      for (int c0 = 0; c0 < P.nks; c0 += CF::kChunkSteps) {
+        const int buf = (int)(use % CF::kBufs);
+        const uint32_t bph = (uint32_t)((use / CF::kBufs) & 1);
+        if (!mbar_wait(&tfull[buf], bph, abort_flag, err, 5)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int h = 0; h < BN / 32; ++h) {
+#pragma unroll
+          for (int g = 0; g < S; ++g) {
+            uint32_t v[32];
+            tmem_ld32(tmem_base + lane_addr + (uint32_t)((buf * S + g) * BN + h * 32), v);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) two_sum_acc(hi[h * 32 + j], lo[h * 32 + j], __uint_as_float(v[j]));
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(&tempty[buf]);
+        ++use;
+      }
+      if (!ok) break;
+      const int64_t row = mi * BM + lrow;
+      if (row < P.M) {
+        const int Rr = RA[P.rA + row];
+        double* Cp = C + P.offC + row;
+#pragma unroll
+        for (int j = 0; j < BN; ++j) {
+          const int64_t col = ni * BN + j;
+          if (col < P.N) Cp[col * P.ldc] = ds_to_f64(hi[j], lo[j], Rr + CB[P.rB + col]);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem_base, CF::kTmemCols);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    MPSG_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                               cudaEnableDefault, &q));
+    if (!p || q != cudaDriverEntryPointSuccess)
+      throw Error(kErrCuda, "cuTensorMapEncodeTiled is not available");
+    fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+static void make_map(CUtensorMap* map, void* base, int64_t rows_total, int S, int box_rows) {
+  cuuint64_t gdim[3] = {64, (cuuint64_t)rows_total, (cuuint64_t)S};
+  cuuint64_t gstride[2] = {128, (cuuint64_t)rows_total * 128};
+  cuuint32_t box[3] = {64, (cuuint32_t)box_rows, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, gdim, gstride, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error(kErrCuda, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+int chunk_for(int S) { return ((1024 / S) / BK) * BK; }
+
+void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
+  release();
+  S = S_;
+  if (S < 2 || S > 4) throw Error(kErrUnsupported, "split precision supports 2..4 slices");
+  const int chunk = chunk_for(S);
+  probs.clear();
+  int64_t tA = 0, tB = 0, rA = 0, rB = 0, eA = 0, eB = 0;
+  std::vector<int64_t> tile_prefix(1, 0), packA_prefix(1, 0), packB_prefix(1, 0),
+      rowA_prefix(1, 0), rowB_prefix(1, 0);
+  flops = 0;
+  for (const GemmTask& t : g) {
+    Problem P;
+    P.M = t.M;
+    P.N = t.N;
+    P.K = t.K;
+    P.offA = t.offA;
+    P.offB = t.offB;
+    P.offC = t.offC;
+    P.lda = t.lda;
+    P.ldb = t.ldb;
+    P.ldc = t.ldc;
+    P.mt = (int)((t.M + BM - 1) / BM);
+    P.nt = (int)((t.N + BN - 1) / BN);
+    P.nks = (int)((t.K + BK - 1) / BK);
+    P.nch = (int)((t.K + chunk - 1) / chunk);
+    P.tA = tA;
+    P.tB = tB;
+    P.rA = rA;
+    P.rB = rB;
+    P.eA = eA;
+    P.eB = eB;
+    tA += (int64_t)P.mt * P.nks;
+    tB += (int64_t)P.nt * P.nks;
+    rA += (int64_t)P.mt * BM;
+    rB += (int64_t)P.nt * BN;
+    eA += (int64_t)P.mt * BM * std::max(P.nch, 1);
+    eB += (int64_t)P.nt * BN * std::max(P.nch, 1);
+    tile_prefix.push_back(tile_prefix.back() + (int64_t)P.mt * P.nt);
+    packA_prefix.push_back(packA_prefix.back() + (int64_t)P.mt * P.nks);
+    packB_prefix.push_back(packB_prefix.back() + (int64_t)P.nt * P.nks);
+    rowA_prefix.push_back(rowA_prefix.back() + (P.nks ? P.M : 0));
+    rowB_prefix.push_back(rowB_prefix.back() + (P.nks ? P.N : 0));
+    flops += 2.0 * t.M * t.N * t.K;
+    probs.push_back(P);
+  }
+  nprob = (int)probs.size();
+  ntiles = tile_prefix.back();
+  tilesA = tA;
+  tilesB = tB;
+  rowsA = tA * BM;
+  rowsB = tB * BN;
+  nrowsA = rowA_prefix.back();
+  nrowsB = rowB_prefix.back();
+  if (nprob == 0) return;
+  auto up = [](void** d, const void* h, size_t bytes) {
+    MPSG_CUDA(cudaMalloc(d, std::max<size_t>(bytes, 16)));
+    if (bytes) MPSG_CUDA(cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice));
+  };
+  up((void**)&d_probs, probs.data(), sizeof(Problem) * nprob);
+  up((void**)&d_tile_prefix, tile_prefix.data(), sizeof(int64_t) * (nprob + 1));
+  up((void**)&d_packA_prefix, packA_prefix.data(), sizeof(int64_t) * (nprob + 1));
+  up((void**)&d_packB_prefix, packB_prefix.data(), sizeof(int64_t) * (nprob + 1));
+  up((void**)&d_rowA_prefix, rowA_prefix.data(), sizeof(int64_t) * (nprob + 1));
+  up((void**)&d_rowB_prefix, rowB_prefix.data(), sizeof(int64_t) * (nprob + 1));
+  MPSG_CUDA(cudaMalloc(&d_RA, sizeof(int32_t) * std::max<int64_t>(rA, 1)));
+  MPSG_CUDA(cudaMalloc(&d_CB, sizeof(int32_t) * std::max<int64_t>(rB, 1)));
+  MPSG_CUDA(cudaMemset(d_RA, 0, sizeof(int32_t) * std::max<int64_t>(rA, 1)));
+  MPSG_CUDA(cudaMemset(d_CB, 0, sizeof(int32_t) * std::max<int64_t>(rB, 1)));
+  MPSG_CUDA(cudaMalloc(&d_EA, sizeof(int16_t) * std::max<int64_t>(eA, 1)));
+  MPSG_CUDA(cudaMalloc(&d_EB, sizeof(int16_t) * std::max<int64_t>(eB, 1)));
+  MPSG_CUDA(cudaMemset(d_EA, 0, sizeof(int16_t) * std::max<int64_t>(eA, 1)));
+  MPSG_CUDA(cudaMemset(d_EB, 0, sizeof(int16_t) * std::max<int64_t>(eB, 1)));
+  MPSG_CUDA(cudaMalloc(&d_packA, std::max<int64_t>(S * rowsA * 64 * 2, 128 * 128)));
+  MPSG_CUDA(cudaMalloc(&d_packB, std::max<int64_t>(S * rowsB * 64 * 2, 128 * 128)));
+  MPSG_CUDA(cudaMalloc(&d_err, sizeof(int)));
+  MPSG_CUDA(cudaMemset(d_err, 0, sizeof(int)));
+  make_map(&tmA, d_packA, std::max<int64_t>(rowsA, BM), S, BM);
+  make_map(&tmB, d_packB, std::max<int64_t>(rowsB, BN), S, BN);
+  (void)ctx;
+}
+
+void SplitPlan::release() {
+  void* ptrs[] = {d_probs, d_tile_prefix, d_packA_prefix, d_packB_prefix, d_rowA_prefix,
+                  d_rowB_prefix, d_RA, d_CB, d_EA, d_EB, d_packA, d_packB, d_err};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  d_probs = nullptr;
+  d_tile_prefix = d_packA_prefix = d_packB_prefix = d_rowA_prefix = d_rowB_prefix = nullptr;
+  d_RA = d_CB = nullptr;
+  d_EA = d_EB = nullptr;
+  d_packA = d_packB = nullptr;
+  d_err = nullptr;
+  nprob = 0;
+}
+
+template <int S>
+static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double* B, double* C,
+                     int what) {
+  using CF = Cfg<S>;
+  const int chunk = chunk_for(S);
+  constexpr int kPackSmem = 128 * 65 * (int)sizeof(double);
+  static bool pack_attr = false;
+  if (!pack_attr) {
+    MPSG_CUDA(cudaFuncSetAttribute(pack_slices_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   kPackSmem));
+    pack_attr = true;
+  }
+  if (what & kPackA) {
+    KernelTimer timer(ctx, kKindPack);
+    if (sp.nrowsA) {
+      int g = (int)std::min<int64_t>((sp.nrowsA + 255) / 256, (int64_t)ctx->num_sms * 8);
+      pack_exponents_kernel<<<g, 256, 0, ctx->stream>>>(sp.d_probs, sp.d_rowA_prefix, sp.nprob,
+                                                       sp.nrowsA, 0, chunk, A, sp.d_EA, sp.d_RA);
+    }
+    if (sp.tilesA) {
+      int g = (int)std::min<int64_t>(sp.tilesA, (int64_t)ctx->num_sms * 6);
+      pack_slices_kernel<S><<<g, 256, kPackSmem, ctx->stream>>>(
+          sp.d_probs, sp.d_packA_prefix, sp.nprob, sp.tilesA, 0, chunk, BM, sp.rowsA, A, sp.d_EA,
+          sp.d_RA, (__nv_bfloat16*)sp.d_packA);
+    }
+    MPSG_CUDA(cudaGetLastError());
+    ctx->kernel_launches += 2;
+  }
+  if (what & kPackB) {
+    KernelTimer timer(ctx, kKindPack);
+    if (sp.nrowsB) {
+      int g = (int)std::min<int64_t>((sp.nrowsB + 255) / 256, (int64_t)ctx->num_sms * 8);
+      pack_exponents_kernel<<<g, 256, 0, ctx->stream>>>(sp.d_probs, sp.d_rowB_prefix, sp.nprob,
+                                                       sp.nrowsB, 1, chunk, B, sp.d_EB, sp.d_CB);
+    }
+    if (sp.tilesB) {
+      int g = (int)std::min<int64_t>(sp.tilesB, (int64_t)ctx->num_sms * 6);
+      pack_slices_kernel<S><<<g, 256, kPackSmem, ctx->stream>>>(
+          sp.d_probs, sp.d_packB_prefix, sp.nprob, sp.tilesB, 1, chunk, BN, sp.rowsB, B, sp.d_EB,
+          sp.d_CB, (__nv_bfloat16*)sp.d_packB);
+    }
+    MPSG_CUDA(cudaGetLastError());
+    ctx->kernel_launches += 2;
+  }
+  if (!(what & kRunGemm)) return;
+  static bool attr_set = false;
+  if (!attr_set) {
+    MPSG_CUDA(cudaFuncSetAttribute(split_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   CF::kSmemBytes));
+    attr_set = true;
+  }
+  const int grid = (int)std::min<int64_t>(sp.ntiles, (int64_t)ctx->num_sms);
+  KernelTimer timer(ctx, kKindGemmSplit, sp.flops);
+  split_gemm_kernel<S><<<grid, 192, CF::kSmemBytes, ctx->stream>>>(
+      sp.tmA, sp.tmB, sp.d_probs, sp.d_tile_prefix, sp.nprob, sp.ntiles, sp.d_RA, sp.d_CB, C,
+      sp.d_err);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches++;
+  ctx->gemm_flops += sp.flops;
+}
+
+void launch_split_gemm(Context* ctx, SplitPlan& sp, const double* A, const double* B, double* C,
+                       int what) {
+  if (sp.ntiles == 0) return;
+  switch (sp.S) {
+    case 2: launch_t<2>(ctx, sp, A, B, C, what); break;
+    case 3: launch_t<3>(ctx, sp, A, B, C, what); break;
+    case 4: launch_t<4>(ctx, sp, A, B, C, what); break;
+    default: throw Error(kErrUnsupported, "split precision supports 2..4 slices");
+  }
+}
+
+int read_error(Context* ctx, SplitPlan& sp) {
+  int e = 0;
+  if (!sp.d_err) return 0;
+  MPSG_CUDA(cudaMemcpyAsync(&e, sp.d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return e;
+}
+
+}  // namespace split
+}  // namespace mpsg

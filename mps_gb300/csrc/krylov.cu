@@ -86,9 +86,8 @@ EigResult eigsolve_heff2(Context* ctx, const DeviceTensor& x0, const DeviceTenso
                          int krylovdim, int maxiter, double tol, int precision) {
   if (krylovdim < 2) throw Error(kErrArgument, "krylovdim must be at least 2");
   if (maxiter < 1) throw Error(kErrArgument, "maxiter must be at least 1");
-  auto f = [&](const DeviceTensor& x) {
-    return applymps2site(ctx, x, envL, envR, W1, W2, precision);
-  };
+  auto op = heff_create(ctx, x0.meta, envL, envR, W1, W2, precision);
+  auto f = [&](const DeviceTensor& x) { return heff_apply(*op, x); };
   const int kd = krylovdim;
   std::vector<double> H((kd + 1) * (kd + 1), 0.0);
   auto Hat = [&](int i, int j) -> double& { return H[i + (kd + 1) * j]; };

@@ -3,6 +3,7 @@
 #include <sstream>
 
 #include "ops.hpp"
+#include "split.hpp"
 
 namespace mpsg {
 
@@ -208,13 +209,20 @@ DeviceTensor symmatrix(Context* ctx, const DeviceTensor& a, const std::vector<in
 // ------------------------------------------------------------------------------------------
 // block GEMM dispatch
 // ------------------------------------------------------------------------------------------
-static void run_gemm(Context* ctx, const DevGemmPlan& g, const double* A, const double* B,
+static void run_gemm(Context* ctx, DevGemmPlan& g, const double* A, const double* B,
                      double* C, int precision) {
   if (precision == 0) {
     launch_gemm_f64(ctx, g, A, B, C);
     return;
   }
-  throw Error(kErrUnsupported, "split-precision GEMM not available in this build");
+  if (precision < 2 || precision > 4)
+    throw Error(kErrUnsupported, "precision must be 0 (FP64) or 2..4 bf16 slices");
+  auto& sp = g.splitp[precision];
+  if (!sp) {
+    sp = std::make_shared<split::SplitPlan>();
+    sp->build(ctx, g.host, precision);
+  }
+  split::launch_split_gemm(ctx, *sp, A, B, C);
 }
 
 DeviceTensor matmul(Context* ctx, const DeviceTensor& a, const DeviceTensor& b, int precision) {
@@ -325,6 +333,10 @@ static const std::vector<int> kH4A = {1, 2, 3, -1, -2}, kH4B = {-2, -1, 4};
 DeviceTensor applymps2site(Context* ctx, const DeviceTensor& v, const DeviceTensor& envL,
                            const DeviceTensor& envR, const DeviceTensor& W1,
                            const DeviceTensor& W2, int precision) {
+  if (precision != 0) {  // tensor-core path: prepared (W-folded) operator, built per call here
+    auto op = heff_create(ctx, v.meta, envL, envR, W1, W2, precision);
+    return heff_apply(*op, v);
+  }
   DeviceTensor t1 = contract(ctx, envL, kH1A, v, kH1B, precision, nullptr);
   DeviceTensor t2 = contract(ctx, t1, kH2A, W1, kH2B, precision, nullptr);
   t1 = DeviceTensor();
@@ -354,6 +366,114 @@ DeviceTensor mpsupdateright(Context* ctx, const DeviceTensor& env, const DeviceT
   DeviceTensor t = contract(ctx, env, {-1, 3, 4}, A, {1, 2, -1}, precision, nullptr);
   t = contract(ctx, t, {1, -1, -2, 4}, W, {3, 2, -2, -1}, precision, nullptr);
   return contract(ctx, t, {1, -1, 2, -2}, dual_view(A), {3, -1, -2}, precision, nullptr);
+}
+
+// ------------------------------------------------------------------------------------------
+// prepared effective Hamiltonian
+// ------------------------------------------------------------------------------------------
+static std::shared_ptr<DevContract> private_contract_plan(const TensorMeta& A,
+                                                          const std::vector<int>& idxA,
+                                                          const TensorMeta& B,
+                                                          const std::vector<int>& idxB) {
+  auto p = std::make_shared<DevContract>();
+  p->host = plan_contract(A, idxA, B, idxB);
+  if (p->host->scalar) throw Error(kErrArgument, "unexpected full contraction");
+  p->fa.upload(p->host->fa.tasks, p->host->fa.identity);
+  p->fb.upload(p->host->fb.tasks, p->host->fb.identity);
+  p->mm.upload(p->host->mm.gemms, p->host->mm.flops);
+  p->split.upload(p->host->split.tasks, p->host->split.identity);
+  return p;
+}
+
+static const std::vector<int> kLW_A = {1, -1, 3}, kLW_B = {-1, 5, 4, 2};
+static const std::vector<int> kRW_A = {2, 4, -1, 3}, kRW_B = {1, -1, 5};
+static const std::vector<int> kX_A = {-1, -2, 1, 3, 2}, kX_B = {-1, -2, 4, 5};
+static const std::vector<int> kO_A = {1, 2, -1, -2, -3}, kO_B = {-3, -1, -2, 3, 4};
+
+std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const DeviceTensor& envL,
+                                    const DeviceTensor& envR, const DeviceTensor& W1,
+                                    const DeviceTensor& W2, int precision) {
+  auto op = std::make_shared<HeffOp>();
+  op->ctx = ctx;
+  op->precision = precision;
+  op->vmeta = vmeta;
+  op->ref_flops = applymps2site_flops(ctx, vmeta, envL.meta, envR.meta, W1.meta, W2.meta);
+  if (precision == 0) {
+    op->envL = envL;
+    op->envR = envR;
+    op->W1 = W1;
+    op->W2 = W2;
+    return op;
+  }
+  if (precision < 2 || precision > 4)
+    throw Error(kErrUnsupported, "precision must be 0 (FP64) or 2..4 bf16 slices");
+  op->envLW = contract(ctx, envL, kLW_A, W1, kLW_B, 0, nullptr);
+  op->envRW = contract(ctx, W2, kRW_A, envR, kRW_B, 0, nullptr);
+  op->c1 = private_contract_plan(op->envLW.meta, kX_A, vmeta, kX_B);
+  op->c2 = private_contract_plan(op->c1->host->split.out, kO_A, op->envRW.meta, kO_B);
+  // constant operands: fuse once, slice once
+  op->fusedA1 = alloc_buffer(ctx, op->c1->host->fa.out.total);
+  launch_copy(ctx, op->c1->fa, op->envLW.data(), op->fusedA1->ptr);
+  op->fusedB2 = alloc_buffer(ctx, op->c2->host->fb.out.total);
+  launch_copy(ctx, op->c2->fb, op->envRW.data(), op->fusedB2->ptr);
+  for (auto* c : {op->c1.get(), op->c2.get()}) {
+    auto& sp = c->mm.splitp[precision];
+    sp = std::make_shared<split::SplitPlan>();
+    sp->build(ctx, c->mm.host, precision);
+  }
+  split::launch_split_gemm(ctx, *op->c1->mm.splitp[precision], op->fusedA1->ptr, nullptr, nullptr,
+                           split::kPackA);
+  split::launch_split_gemm(ctx, *op->c2->mm.splitp[precision], nullptr, op->fusedB2->ptr, nullptr,
+                           split::kPackB);
+  return op;
+}
+
+DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v) {
+  Context* ctx = op.ctx;
+  if (!same_meta(v.meta, op.vmeta))
+    throw Error(kErrSpaceMismatch, "H_eff applied to a tensor of another structure");
+  if (op.precision == 0) return applymps2site(ctx, v, op.envL, op.envR, op.W1, op.W2, 0);
+  const int S = op.precision;
+  // X = envLW . v
+  DevContract& c1 = *op.c1;
+  auto fb = alloc_buffer(ctx, c1.host->fb.out.total);
+  launch_copy(ctx, c1.fb, v.data(), fb->ptr);
+  auto fc1 = alloc_buffer(ctx, c1.host->mm.out.total);
+  split::launch_split_gemm(ctx, *c1.mm.splitp[S], nullptr, fb->ptr, fc1->ptr,
+                           split::kPackB | split::kRunGemm);
+  DeviceTensor X;
+  X.ctx = ctx;
+  X.meta = c1.host->split.out;
+  if (c1.split.identity) {
+    X.buf = fc1;
+  } else {
+    X.buf = alloc_buffer(ctx, X.meta.total);
+    launch_copy(ctx, c1.split, fc1->ptr, X.data());
+  }
+  fb.reset();
+  fc1.reset();
+  // v' = X . envRW
+  DevContract& c2 = *op.c2;
+  std::shared_ptr<Buffer> fa;
+  const double* pa = X.data();
+  if (!c2.fa.identity) {
+    fa = alloc_buffer(ctx, c2.host->fa.out.total);
+    launch_copy(ctx, c2.fa, X.data(), fa->ptr);
+    pa = fa->ptr;
+  }
+  auto fc2 = alloc_buffer(ctx, c2.host->mm.out.total);
+  split::launch_split_gemm(ctx, *c2.mm.splitp[S], pa, nullptr, fc2->ptr,
+                           split::kPackA | split::kRunGemm);
+  DeviceTensor out;
+  out.ctx = ctx;
+  out.meta = c2.host->split.out;
+  if (c2.split.identity) {
+    out.buf = fc2;
+  } else {
+    out.buf = alloc_buffer(ctx, out.meta.total);
+    launch_copy(ctx, c2.split, fc2->ptr, out.data());
+  }
+  return out;
 }
 
 // ------------------------------------------------------------------------------------------

@@ -40,4 +40,26 @@ DeviceTensor mpsupdateright(Context* ctx, const DeviceTensor& env, const DeviceT
 
 double dot(Context* ctx, const DeviceTensor& a, const DeviceTensor& b);
 
+// Two-site effective Hamiltonian prepared for repeated application.
+//  * precision 0: the reference's four contractions (src/apply.jl:99-103) in FP64.
+//  * precision S >= 2: W1 folded into envL and W2 into envR once (FP64), so that every
+//    application is two large block GEMMs on the tensor cores:
+//      X(l,s1',m',s2,r)  = envLW(l',s1,l,m',s1') . v(l',s1,s2,r)        over (l', s1)
+//      v'(l,s1',s2',r')  = X . envRW(r,m',s2,s2',r')                      over (m', s2, r)
+//    with the constant operands fused and sliced once.
+struct HeffOp {
+  Context* ctx = nullptr;
+  int precision = 0;
+  DeviceTensor envL, envR, W1, W2;   // precision 0
+  DeviceTensor envLW, envRW;         // precision >= 2
+  TensorMeta vmeta;
+  std::shared_ptr<DevContract> c1, c2;
+  std::shared_ptr<Buffer> fusedA1, fusedB2;
+  double ref_flops = 0;  // algorithmic flops of the reference contraction order
+};
+std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const DeviceTensor& envL,
+                                    const DeviceTensor& envR, const DeviceTensor& W1,
+                                    const DeviceTensor& W2, int precision);
+DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v);
+
 }  // namespace mpsg

@@ -22,6 +22,9 @@ namespace mpsg {
   } while (0)
 
 struct Context;
+namespace split {
+struct SplitPlan;
+}
 
 // Stream-ordered device allocation.  Every buffer co-owns its context, so the context (stream,
 // caches) outlives the last tensor whatever order a caller releases handles in.
@@ -62,6 +65,7 @@ struct DevGemmPlan {
   int64_t* d_prefix = nullptr;
   int64_t max_ld = 0;
   std::vector<GemmTask> host;
+  std::shared_ptr<split::SplitPlan> splitp[8];  // split-precision plans by slice count
   void upload(const std::vector<GemmTask>& g, double flops_);
   void release();
 };

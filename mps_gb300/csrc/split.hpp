@@ -1,0 +1,55 @@
+// Split-precision (bf16 slices on tcgen05) grouped block GEMM: host plan and launcher.
+#pragma once
+
+#include <cuda.h>
+
+#include "runtime.hpp"
+
+namespace mpsg {
+namespace split {
+
+constexpr int BM = 128, BN = 64, BK = 64;
+constexpr int kSliceBits = 7;  // beta: bits per bf16 slice digit
+
+// One sector GEMM as the split kernels see it (column-major A: M x K, B: K x N, C: M x N).
+struct Problem {
+  int64_t M, N, K;
+  int64_t offA, offB, offC, lda, ldb, ldc;
+  int32_t mt, nt, nks, nch;  // M tiles, N tiles, K steps of 64, K chunks
+  int64_t tA, tB;            // first packed tile of A / of B
+  int64_t rA, rB;            // first row in the per-row exponent arrays (A rows, B columns)
+  int64_t eA, eB;            // first entry in the per-(row, chunk) exponent arrays
+};
+
+// Device tables, packed-slice scratch and TMA descriptors of one grouped GEMM at S slices.
+struct SplitPlan {
+  int S = 0;
+  int nprob = 0;
+  int64_t ntiles = 0, tilesA = 0, tilesB = 0, rowsA = 0, rowsB = 0, nrowsA = 0, nrowsB = 0;
+  double flops = 0;
+  std::vector<Problem> probs;
+  Problem* d_probs = nullptr;
+  int64_t *d_tile_prefix = nullptr, *d_packA_prefix = nullptr, *d_packB_prefix = nullptr;
+  int64_t *d_rowA_prefix = nullptr, *d_rowB_prefix = nullptr;
+  int32_t *d_RA = nullptr, *d_CB = nullptr;
+  int16_t *d_EA = nullptr, *d_EB = nullptr;
+  void *d_packA = nullptr, *d_packB = nullptr;
+  int* d_err = nullptr;
+  alignas(64) CUtensorMap tmA;
+  alignas(64) CUtensorMap tmB;
+  void build(Context* ctx, const std::vector<GemmTask>& g, int S);
+  void release();
+  ~SplitPlan() { release(); }
+};
+
+int chunk_for(int S);
+// what: bit 0 = pack A, bit 1 = pack B, bit 2 = run the GEMM (an operand packed by an earlier
+// call stays valid in the plan's scratch until the plan is packed again).
+enum { kPackA = 1, kPackB = 2, kRunGemm = 4, kAll = 7 };
+void launch_split_gemm(Context* ctx, SplitPlan& sp, const double* A, const double* B, double* C,
+                       int what = kAll);
+// Error code recorded by the kernel (0 = none; nonzero = a bounded wait timed out).
+int read_error(Context* ctx, SplitPlan& sp);
+
+}  // namespace split
+}  // namespace mpsg

@@ -24,7 +24,7 @@ __all__ = [
     "matmul", "contract", "contract_flops", "dot", "norm", "axpy", "axpby", "rmul", "mul",
     "similar", "copy", "fill_", "applymps2site", "applymps2site_flops", "mpsupdateleft",
     "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision", "_svd_",
-    "svdtrunc", "truncatedsizes", "small_eigh", "eigsolve_heff2", "EigInfo",
+    "svdtrunc", "truncatedsizes", "small_eigh", "eigsolve_heff2", "EigInfo", "Heff2",
 ]
 
 
@@ -516,6 +516,39 @@ def applymps2site(v, envL, envR, W1, W2, precision=None) -> SymTensor:
     call("mpsg_applymps2site", v.ctx.handle, v.handle, envL.handle, envR.handle, W1.handle,
          W2.handle, _prec(precision), C.byref(h))
     return SymTensor(h, v.ctx)
+
+
+class Heff2:
+    """The two-site effective Hamiltonian v -> _applymps2site(v, envL, envR, W1, W2)
+    (src/apply.jl:93-105) prepared once and applied many times, as the Krylov solver does
+    (src/dmrg.jl:77).  ``precision`` 0 = the reference's FP64 contractions; S >= 2 = W-folded
+    split-precision tensor-core path."""
+
+    def __init__(self, v_like, envL, envR, W1, W2, precision=None):
+        h = C.c_void_p()
+        call("mpsg_heff2_create", v_like.ctx.handle, v_like.handle, envL.handle, envR.handle,
+             W1.handle, W2.handle, _prec(precision), C.byref(h))
+        self._h = h
+        self.ctx = v_like.ctx
+        self._free = _lib.lib.mpsg_heff2_free
+
+    def __call__(self, v) -> SymTensor:
+        h = C.c_void_p()
+        call("mpsg_heff2_apply", self.ctx.handle, self._h, v.handle, C.byref(h))
+        return SymTensor(h, self.ctx)
+
+    def flops(self) -> float:
+        f = C.c_double()
+        call("mpsg_heff2_flops", self._h, C.byref(f))
+        return f.value
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._free(self._h)
+                self._h = None
+        except Exception:
+            pass
 
 
 def applymps2site_flops(v, envL, envR, W1, W2) -> float:

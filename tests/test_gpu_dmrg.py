@@ -87,10 +87,12 @@ def test_center_at_matches_oracle():
 
 
 def heisenberg_setup(lx, chi, seed=1911):
+    """Oracle MPS canonicalised on the CPU; the device MPS is uploaded from the same tensors so
+    that gauge-dependent objects (environments, eigenvectors) compare elementwise."""
     sites = gd.random_mps_host(lx, lx // 2, chi, seed=seed)
-    mo, md = oracle_mps(sites), gd.mps_from_host(sites)
+    mo = oracle_mps(sites)
     om.center_at(mo, 1)
-    gd.center_at(md, 1)
+    md = gd.MPState([to_device(A) for A in mo.As], center=1)
     Wo, Wd = om.xxz_u1mpo(lx, 1.0), gd.xxz_u1mpo(lx, 1.0)
     return mo, md, Wo, Wd, om.initialenv(mo, Wo), gd.initialenv(md, Wd)
 

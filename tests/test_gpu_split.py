@@ -1,0 +1,95 @@
+"""GPU checks of the split-precision tcgen05 block GEMM against the FP64 oracle.
+
+Tolerances follow the slicing bound: S bf16 slices of beta = 7 bits give a per-product error
+below 2^(1 - 7 S) of the row/column scale, so the relative Frobenius error must stay below
+2e-4 (S = 2), 2e-6 (S = 3) and 2e-8 (S = 4).  Integer-valued operands small enough to be
+represented by the leading slice must come out bit-exact: this pins the exact FP32
+accumulation in tensor memory that the error-free splitting relies on.
+"""
+import numpy as np
+import pytest
+
+import mps_gb300 as mg
+from mps_gb300 import dmrg as gd
+from oracle import symtensors as st
+from oracle import mps as om
+from oracle.symtensors import U1Space, dual_space as dual
+
+from helpers import to_device, to_oracle, rand_tensor, relerr
+
+pytestmark = pytest.mark.gpu
+
+TOL = {2: 2e-4, 3: 2e-6, 4: 2e-8}
+
+
+def pair(rng, dims_l, dims_k, dims_r, scale_rows=False):
+    Vl = U1Space(*[(c, d) for c, d in dims_l])
+    Vk = U1Space(*[(c, d) for c, d in dims_k])
+    Vr = U1Space(*[(c, d) for c, d in dims_r])
+    A = rand_tensor(0, (Vl, dual(Vk)), rng)
+    B = rand_tensor(0, (Vk, dual(Vr)), rng)
+    if scale_rows:  # rows spanning 20 orders of magnitude
+        for s, b in A.blocks.items():
+            b *= np.logspace(-10, 10, b.shape[0])[:, None]
+    return A, B
+
+
+@pytest.mark.parametrize("S", [2, 3, 4])
+def test_split_matmul_accuracy(S):
+    rng = np.random.default_rng(S)
+    # ragged sectors: M, N not multiples of the tiles; K from 1 to 700 (several K chunks)
+    A, B = pair(rng, [(0, 200), (1, 129), (2, 7)], [(0, 700), (1, 65), (2, 1)],
+                [(0, 64), (1, 300), (2, 3)])
+    want = st.matmul(A, B)
+    got = mg.matmul(to_device(A), to_device(B), precision=S)
+    for s in want.blocks:
+        e = relerr(got.blocks[s], want.blocks[s])
+        assert e < TOL[S], (s, e)
+
+
+@pytest.mark.parametrize("S", [2, 3, 4])
+def test_split_matmul_wide_dynamic_range(S):
+    rng = np.random.default_rng(10 + S)
+    A, B = pair(rng, [(0, 150)], [(0, 260)], [(0, 90)], scale_rows=True)
+    want = st.matmul(A, B).blocks[(0, 0)]
+    got = mg.matmul(to_device(A), to_device(B), precision=S).blocks[(0, 0)]
+    # every row keeps its own relative accuracy
+    err = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+    assert err.max() < TOL[S]
+
+
+def test_split_exact_on_small_integers():
+    """Entries in [-100, 100] are represented exactly by the leading slice; with K = 512 every
+    result is an integer below 2^24, which exact FP32 accumulation reproduces bit for bit."""
+    rng = np.random.default_rng(0)
+    Vl, Vk, Vr = U1Space((0, 256)), U1Space((0, 512)), U1Space((0, 128))
+    A = st.SymTensor(0, (Vl, dual(Vk)), {(0, 0): rng.integers(-100, 101, (256, 512)).astype(float)})
+    B = st.SymTensor(0, (Vk, dual(Vr)), {(0, 0): rng.integers(-100, 101, (512, 128)).astype(float)})
+    want = A.blocks[(0, 0)] @ B.blocks[(0, 0)]
+    for S in (2, 3, 4):
+        got = mg.matmul(to_device(A), to_device(B), precision=S).blocks[(0, 0)]
+        assert np.array_equal(got, want), S
+
+
+def test_split_zero_sectors_and_partner_free_blocks():
+    rng = np.random.default_rng(3)
+    # A has a row charge whose contracted partner does not exist in B's column space
+    Vl, Vk, Vr = U1Space((0, 5), (1, 6)), U1Space((0, 7)), U1Space((0, 4), (1, 3))
+    A = rand_tensor(0, (Vl, dual(Vk)), rng)
+    B = rand_tensor(0, (Vk, dual(Vr)), rng)
+    want = st.matmul(A, B)
+    got = mg.matmul(to_device(A), to_device(B), precision=3)
+    assert got.sectors() == want.sectors()
+    assert relerr(got.to_flat(), st.flatten(want)) < TOL[3]
+
+
+@pytest.mark.parametrize("S", [2, 3, 4])
+def test_split_heff_chi64(S):
+    (sv, sl, sr), flats = gd.heff_inputs_host(64, 0.5, 1911, 9)
+    conv = lambda sp: tuple(st.VectorSpace(V.sectors, V.isdual) for V in sp)
+    O = [st.from_flat(0, conv(s), f) for s, f in zip((sv, sl, sr), flats)]
+    W = om.xxz_u1mpo(3, 0.5)[1]
+    want = st.flatten(om.applymps2site(O[0], O[1], O[2], W, W))
+    D = gd.heff_problem(64, 0.5, 1911, ncharges=9)
+    got = mg.applymps2site(*D, precision=S).to_flat()
+    assert relerr(got, want) < 4 * TOL[S]
