@@ -264,7 +264,8 @@ def run_ours(args):
 
     # per-kernel CUDA-event times (second pass over the same steps)
     timed_steps(op, args.steps, with_kernel_timing=True)
-    kinds = {k: ctx.kernel_time(k) for k in ("copy", "gemm_f64", "gemm_split", "pack")}
+    kinds = {k: ctx.kernel_time(k) for k in ("copy", "gemm_f64", "gemm_split", "pack",
+                                             "pack_slices")}
     ctx.set_timing(False)
 
     # end to end through the C ABI with host buffers: H2D of all five inputs, the reference-facing

@@ -262,41 +262,75 @@ __device__ __forceinline__ int exp_bound(unsigned long long absbits) {
   return (eb == 0 ? -1022 : eb - 1023) + 1;
 }
 
-// One thread per operand row: chunk exponents e(r,c) and the row reference R(r) = max_c e(r,c).
-__global__ void pack_exponents_kernel(const Problem* __restrict__ probs,
-                                      const int64_t* __restrict__ row_prefix, int nprob,
-                                      int64_t nrows, int is_b, int chunk,
-                                      const double* __restrict__ X, int16_t* __restrict__ E,
-                                      int32_t* __restrict__ R) {
-  for (int64_t gr = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; gr < nrows;
-       gr += (int64_t)gridDim.x * blockDim.x) {
-    const int p = find_problem(row_prefix, nprob, gr);
+constexpr int kNoExponent = (int)0x80808080;  // byte pattern of the reset: "row entirely zero"
+
+// One CTA per (problem, block of 32 operand rows, K chunk): chunk exponents e(r,c), and the row
+// reference R(r) = max_c e(r,c) by atomicMax (R is reset to kNoExponent before the pass).
+// Loads are coalesced along whichever operand axis is contiguous.
+__global__ void __launch_bounds__(256) pack_exponents_kernel(
+    const Problem* __restrict__ probs, const int64_t* __restrict__ item_prefix, int nprob,
+    int64_t nitems, int is_b, int chunk, const double* __restrict__ X, int16_t* __restrict__ E,
+    int32_t* __restrict__ R) {
+  __shared__ unsigned long long red[8][33];
+  const int t = threadIdx.x;
+  for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int p = find_problem(item_prefix, nprob, it);
     const Problem P = probs[p];
-    const int64_t r = gr - row_prefix[p];
+    const int64_t lt = it - item_prefix[p];
     int64_t rows, off, rs, ks;
     operand_geom(P, is_b, rows, off, rs, ks);
+    const int64_t nrb = (rows + 31) / 32;
+    const int64_t r0 = (lt % nrb) * 32;
+    const int c = (int)(lt / nrb);
+    const int64_t k0 = (int64_t)c * chunk, k1 = min(k0 + chunk, P.K);
     const int64_t rbase = is_b ? P.rB : P.rA;
     const int64_t ebase = is_b ? P.eB : P.eA;
-    const int nch = P.nch;
-    int Rr = -100000;
-    bool any = false;
-    for (int c = 0; c < nch; ++c) {
+    if (rs == 1) {
+      // 32 consecutive rows per warp-row of the CTA, 8 interleaved K groups
+      const int r = t & 31, kg = t >> 5;
       unsigned long long m = 0;
-      const int64_t k0 = (int64_t)c * chunk, k1 = min((int64_t)(c + 1) * chunk, P.K);
-      for (int64_t k = k0; k < k1; ++k) {
-        const unsigned long long b =
-            (unsigned long long)__double_as_longlong(X[off + r * rs + k * ks]) &
-            0x7fffffffffffffffull;
-        m = b > m ? b : m;
+      if (r0 + r < rows)
+        for (int64_t k = k0 + kg; k < k1; k += 8) {
+          const unsigned long long b =
+              (unsigned long long)__double_as_longlong(X[off + (r0 + r) + k * ks]) &
+              0x7fffffffffffffffull;
+          m = b > m ? b : m;
+        }
+      red[kg][r] = m;
+      __syncthreads();
+      if (t < 32 && r0 + t < rows) {
+        unsigned long long mm = 0;
+#pragma unroll
+        for (int g = 0; g < 8; ++g) mm = red[g][t] > mm ? red[g][t] : mm;
+        const int e = exp_bound(mm);
+        E[ebase + (r0 + t) * P.nch + c] = (int16_t)e;
+        if (mm) atomicMax(&R[rbase + r0 + t], e);
       }
-      const int e = exp_bound(m);
-      E[ebase + r * nch + c] = (int16_t)e;
-      if (m) {
-        Rr = any ? max(Rr, e) : e;
-        any = true;
+      __syncthreads();
+    } else {
+      // one row per warp at a time, lanes along the contiguous K axis
+      const int lane = t & 31, w = t >> 5;
+      for (int rr = w; rr < 32; rr += 8) {
+        const int64_t r = r0 + rr;
+        if (r >= rows) break;
+        unsigned long long m = 0;
+        for (int64_t k = k0 + lane; k < k1; k += 32) {
+          const unsigned long long b =
+              (unsigned long long)__double_as_longlong(X[off + r * rs + k]) & 0x7fffffffffffffffull;
+          m = b > m ? b : m;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long q = __shfl_xor_sync(0xffffffffu, m, o);
+          m = q > m ? q : m;
+        }
+        if (lane == 0) {
+          const int e = exp_bound(m);
+          E[ebase + r * P.nch + c] = (int16_t)e;
+          if (m) atomicMax(&R[rbase + r], e);
+        }
       }
     }
-    R[rbase + r] = any ? Rr : 0;
   }
 }
 
@@ -344,39 +378,41 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
       if (r < rows) {
         e = E[ebase + r * P.nch + c];
         Rr = R[rbase + r];
+        if (Rr == kNoExponent) Rr = e;  // the whole row is zero: every slice is zero
       }
+      // per-row slice scales 2^(e - R - beta (q+1)) (0 when below the float range: negligible)
+      float scale[S];
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        const int k = e - Rr - kBeta * (q + 1);
+        scale[q] = k >= -126 ? __uint_as_float((uint32_t)(k + 127) << 23) : 0.f;
+      }
+      // F = round(x * 2^(beta S - e)) needs at most beta*S + 1 <= 29 bits: 32-bit integer work
+      // on the top 32 bits of the significand (hi word: 20 bits, lo word: 11 bits, implicit 1)
+      const int sbase = 1054 + e - kBeta * S;  // F = m32 >> (sbase - eb), rounded
       uint32_t packed[S][4];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const long long bits = __double_as_longlong(tile[rr][g8 * 8 + j]);
-        long long F = 0;
-        const int eb = (int)((bits >> 52) & 0x7ff);
-        if (eb != 0 && r < rows) {
-          const unsigned long long mant = ((unsigned long long)bits & ((1ull << 52) - 1)) |
-                                          (1ull << 52);
-          const int sh = eb - 1075 + kBeta * S - e;
-          unsigned long long f;
-          if (sh >= 0) f = mant << sh;
-          else if (sh > -64) f = (mant + (1ull << (-sh - 1))) >> (-sh);
-          else f = 0;
-          F = bits < 0 ? -(long long)f : (long long)f;
+        const double x = tile[rr][g8 * 8 + j];
+        const int hw = __double2hiint(x);
+        const uint32_t lw = (uint32_t)__double2loint(x);
+        const int eb = (hw >> 20) & 0x7ff;
+        const uint32_t m32 = (((uint32_t)hw << 11) | (lw >> 21)) | 0x80000000u;
+        const int s = sbase - eb;  // >= 32 - beta*S > 0 for every element of the row chunk
+        int F = 0;
+        if (eb != 0 && s <= 32 && r < rows) {
+          F = (int)(((m32 >> (s - 1)) + 1u) >> 1);  // round half up
+          if (hw < 0) F = -F;
         }
 #pragma unroll
         for (int q = 0; q < S; ++q) {
           const int shq = kBeta * (S - 1 - q);
-          long long tq;
-          if (shq > 0) tq = (F + (1ll << (shq - 1))) >> shq;
-          else tq = F;
-          F -= tq << shq;
-          // slice value t_q * 2^(e - R - beta (q+1))
-          int k = e - Rr - kBeta * (q + 1);
-          float v = (float)tq;
-          if (k < -126) {
-            v *= 1.1754943508222875e-38f;  // 2^-126
-            k += 126;
-            k = max(k, -126);
+          int tq = F;
+          if (shq > 0) {
+            tq = (F + (1 << (shq - 1))) >> shq;
+            F -= tq * (1 << shq);
           }
-          v *= __uint_as_float((uint32_t)(k + 127) << 23);
+          const float v = (float)tq * scale[q];  // exact: |tq| <= 2^beta
           const uint16_t h = __bfloat16_as_ushort(__float2bfloat16_rn(v));
           if (j & 1) packed[q][j >> 1] |= (uint32_t)h << 16;
           else packed[q][j >> 1] = (uint32_t)h;
@@ -579,7 +615,12 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
 #pragma unroll
         for (int j = 0; j < BN; ++j) {
           const int64_t col = ni * BN + j;
-          if (col < P.N) Cp[col * P.ldc] = ds_to_f64(hi[j], lo[j], Rr + CB[P.rB + col]);
+          if (col < P.N) {
+            const int Cc = CB[P.rB + col];
+            // a zero row or column (no exponent) contributes exact zeros
+            const int E = (Rr == kNoExponent || Cc == kNoExponent) ? 0 : Rr + Cc;
+            Cp[col * P.ldc] = ds_to_f64(hi[j], lo[j], E);
+          }
         }
       }
     }
@@ -668,8 +709,9 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
     tile_prefix.push_back(tile_prefix.back() + (int64_t)P.mt * P.nt);
     packA_prefix.push_back(packA_prefix.back() + (int64_t)P.mt * P.nks);
     packB_prefix.push_back(packB_prefix.back() + (int64_t)P.nt * P.nks);
-    rowA_prefix.push_back(rowA_prefix.back() + (P.nks ? P.M : 0));
-    rowB_prefix.push_back(rowB_prefix.back() + (P.nks ? P.N : 0));
+    // exponent work items: (32-row block, K chunk) pairs
+    rowA_prefix.push_back(rowA_prefix.back() + (P.nks ? ((P.M + 31) / 32) * P.nch : 0));
+    rowB_prefix.push_back(rowB_prefix.back() + (P.nks ? ((P.N + 31) / 32) * P.nch : 0));
     flops += 2.0 * t.M * t.N * t.K;
     probs.push_back(P);
   }
@@ -681,6 +723,8 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   rowsB = tB * BN;
   nrowsA = rowA_prefix.back();
   nrowsB = rowB_prefix.back();
+  rowsRA = std::max<int64_t>(rA, 1);
+  rowsCB = std::max<int64_t>(rB, 1);
   if (nprob == 0) return;
   auto up = [](void** d, const void* h, size_t bytes) {
     MPSG_CUDA(cudaMalloc(d, std::max<size_t>(bytes, 16)));
@@ -735,37 +779,34 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
                                    kPackSmem));
     pack_attr = true;
   }
-  if (what & kPackA) {
-    KernelTimer timer(ctx, kKindPack);
-    if (sp.nrowsA) {
-      int g = (int)std::min<int64_t>((sp.nrowsA + 255) / 256, (int64_t)ctx->num_sms * 8);
-      pack_exponents_kernel<<<g, 256, 0, ctx->stream>>>(sp.d_probs, sp.d_rowA_prefix, sp.nprob,
-                                                       sp.nrowsA, 0, chunk, A, sp.d_EA, sp.d_RA);
+  for (int side = 0; side < 2; ++side) {
+    if (!(what & (side ? kPackB : kPackA))) continue;
+    const int64_t nitems = side ? sp.nrowsB : sp.nrowsA;
+    const int64_t ntile = side ? sp.tilesB : sp.tilesA;
+    const double* X = side ? B : A;
+    int16_t* E = side ? sp.d_EB : sp.d_EA;
+    int32_t* R = side ? sp.d_CB : sp.d_RA;
+    if (nitems) {
+      MPSG_CUDA(cudaMemsetAsync(R, 0x80, sizeof(int32_t) * (side ? sp.rowsCB : sp.rowsRA),
+                                ctx->stream));
+      KernelTimer timer(ctx, kKindPack);
+      int g = (int)std::min<int64_t>(nitems, (int64_t)ctx->num_sms * 8);
+      pack_exponents_kernel<<<g, 256, 0, ctx->stream>>>(
+          sp.d_probs, side ? sp.d_rowB_prefix : sp.d_rowA_prefix, sp.nprob, nitems, side, chunk,
+          X, E, R);
+      MPSG_CUDA(cudaGetLastError());
+      ctx->kernel_launches++;
     }
-    if (sp.tilesA) {
-      int g = (int)std::min<int64_t>(sp.tilesA, (int64_t)ctx->num_sms * 6);
+    if (ntile) {
+      KernelTimer timer(ctx, kKindPackSlices);
+      int g = (int)std::min<int64_t>(ntile, (int64_t)ctx->num_sms * 6);
       pack_slices_kernel<S><<<g, 256, kPackSmem, ctx->stream>>>(
-          sp.d_probs, sp.d_packA_prefix, sp.nprob, sp.tilesA, 0, chunk, BM, sp.rowsA, A, sp.d_EA,
-          sp.d_RA, (__nv_bfloat16*)sp.d_packA);
+          sp.d_probs, side ? sp.d_packB_prefix : sp.d_packA_prefix, sp.nprob, ntile, side, chunk,
+          side ? BN : BM, side ? sp.rowsB : sp.rowsA, X, E, R,
+          (__nv_bfloat16*)(side ? sp.d_packB : sp.d_packA));
+      MPSG_CUDA(cudaGetLastError());
+      ctx->kernel_launches++;
     }
-    MPSG_CUDA(cudaGetLastError());
-    ctx->kernel_launches += 2;
-  }
-  if (what & kPackB) {
-    KernelTimer timer(ctx, kKindPack);
-    if (sp.nrowsB) {
-      int g = (int)std::min<int64_t>((sp.nrowsB + 255) / 256, (int64_t)ctx->num_sms * 8);
-      pack_exponents_kernel<<<g, 256, 0, ctx->stream>>>(sp.d_probs, sp.d_rowB_prefix, sp.nprob,
-                                                       sp.nrowsB, 1, chunk, B, sp.d_EB, sp.d_CB);
-    }
-    if (sp.tilesB) {
-      int g = (int)std::min<int64_t>(sp.tilesB, (int64_t)ctx->num_sms * 6);
-      pack_slices_kernel<S><<<g, 256, kPackSmem, ctx->stream>>>(
-          sp.d_probs, sp.d_packB_prefix, sp.nprob, sp.tilesB, 1, chunk, BN, sp.rowsB, B, sp.d_EB,
-          sp.d_CB, (__nv_bfloat16*)sp.d_packB);
-    }
-    MPSG_CUDA(cudaGetLastError());
-    ctx->kernel_launches += 2;
   }
   if (!(what & kRunGemm)) return;
   static bool attr_set = false;
@@ -782,6 +823,11 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
   MPSG_CUDA(cudaGetLastError());
   ctx->kernel_launches++;
   ctx->gemm_flops += sp.flops;
+  if (ctx->debug_sync) {
+    MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int e = read_error(ctx, sp);
+    if (e) throw Error(kErrCuda, "split GEMM: a bounded wait expired (role code " + std::to_string(e) + ")");
+  }
 }
 
 void launch_split_gemm(Context* ctx, SplitPlan& sp, const double* A, const double* B, double* C,

@@ -33,6 +33,8 @@ void context_init(Context* ctx, int device) {
   MPSG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
   MPSG_CUDA(cudaMalloc(&ctx->d_partials, sizeof(double) * (ctx->num_sms * 4 + 64)));
   MPSG_CUDA(cudaMallocHost(&ctx->h_pinned, sizeof(double) * 64));
+  const char* dbg = std::getenv("MPSG_DEBUG_SYNC");
+  ctx->debug_sync = dbg && dbg[0] == '1';
 }
 
 static cudaEvent_t take_event(Context* ctx) {

@@ -93,11 +93,12 @@ struct Context : std::enable_shared_from_this<Context> {
   std::unordered_map<std::string, std::shared_ptr<DevReleg>> releg_cache;
   std::unordered_map<std::string, std::shared_ptr<DevGemmPlan>> matmul_cache;
   int64_t kernel_launches = 0;    // launches of this library's kernels
+  bool debug_sync = false;        // MPSG_DEBUG_SYNC=1: synchronise and check after tensor-core GEMMs
   double gemm_flops = 0;          // algorithmic flops issued through block GEMMs
   void* solver = nullptr;         // cusolverDnHandle_t, created on first SVD
   void (*solver_destroy)(void*) = nullptr;
   // optional per-kernel-class event timing (see mpsg_ctx_set_timing)
-  static constexpr int kKinds = 5;
+  static constexpr int kKinds = 6;
   bool timing = false;
   struct TimedLaunch {
     cudaEvent_t a, b;
@@ -105,13 +106,20 @@ struct Context : std::enable_shared_from_this<Context> {
   };
   std::vector<TimedLaunch> events[kKinds];
   std::vector<cudaEvent_t> event_pool;
-  double timed_ms[kKinds] = {0, 0, 0, 0, 0};
-  int64_t timed_launches[kKinds] = {0, 0, 0, 0, 0};
-  double timed_flops[kKinds] = {0, 0, 0, 0, 0};
+  double timed_ms[kKinds] = {0, 0, 0, 0, 0, 0};
+  int64_t timed_launches[kKinds] = {0, 0, 0, 0, 0, 0};
+  double timed_flops[kKinds] = {0, 0, 0, 0, 0, 0};
   ~Context();
 };
 
-enum KernelKind { kKindCopy = 0, kKindGemmF64 = 1, kKindGemmSplit = 2, kKindPack = 3, kKindVec = 4 };
+enum KernelKind {
+  kKindCopy = 0,
+  kKindGemmF64 = 1,
+  kKindGemmSplit = 2,
+  kKindPack = 3,       // split operand packing: exponent pass
+  kKindVec = 4,
+  kKindPackSlices = 5  // split operand packing: slice pass
+};
 
 // RAII bracket of one launch with events when timing is enabled.
 struct KernelTimer {

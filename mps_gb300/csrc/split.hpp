@@ -26,6 +26,7 @@ struct SplitPlan {
   int S = 0;
   int nprob = 0;
   int64_t ntiles = 0, tilesA = 0, tilesB = 0, rowsA = 0, rowsB = 0, nrowsA = 0, nrowsB = 0;
+  int64_t rowsRA = 0, rowsCB = 0;  // entries of the row-reference exponent arrays
   double flops = 0;
   std::vector<Problem> probs;
   Problem* d_probs = nullptr;

@@ -145,7 +145,8 @@ class Context:
         call("mpsg_ctx_stream", self._h, C.byref(s))
         return s.value or 0
 
-    KERNEL_KINDS = {"copy": 0, "gemm_f64": 1, "gemm_split": 2, "pack": 3, "vec": 4}
+    KERNEL_KINDS = {"copy": 0, "gemm_f64": 1, "gemm_split": 2, "pack": 3, "vec": 4,
+                    "pack_slices": 5}
 
     def set_timing(self, enable: bool):
         """Bracket every kernel launch with CUDA events (resets the accumulated times)."""
