@@ -183,6 +183,11 @@ int mpsg_heff2_apply(mpsg_ctx* ctx, mpsg_heff* op, const mpsg_tensor* v, mpsg_te
 /* Algorithmic flops of one application in the reference contraction order. */
 int mpsg_heff2_flops(const mpsg_heff* op, double* flops);
 int mpsg_heff2_free(mpsg_heff* op);
+/* Host self-check of the tensor-core H_eff plans for these structures (any tensors, also
+ * structure-only ones): every copy and GEMM window in bounds, every output element written
+ * once, and the composed intermediate copy equal to the two-step copy. */
+int mpsg_plan_heff2_check(const mpsg_tensor* v, const mpsg_tensor* envl, const mpsg_tensor* envr,
+                          const mpsg_tensor* w1, const mpsg_tensor* w2);
 
 /* ---- vector operations used by the Krylov solver (src/symtensor.jl:252-323) -------------- */
 int mpsg_fill(mpsg_ctx* ctx, mpsg_tensor* a, double x);                          /* :166-171 */

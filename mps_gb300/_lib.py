@@ -93,6 +93,7 @@ SIGNATURES = {
     "mpsg_heff2_apply": [P, P, P, PP],
     "mpsg_heff2_flops": [P, PF64],
     "mpsg_heff2_free": [P],
+    "mpsg_plan_heff2_check": [P, P, P, P, P],
     "mpsg_meta_create": [I32, I32, PI32, PI32, PI64, PI32, PP],
     "mpsg_plan_permutelegs": [P, PI32, PP],
     "mpsg_plan_fuselegs": [P, I32, I32, I32, PP],

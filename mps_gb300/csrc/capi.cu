@@ -556,6 +556,18 @@ int mpsg_heff2_free(mpsg_heff* op) {
   return guarded([&] { delete op; });
 }
 
+int mpsg_plan_heff2_check(const mpsg_tensor* v, const mpsg_tensor* envl, const mpsg_tensor* envr,
+                          const mpsg_tensor* w1, const mpsg_tensor* w2) {
+  return guarded([&] {
+    need(v, "v");
+    need(envl, "envl");
+    need(envr, "envr");
+    need(w1, "w1");
+    need(w2, "w2");
+    mpsg::check_heff_folded(v->t.meta, envl->t.meta, envr->t.meta, w1->t.meta, w2->t.meta);
+  });
+}
+
 static mpsg_tensor* meta_only(const mpsg::TensorMeta& m) {
   mpsg::DeviceTensor t;
   t.meta = m;

@@ -2,12 +2,13 @@
 // splitleg, SymMatrix fusion and the split+permute of contraction outputs are all such lists).
 //
 // Two tile shapes, chosen per task on the host:
-//   * flat  : source and destination share their unit-stride axis (or one side has none);
-//             the task is walked in destination order, 2048 elements per tile, so writes and
-//             reads are both coalesced along that axis;
-//   * tile  : the unit-stride axes differ (a transpose); a 32x32 tile is staged in shared
-//             memory so that reads are coalesced along the source axis and writes along the
-//             destination axis.
+//   * rows : source and destination share their unit-stride axis a (or one side has none);
+//            the task is walked as rows along axis a: each warp decodes a row's multi-index once
+//            (magic-number division, no per-element div/mod) and its lanes stream the row, so
+//            reads and writes are coalesced along a;
+//   * tile : the unit-stride axes differ (a transpose); a 32x32 tile is staged in shared
+//            memory so that reads are coalesced along the source axis and writes along the
+//            destination axis.
 // The kernel is persistent: a grid sized to the SM count walks a global tile index and finds its
 // task by binary search in the per-task tile prefix sums.
 #include "runtime.hpp"
@@ -16,24 +17,39 @@ namespace mpsg {
 
 namespace {
 
-constexpr int kFlatTile = 2048;
+constexpr int kRowTile = 2048;  // target elements per row-mode tile
 constexpr int kT = 32;
 
+// Per-task launch data: axis roles, tiling and division constants (q = (umulhi(n,m)+n) >> s
+// equals n / ext for every n < 2^31).
+struct TaskAux {
+  int32_t mode, a, b, rows_per_tile;
+  int64_t outer;                  // rows (row mode)
+  uint32_t mag[kMaxTaskDims];
+  uint32_t shf[kMaxTaskDims];
+};
+
 struct TaskView {
-  int nd;
-  int a, b, mode;
+  int nd, a, b, mode, rpt;
+  int64_t outer;
   int64_t ext[kMaxTaskDims], sstr[kMaxTaskDims], dstr[kMaxTaskDims];
+  uint32_t mag[kMaxTaskDims], shf[kMaxTaskDims];
   int64_t soff, doff, first_tile;
 };
 
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, uint32_t m, uint32_t s) {
+  return (__umulhi(n, m) + n) >> s;
+}
+
 __global__ void __launch_bounds__(256) copy_tasks_kernel(
     const CopyTask* __restrict__ tasks, const int64_t* __restrict__ prefix,
-    const int32_t* __restrict__ modes, int ntasks, int64_t ntiles,
-    const double* __restrict__ src, double* __restrict__ dst) {
+    const TaskAux* __restrict__ aux, int ntasks, int64_t ntiles, const double* __restrict__ src,
+    double* __restrict__ dst) {
   __shared__ double tile[kT][kT + 1];
   __shared__ TaskView tv;
   __shared__ int cur_task;
   const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31;
   if (tid == 0) cur_task = -1;
   __syncthreads();
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -46,18 +62,22 @@ __global__ void __launch_bounds__(256) copy_tasks_kernel(
       }
       if (lo != cur_task) {
         const CopyTask& T = tasks[lo];
+        const TaskAux& X = aux[lo];
         tv.nd = T.nd;
         for (int i = 0; i < T.nd; ++i) {
           tv.ext[i] = T.ext[i];
           tv.sstr[i] = T.sstr[i];
           tv.dstr[i] = T.dstr[i];
+          tv.mag[i] = X.mag[i];
+          tv.shf[i] = X.shf[i];
         }
         tv.soff = T.soff;
         tv.doff = T.doff;
-        int32_t m = modes[lo];
-        tv.mode = m & 0xff;
-        tv.a = (m >> 8) & 0xff;
-        tv.b = (m >> 16) & 0xff;
+        tv.mode = X.mode;
+        tv.a = X.a;
+        tv.b = X.b;
+        tv.rpt = X.rows_per_tile;
+        tv.outer = X.outer;
         tv.first_tile = prefix[lo];
         cur_task = lo;
       }
@@ -66,26 +86,24 @@ __global__ void __launch_bounds__(256) copy_tasks_kernel(
     const int64_t lt = t - tv.first_tile;
     const int nd = tv.nd;
     if (tv.mode == 0) {
-      // flat walk, axis a innermost
+      // row walk along axis a
       const int a = tv.a;
-      int64_t total = 1;
-      for (int i = 0; i < nd; ++i) total *= tv.ext[i];
-      const int64_t base = lt * kFlatTile;
-      for (int e = tid; e < kFlatTile; e += 256) {
-        int64_t f = base + e;
-        if (f >= total) break;
-        int64_t q = f / tv.ext[a];
-        int64_t ia = f - q * tv.ext[a];
-        int64_t so = tv.soff + ia * tv.sstr[a], dof = tv.doff + ia * tv.dstr[a];
+      const int64_t ea = tv.ext[a];
+      const int64_t sa = tv.sstr[a], da = tv.dstr[a];
+      const int64_t r0 = lt * tv.rpt;
+      const int64_t r1 = min(r0 + tv.rpt, tv.outer);
+      for (int64_t row = r0 + warp; row < r1; row += 8) {
+        uint32_t q = (uint32_t)row;
+        int64_t so = tv.soff, dof = tv.doff;
         for (int i = 0; i < nd; ++i) {
           if (i == a) continue;
-          int64_t qi = q / tv.ext[i];
-          int64_t ii = q - qi * tv.ext[i];
+          const uint32_t qi = fdiv(q, tv.mag[i], tv.shf[i]);
+          const int64_t ii = (int64_t)(q - qi * (uint32_t)tv.ext[i]);
           q = qi;
           so += ii * tv.sstr[i];
           dof += ii * tv.dstr[i];
         }
-        dst[dof] = __ldg(src + so);
+        for (int64_t ia = lane; ia < ea; ia += 32) dst[dof + ia * da] = __ldg(src + so + ia * sa);
       }
     } else {
       const int a = tv.a, b = tv.b;
@@ -97,11 +115,12 @@ __global__ void __launch_bounds__(256) copy_tasks_kernel(
       const int64_t ib = q % tb;
       q /= tb;
       int64_t so = tv.soff, dof = tv.doff;
+      uint32_t q32 = (uint32_t)q;
       for (int i = 0; i < nd; ++i) {
         if (i == a || i == b) continue;
-        int64_t qi = q / tv.ext[i];
-        int64_t ii = q - qi * tv.ext[i];
-        q = qi;
+        const uint32_t qi = fdiv(q32, tv.mag[i], tv.shf[i]);
+        const int64_t ii = (int64_t)(q32 - qi * (uint32_t)tv.ext[i]);
+        q32 = qi;
         so += ii * tv.sstr[i];
         dof += ii * tv.dstr[i];
       }
@@ -121,6 +140,13 @@ __global__ void __launch_bounds__(256) copy_tasks_kernel(
   }
 }
 
+void magic_u31(uint32_t d, uint32_t& m, uint32_t& s) {
+  uint32_t l = 0;
+  while (((uint64_t)1 << l) < d) ++l;
+  m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << l) - d)) / d + 1);
+  s = l;
+}
+
 }  // namespace
 
 void DevCopyPlan::upload(const std::vector<CopyTask>& tasks, bool identity_) {
@@ -128,7 +154,7 @@ void DevCopyPlan::upload(const std::vector<CopyTask>& tasks, bool identity_) {
   identity = identity_;
   ntasks = (int)tasks.size();
   std::vector<int64_t> prefix(ntasks + 1, 0);
-  std::vector<int32_t> modes(ntasks, 0);
+  std::vector<TaskAux> aux(ntasks);
   elems = 0;
   for (int k = 0; k < ntasks; ++k) {
     const CopyTask& T = tasks[k];
@@ -137,39 +163,46 @@ void DevCopyPlan::upload(const std::vector<CopyTask>& tasks, bool identity_) {
       if (T.dstr[i] < T.dstr[a]) a = i;
       if (T.sstr[i] < T.sstr[b]) b = i;
     }
-    int64_t n = T.numel();
+    const int64_t n = T.numel();
+    if (n >= ((int64_t)1 << 31)) throw Error(kErrUnsupported, "copy task above 2^31 elements");
     elems += n;
+    TaskAux& X = aux[k];
+    for (int i = 0; i < T.nd; ++i) magic_u31((uint32_t)T.ext[i], X.mag[i], X.shf[i]);
     int64_t tiles;
-    int mode;
     if (a == b || T.nd == 1 || T.sstr[b] != 1 || T.dstr[a] != 1) {
-      mode = 0;
-      tiles = (n + kFlatTile - 1) / kFlatTile;
+      X.mode = 0;
+      X.outer = n / T.ext[a];
+      X.rows_per_tile = (int)std::max<int64_t>(1, std::min<int64_t>(X.outer, kRowTile / T.ext[a]));
+      tiles = (X.outer + X.rows_per_tile - 1) / X.rows_per_tile;
     } else {
-      mode = 1;
+      X.mode = 1;
+      X.outer = 0;
+      X.rows_per_tile = 0;
       int64_t rest = n / (T.ext[a] * T.ext[b]);
       tiles = ((T.ext[a] + kT - 1) / kT) * ((T.ext[b] + kT - 1) / kT) * rest;
     }
-    modes[k] = mode | (a << 8) | (b << 16);
+    X.a = a;
+    X.b = b;
     prefix[k + 1] = prefix[k] + tiles;
   }
   ntiles = prefix[ntasks];
   if (ntasks == 0) return;
   MPSG_CUDA(cudaMalloc(&d_tasks, sizeof(CopyTask) * ntasks));
   MPSG_CUDA(cudaMalloc(&d_prefix, sizeof(int64_t) * (ntasks + 1)));
-  MPSG_CUDA(cudaMalloc(&d_mode, sizeof(int32_t) * ntasks));
+  MPSG_CUDA(cudaMalloc(&d_aux, sizeof(TaskAux) * ntasks));
   MPSG_CUDA(cudaMemcpy(d_tasks, tasks.data(), sizeof(CopyTask) * ntasks, cudaMemcpyHostToDevice));
   MPSG_CUDA(cudaMemcpy(d_prefix, prefix.data(), sizeof(int64_t) * (ntasks + 1),
                        cudaMemcpyHostToDevice));
-  MPSG_CUDA(cudaMemcpy(d_mode, modes.data(), sizeof(int32_t) * ntasks, cudaMemcpyHostToDevice));
+  MPSG_CUDA(cudaMemcpy(d_aux, aux.data(), sizeof(TaskAux) * ntasks, cudaMemcpyHostToDevice));
 }
 
 void DevCopyPlan::release() {
   if (d_tasks) cudaFree(d_tasks);
   if (d_prefix) cudaFree(d_prefix);
-  if (d_mode) cudaFree(d_mode);
+  if (d_aux) cudaFree(d_aux);
   d_tasks = nullptr;
   d_prefix = nullptr;
-  d_mode = nullptr;
+  d_aux = nullptr;
   ntasks = 0;
   ntiles = 0;
 }
@@ -185,7 +218,7 @@ void launch_copy(Context* ctx, const DevCopyPlan& p, const double* src, double* 
   int64_t grid = std::min<int64_t>(p.ntiles, (int64_t)ctx->num_sms * 8);
   KernelTimer timer(ctx, kKindCopy);
   copy_tasks_kernel<<<(unsigned)grid, dim3(32, 8), 0, ctx->stream>>>(
-      p.d_tasks, p.d_prefix, p.d_mode, p.ntasks, p.ntiles, src, dst);
+      p.d_tasks, p.d_prefix, (const TaskAux*)p.d_aux, p.ntasks, p.ntiles, src, dst);
   MPSG_CUDA(cudaGetLastError());
   ctx->kernel_launches++;
 }

@@ -269,7 +269,8 @@ constexpr int kNoExponent = (int)0x80808080;  // byte pattern of the reset: "row
 // Loads are coalesced along whichever operand axis is contiguous.
 __global__ void __launch_bounds__(256) pack_exponents_kernel(
     const Problem* __restrict__ probs, const int64_t* __restrict__ item_prefix, int nprob,
-    int64_t nitems, int is_b, int chunk, const double* __restrict__ X, int16_t* __restrict__ E,
+    int64_t nitems, int is_b, int chunk, int write_e, const double* __restrict__ X,
+    int16_t* __restrict__ E,
     int32_t* __restrict__ R) {
   __shared__ unsigned long long red[8][33];
   const int t = threadIdx.x;
@@ -303,7 +304,7 @@ __global__ void __launch_bounds__(256) pack_exponents_kernel(
 #pragma unroll
         for (int g = 0; g < 8; ++g) mm = red[g][t] > mm ? red[g][t] : mm;
         const int e = exp_bound(mm);
-        E[ebase + (r0 + t) * P.nch + c] = (int16_t)e;
+        if (write_e) E[ebase + (r0 + t) * P.nch + c] = (int16_t)e;
         if (mm) atomicMax(&R[rbase + r0 + t], e);
       }
       __syncthreads();
@@ -326,7 +327,7 @@ __global__ void __launch_bounds__(256) pack_exponents_kernel(
         }
         if (lane == 0) {
           const int e = exp_bound(m);
-          E[ebase + r * P.nch + c] = (int16_t)e;
+          if (write_e) E[ebase + r * P.nch + c] = (int16_t)e;
           if (m) atomicMax(&R[rbase + r], e);
         }
       }
@@ -338,7 +339,7 @@ __global__ void __launch_bounds__(256) pack_exponents_kernel(
 template <int S>
 __global__ void __launch_bounds__(256) pack_slices_kernel(
     const Problem* __restrict__ probs, const int64_t* __restrict__ tile_prefix, int nprob,
-    int64_t ntiles, int is_b, int chunk, int rows_per_tile, int64_t rows_total,
+    int64_t ntiles, int is_b, int chunk, int use_r, int rows_per_tile, int64_t rows_total,
     const double* __restrict__ X, const int16_t* __restrict__ E, const int32_t* __restrict__ R,
     __nv_bfloat16* __restrict__ out) {
   constexpr int kBeta = kSliceBits;
@@ -351,81 +352,86 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
     const int64_t ri = lt / P.nks, kstep = lt % P.nks;
     int64_t rows, off, rs, ks;
     operand_geom(P, is_b, rows, off, rs, ks);
-    const int64_t r0 = ri * rows_per_tile, k0 = kstep * 64;
-    // stage the FP64 tile in shared memory, coalesced along the contiguous axis
-    if (rs == 1) {
-      for (int i = threadIdx.x; i < rows_per_tile * 64; i += 256) {
-        const int rr = i % rows_per_tile, kk = i / rows_per_tile;
-        const int64_t r = r0 + rr, k = k0 + kk;
-        tile[rr][kk] = (r < rows && k < P.K) ? X[off + r * rs + k * ks] : 0.0;
-      }
-    } else {
-      for (int i = threadIdx.x; i < rows_per_tile * 64; i += 256) {
-        const int kk = i % 64, rr = i / 64;
-        const int64_t r = r0 + rr, k = k0 + kk;
-        tile[rr][kk] = (r < rows && k < P.K) ? X[off + r * rs + k * ks] : 0.0;
-      }
-    }
-    __syncthreads();
+    const int64_t k0 = kstep * 64;
     const int64_t rbase = is_b ? P.rB : P.rA;
     const int64_t ebase = is_b ? P.eB : P.eA;
     const int c = (int)(k0 / chunk);
     const int64_t tile_row0 = (is_b ? P.tB : P.tA) * rows_per_tile + lt * rows_per_tile;
-    for (int i = threadIdx.x; i < rows_per_tile * 8; i += 256) {
-      const int g8 = i % 8, rr = i / 8;
-      const int64_t r = r0 + rr;
-      int e = 0, Rr = 0;
-      if (r < rows) {
-        e = E[ebase + r * P.nch + c];
-        Rr = R[rbase + r];
-        if (Rr == kNoExponent) Rr = e;  // the whole row is zero: every slice is zero
+    // tiles of up to 256 rows are processed in halves of 128 rows through shared memory
+    for (int h0 = 0; h0 < rows_per_tile; h0 += 128) {
+      const int hrows = min(128, rows_per_tile - h0);  // rows of this tile handled in this pass
+      const int64_t r0 = ri * rows_per_tile + h0;
+      // stage the FP64 half tile in shared memory, coalesced along the contiguous axis
+      if (rs == 1) {
+        for (int i = threadIdx.x; i < hrows * 64; i += 256) {
+          const int rr = i % hrows, kk = i / hrows;
+          const int64_t r = r0 + rr, k = k0 + kk;
+          tile[rr][kk] = (r < rows && k < P.K) ? X[off + r * rs + k * ks] : 0.0;
+        }
+      } else {
+        for (int i = threadIdx.x; i < hrows * 64; i += 256) {
+          const int kk = i % 64, rr = i / 64;
+          const int64_t r = r0 + rr, k = k0 + kk;
+          tile[rr][kk] = (r < rows && k < P.K) ? X[off + r * rs + k * ks] : 0.0;
+        }
       }
-      // per-row slice scales 2^(e - R - beta (q+1)) (0 when below the float range: negligible)
-      float scale[S];
+      __syncthreads();
+      for (int i = threadIdx.x; i < hrows * 8; i += 256) {
+        const int g8 = i % 8, rr = i / 8;
+        const int64_t r = r0 + rr;
+        int e = 0, Rr = 0;
+        if (r < rows) {
+          e = use_r ? R[rbase + r] : E[ebase + r * P.nch + c];
+          Rr = R[rbase + r];
+          if (Rr == kNoExponent) Rr = e;  // the whole row is zero: every slice is zero
+        }
+        // per-row slice scales 2^(e - R - beta (q+1)) (0 below the float range: negligible)
+        float scale[S];
 #pragma unroll
-      for (int q = 0; q < S; ++q) {
-        const int k = e - Rr - kBeta * (q + 1);
-        scale[q] = k >= -126 ? __uint_as_float((uint32_t)(k + 127) << 23) : 0.f;
-      }
-      // F = round(x * 2^(beta S - e)) needs at most beta*S + 1 <= 29 bits: 32-bit integer work
-      // on the top 32 bits of the significand (hi word: 20 bits, lo word: 11 bits, implicit 1)
-      const int sbase = 1054 + e - kBeta * S;  // F = m32 >> (sbase - eb), rounded
-      uint32_t packed[S][4];
+        for (int q = 0; q < S; ++q) {
+          const int k = e - Rr - kBeta * (q + 1);
+          scale[q] = k >= -126 ? __uint_as_float((uint32_t)(k + 127) << 23) : 0.f;
+        }
+        // F = round(x * 2^(beta S - e)) needs at most beta*S + 1 <= 29 bits: 32-bit integer
+        // work on the top 32 bits of the significand (hi word 20 bits, lo word 11, implicit 1)
+        const int sbase = 1054 + e - kBeta * S;  // F = m32 >> (sbase - eb), rounded
+        uint32_t packed[S][4];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const double x = tile[rr][g8 * 8 + j];
-        const int hw = __double2hiint(x);
-        const uint32_t lw = (uint32_t)__double2loint(x);
-        const int eb = (hw >> 20) & 0x7ff;
-        const uint32_t m32 = (((uint32_t)hw << 11) | (lw >> 21)) | 0x80000000u;
-        const int s = sbase - eb;  // >= 32 - beta*S > 0 for every element of the row chunk
-        int F = 0;
-        if (eb != 0 && s <= 32 && r < rows) {
-          F = (int)(((m32 >> (s - 1)) + 1u) >> 1);  // round half up
-          if (hw < 0) F = -F;
+        for (int j = 0; j < 8; ++j) {
+          const double x = tile[rr][g8 * 8 + j];
+          const int hw = __double2hiint(x);
+          const uint32_t lw = (uint32_t)__double2loint(x);
+          const int eb = (hw >> 20) & 0x7ff;
+          const uint32_t m32 = (((uint32_t)hw << 11) | (lw >> 21)) | 0x80000000u;
+          const int s = sbase - eb;  // >= 32 - beta*S > 0 for every element of the row chunk
+          int F = 0;
+          if (eb != 0 && s <= 32 && r < rows) {
+            F = (int)(((m32 >> (s - 1)) + 1u) >> 1);  // round half up
+            if (hw < 0) F = -F;
+          }
+#pragma unroll
+          for (int q = 0; q < S; ++q) {
+            const int shq = kBeta * (S - 1 - q);
+            int tq = F;
+            if (shq > 0) {
+              tq = (F + (1 << (shq - 1))) >> shq;
+              F -= tq * (1 << shq);
+            }
+            const float v = (float)tq * scale[q];  // exact: |tq| <= 2^beta
+            const uint16_t h = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+            if (j & 1) packed[q][j >> 1] |= (uint32_t)h << 16;
+            else packed[q][j >> 1] = (uint32_t)h;
+          }
         }
 #pragma unroll
         for (int q = 0; q < S; ++q) {
-          const int shq = kBeta * (S - 1 - q);
-          int tq = F;
-          if (shq > 0) {
-            tq = (F + (1 << (shq - 1))) >> shq;
-            F -= tq * (1 << shq);
-          }
-          const float v = (float)tq * scale[q];  // exact: |tq| <= 2^beta
-          const uint16_t h = __bfloat16_as_ushort(__float2bfloat16_rn(v));
-          if (j & 1) packed[q][j >> 1] |= (uint32_t)h << 16;
-          else packed[q][j >> 1] = (uint32_t)h;
+          uint4 w = make_uint4(packed[q][0], packed[q][1], packed[q][2], packed[q][3]);
+          const int64_t idx = ((int64_t)q * rows_total + tile_row0 + h0 + rr) * 64 + g8 * 8;
+          *reinterpret_cast<uint4*>(out + idx) = w;
         }
       }
-#pragma unroll
-      for (int q = 0; q < S; ++q) {
-        uint4 w = make_uint4(packed[q][0], packed[q][1], packed[q][2], packed[q][3]);
-        const int64_t idx = ((int64_t)q * rows_total + tile_row0 + rr) * 64 + g8 * 8;
-        *reinterpret_cast<uint4*>(out + idx) = w;
-      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
@@ -447,12 +453,18 @@ struct Cfg {
   static constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
 };
 
+// Static schedule shared by the three roles: the host sorts output tiles by decreasing K and the
+// CTAs deal them out in snake order (b, 2G-1-b, 2G+b, ...), which balances ragged sectors.
+__device__ __forceinline__ int64_t sched_pos(int64_t i, int G, int b) {
+  return i * G + ((i & 1) ? (G - 1 - b) : b);
+}
+
 template <int S>
 __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
     const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-    const Problem* __restrict__ probs, const int64_t* __restrict__ tile_prefix, int nprob,
-    int64_t ntiles, const int32_t* __restrict__ RA, const int32_t* __restrict__ CB,
-    double* __restrict__ C, int* __restrict__ err) {
+    const Problem* __restrict__ probs, const int4* __restrict__ tiles, int64_t ntiles,
+    const int32_t* __restrict__ RA, const int32_t* __restrict__ CB, double* __restrict__ C,
+    int* __restrict__ err) {
   using CF = Cfg<S>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -490,18 +502,20 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
-      for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
-        const int p = find_problem(tile_prefix, nprob, t);
-        const Problem& P = probs[p];
-        const int64_t lt = t - tile_prefix[p];
-        const int64_t mi = lt % P.mt, ni = lt / P.mt;
-        for (int ks = 0; ks < P.nks; ++ks) {
+      for (int64_t i = 0; !*abort_flag; ++i) {
+        const int64_t pos = sched_pos(i, gridDim.x, blockIdx.x);
+        if (pos >= ntiles) break;
+        const int4 tr = tiles[pos];
+        const int nks = probs[tr.x].nks;
+        const int64_t baseA = (probs[tr.x].tA + (int64_t)tr.y * nks) * BM;
+        const int64_t baseB = (probs[tr.x].tB + (int64_t)tr.z * nks) * BN;
+        for (int ks = 0; ks < nks; ++ks) {
           if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) break;
           uint8_t* sA = smem + stage * CF::kStageBytes;
           uint8_t* sB = sA + S * CF::kABytes;
           mbar_expect_tx(&full[stage], CF::kStageBytes);
-          const int rowA = (int)((P.tA + mi * P.nks + ks) * BM);
-          const int rowB = (int)((P.tB + ni * P.nks + ks) * BN);
+          const int rowA = (int)(baseA + (int64_t)ks * BM);
+          const int rowB = (int)(baseB + (int64_t)ks * BN);
 #pragma unroll
           for (int s = 0; s < S; ++s) tma_load_3d(sA + s * CF::kABytes, &tmA, &full[stage], 0, rowA, s);
 #pragma unroll
@@ -521,16 +535,17 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
       uint32_t phase = 0;
       int64_t use = 0;
       bool issued = false;
-      for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
-        const int p = find_problem(tile_prefix, nprob, t);
-        const Problem& P = probs[p];
-        for (int c0 = 0; c0 < P.nks && !*abort_flag; c0 += CF::kChunkSteps) {
+      for (int64_t i = 0; !*abort_flag; ++i) {
+        const int64_t pos = sched_pos(i, gridDim.x, blockIdx.x);
+        if (pos >= ntiles) break;
+        const int nks = probs[tiles[pos].x].nks;
+        for (int c0 = 0; c0 < nks && !*abort_flag; c0 += CF::kChunkSteps) {
           const int buf = (int)(use % CF::kBufs);
           const uint32_t bph = (uint32_t)((use / CF::kBufs) & 1);
           if (!mbar_wait(&tempty[buf], bph ^ 1, abort_flag, err, 2)) break;
           tc_fence_after();
           uint32_t init = 0;  // bit g: accumulator g already written in this chunk
-          const int c1 = min(P.nks, c0 + CF::kChunkSteps);
+          const int c1 = min(nks, c0 + CF::kChunkSteps);
           for (int ks = c0; ks < c1; ++ks) {
             if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) break;
             tc_fence_after();
@@ -573,11 +588,12 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
     const int lrow = 32 * (warp & 3) + lane;
     const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
     int64_t use = 0;
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-      const int p = find_problem(tile_prefix, nprob, t);
-      const Problem& P = probs[p];
-      const int64_t lt = t - tile_prefix[p];
-      const int64_t mi = lt % P.mt, ni = lt / P.mt;
+    for (int64_t i = 0;; ++i) {
+      const int64_t pos = sched_pos(i, gridDim.x, blockIdx.x);
+      if (pos >= ntiles) break;
+      const int4 tr = tiles[pos];
+      const Problem P = probs[tr.x];
+      const int64_t mi = tr.y, ni = tr.z;
       float hi[BN], lo[BN];
 #pragma unroll
       for (int j = 0; j < BN; ++j) {
@@ -634,6 +650,224 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
 }
 
 // ------------------------------------------------------------------------------------------
+// fast mode (S <= 3): one FP32 accumulator, per-row scale over the whole K, 128 x 256 tiles
+// ------------------------------------------------------------------------------------------
+// Every slice already carries its true scale 2^(e(i) - R(i) - beta(p+1)), so the products of
+// all pairs (p, q) with p + q < S can share one FP32 accumulator: FP32 rounding (2^-24) stays
+// below the 2^(-7 S) slicing error for S <= 3.  Without chunk flushes the epilogue is one TMEM
+// read, one exponent shift and one FP64 store per element, which lets the tile grow to
+// 128 x 256 (double-buffered: 2 x 256 TMEM columns) and the K step shrink to 32 (64-byte
+// swizzle), doubling the MMA work per byte staged in shared memory.
+constexpr int BNF = 256, BKF = 32;
+
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;           // stride byte offset: 8 rows x 64 B
+  d |= (uint64_t)1 << 46;                    // descriptor version
+  d |= (uint64_t)4 << 61;                    // 64-byte swizzle
+  return d;
+}
+
+// v * 2^E as FP64 from the FP32 bit pattern (integer instructions only)
+__device__ __forceinline__ double f32_to_f64_scaled(float v, int E) {
+  const uint32_t u = __float_as_uint(v);
+  const int ef = (int)((u >> 23) & 0xff);
+  if (ef == 0) return 0.0;  // zero (FP32 denormals are far below the accuracy of this path)
+  const long long be = (long long)ef - 127 + 1023 + E;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  if (be <= 0) return 0.0;
+  if (be >= 2047) return __longlong_as_double((long long)(sign | (0x7ffull << 52)));
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)be << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+template <int S>
+struct FastCfg {
+  static constexpr int kABytes = BM * BKF * 2;   // 8 KB
+  static constexpr int kBBytes = BNF * BKF * 2;  // 16 KB
+  static constexpr int kStageBytes = S * (kABytes + kBBytes);
+  static constexpr int kStages = (220 * 1024) / kStageBytes > 6 ? 6 : (220 * 1024) / kStageBytes;
+  static constexpr int kTmemCols = 2 * BNF;
+  static constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+};
+
+template <int S>
+__global__ void __launch_bounds__(192, 1) split_gemm_fast_kernel(
+    const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+    const Problem* __restrict__ probs, const int4* __restrict__ tiles, int64_t ntiles,
+    const int32_t* __restrict__ RA, const int32_t* __restrict__ CB, double* __restrict__ C,
+    int* __restrict__ err) {
+  using CF = FastCfg<S>;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = (uint64_t*)(smem + CF::kStages * CF::kStageBytes);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + CF::kStages;
+  uint64_t* tfull = bars + 2 * CF::kStages;
+  uint64_t* tempty = tfull + 2;
+  uint64_t* drain = tempty + 2;
+  uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < CF::kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 128);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, CF::kTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      for (int64_t i = 0; !*abort_flag; ++i) {
+        const int64_t pos = sched_pos(i, gridDim.x, blockIdx.x);
+        if (pos >= ntiles) break;
+        const int4 tr = tiles[pos];
+        const int nks = probs[tr.x].nks;
+        const int64_t baseA = (probs[tr.x].tA + (int64_t)tr.y * nks) * BM;
+        const int64_t baseB = (probs[tr.x].tB + (int64_t)tr.z * nks) * BNF;
+        for (int kb = 0; kb < 2 * nks; ++kb) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) break;
+          uint8_t* sA = smem + stage * CF::kStageBytes;
+          uint8_t* sB = sA + S * CF::kABytes;
+          mbar_expect_tx(&full[stage], CF::kStageBytes);
+          const int x = (kb & 1) * BKF;
+          const int rowA = (int)(baseA + (int64_t)(kb >> 1) * BM);
+          const int rowB = (int)(baseB + (int64_t)(kb >> 1) * BNF);
+#pragma unroll
+          for (int s = 0; s < S; ++s) tma_load_3d(sA + s * CF::kABytes, &tmA, &full[stage], x, rowA, s);
+#pragma unroll
+          for (int s = 0; s < S; ++s) tma_load_3d(sB + s * CF::kBBytes, &tmB, &full[stage], x, rowB, s);
+          if (++stage == CF::kStages) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc = make_idesc(BM, BNF);
+      int stage = 0;
+      uint32_t phase = 0;
+      int64_t use = 0;
+      bool issued = false;
+      for (int64_t i = 0; !*abort_flag; ++i) {
+        const int64_t pos = sched_pos(i, gridDim.x, blockIdx.x);
+        if (pos >= ntiles) break;
+        const int nks = probs[tiles[pos].x].nks;
+        if (nks == 0) continue;
+        const int buf = (int)(use & 1);
+        const uint32_t bph = (uint32_t)((use >> 1) & 1);
+        if (!mbar_wait(&tempty[buf], bph ^ 1, abort_flag, err, 2)) break;
+        tc_fence_after();
+        const uint32_t dcol = tmem_base + (uint32_t)(buf * BNF);
+        uint32_t acc = 0;
+        for (int kb = 0; kb < 2 * nks; ++kb) {
+          if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) break;
+          tc_fence_after();
+          const uint32_t sA = smem_u32(smem + stage * CF::kStageBytes);
+          const uint32_t sB = sA + S * CF::kABytes;
+#pragma unroll
+          for (int pa = 0; pa < S; ++pa) {
+#pragma unroll
+            for (int qb = 0; qb < S - pa; ++qb) {
+              const uint64_t ad = sw64_desc(sA + pa * CF::kABytes);
+              const uint64_t bd = sw64_desc(sB + qb * CF::kBBytes);
+#pragma unroll
+              for (int kk = 0; kk < BKF / 16; ++kk) {
+                umma_bf16(dcol, ad + 2 * kk, bd + 2 * kk, idesc, acc);
+                acc = 1;
+              }
+            }
+          }
+          umma_commit(&empty[stage]);
+          issued = true;
+          if (++stage == CF::kStages) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+        umma_commit(&tfull[buf]);
+        ++use;
+      }
+      if (issued) {
+        umma_commit(drain);
+        volatile int no_abort = 0;
+        mbar_wait(drain, 0, &no_abort, err, 4);
+      }
+    }
+  } else {
+    // ---------------- epilogue: warps 2..5, one TMEM lane (= output row) per thread --------
+    const int lrow = 32 * (warp & 3) + lane;
+    const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
+    int64_t use = 0;
+    for (int64_t i = 0;; ++i) {
+      const int64_t pos = sched_pos(i, gridDim.x, blockIdx.x);
+      if (pos >= ntiles) break;
+      const int4 tr = tiles[pos];
+      const Problem P = probs[tr.x];
+      const int64_t row = (int64_t)tr.y * BM + lrow;
+      const int64_t col0 = (int64_t)tr.z * BNF;
+      double* Cp = C + P.offC + row;
+      if (P.nks == 0) {  // allowed sector without partner blocks: zeros
+        if (row < P.M)
+          for (int j = 0; j < BNF && col0 + j < P.N; ++j) Cp[(col0 + j) * P.ldc] = 0.0;
+        continue;
+      }
+      const int buf = (int)(use & 1);
+      const uint32_t bph = (uint32_t)((use >> 1) & 1);
+      if (!mbar_wait(&tfull[buf], bph, abort_flag, err, 5)) break;
+      tc_fence_after();
+      const int Rr = row < P.M ? RA[P.rA + row] : 0;
+#pragma unroll 1
+      for (int h = 0; h < BNF / 32; ++h) {
+        uint32_t v[32];
+        tmem_ld32(tmem_base + lane_addr + (uint32_t)(buf * BNF + h * 32), v);
+        if (row < P.M) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int64_t col = col0 + h * 32 + j;
+            if (col < P.N) {
+              const int Cc = CB[P.rB + col];
+              const int E = (Rr == kNoExponent || Cc == kNoExponent) ? 0 : Rr + Cc;
+              Cp[col * P.ldc] = f32_to_f64_scaled(__uint_as_float(v[j]), E);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&tempty[buf]);
+      ++use;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem_base, CF::kTmemCols);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------------
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
@@ -655,13 +889,16 @@ static EncodeTiledFn encode_fn() {
   return fn;
 }
 
-static void make_map(CUtensorMap* map, void* base, int64_t rows_total, int S, int box_rows) {
+// Packed operand [S][rows_total][64] bf16; box = box_x K-columns x box_rows rows of one slice.
+static void make_map(CUtensorMap* map, void* base, int64_t rows_total, int S, int box_rows,
+                     int box_x) {
   cuuint64_t gdim[3] = {64, (cuuint64_t)rows_total, (cuuint64_t)S};
   cuuint64_t gstride[2] = {128, (cuuint64_t)rows_total * 128};
-  cuuint32_t box[3] = {64, (cuuint32_t)box_rows, 1};
+  cuuint32_t box[3] = {(cuuint32_t)box_x, (cuuint32_t)box_rows, 1};
   cuuint32_t es[3] = {1, 1, 1};
   CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, gdim, gstride, box, es,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           box_x == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) throw Error(kErrCuda, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
@@ -673,7 +910,11 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   release();
   S = S_;
   if (S < 2 || S > 4) throw Error(kErrUnsupported, "split precision supports 2..4 slices");
-  const int chunk = chunk_for(S);
+  const char* ex = std::getenv("MPSG_SPLIT_EXACT");
+  fast = S <= 3 && !(ex && ex[0] == '1');
+  bn = fast ? BNF : BN;
+  chunk = fast ? (1 << 30) : chunk_for(S);
+  seg = fast ? 256 : chunk;
   probs.clear();
   int64_t tA = 0, tB = 0, rA = 0, rB = 0, eA = 0, eB = 0;
   std::vector<int64_t> tile_prefix(1, 0), packA_prefix(1, 0), packB_prefix(1, 0),
@@ -691,9 +932,9 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
     P.ldb = t.ldb;
     P.ldc = t.ldc;
     P.mt = (int)((t.M + BM - 1) / BM);
-    P.nt = (int)((t.N + BN - 1) / BN);
+    P.nt = (int)((t.N + bn - 1) / bn);
     P.nks = (int)((t.K + BK - 1) / BK);
-    P.nch = (int)((t.K + chunk - 1) / chunk);
+    P.nch = (int)(((int64_t)t.K + chunk - 1) / chunk);
     P.tA = tA;
     P.tB = tB;
     P.rA = rA;
@@ -703,24 +944,33 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
     tA += (int64_t)P.mt * P.nks;
     tB += (int64_t)P.nt * P.nks;
     rA += (int64_t)P.mt * BM;
-    rB += (int64_t)P.nt * BN;
+    rB += (int64_t)P.nt * bn;
     eA += (int64_t)P.mt * BM * std::max(P.nch, 1);
-    eB += (int64_t)P.nt * BN * std::max(P.nch, 1);
+    eB += (int64_t)P.nt * bn * std::max(P.nch, 1);
     tile_prefix.push_back(tile_prefix.back() + (int64_t)P.mt * P.nt);
     packA_prefix.push_back(packA_prefix.back() + (int64_t)P.mt * P.nks);
     packB_prefix.push_back(packB_prefix.back() + (int64_t)P.nt * P.nks);
     // exponent work items: (32-row block, K chunk) pairs
-    rowA_prefix.push_back(rowA_prefix.back() + (P.nks ? ((P.M + 31) / 32) * P.nch : 0));
-    rowB_prefix.push_back(rowB_prefix.back() + (P.nks ? ((P.N + 31) / 32) * P.nch : 0));
+    // (in fast mode the K range is only split for parallelism: segments of `seg` columns)
+    const int64_t nseg = fast ? ((int64_t)t.K + seg - 1) / seg : P.nch;
+    rowA_prefix.push_back(rowA_prefix.back() + (P.nks ? ((P.M + 31) / 32) * nseg : 0));
+    rowB_prefix.push_back(rowB_prefix.back() + (P.nks ? ((P.N + 31) / 32) * nseg : 0));
     flops += 2.0 * t.M * t.N * t.K;
     probs.push_back(P);
   }
   nprob = (int)probs.size();
   ntiles = tile_prefix.back();
+  // output tiles ordered by decreasing K (ties: problem, then M tile) for the snake schedule
+  std::vector<int4> tl;
+  tl.reserve(ntiles);
+  for (int p = 0; p < nprob; ++p)
+    for (int ni = 0; ni < probs[p].nt; ++ni)
+      for (int mi = 0; mi < probs[p].mt; ++mi) tl.push_back(make_int4(p, mi, ni, probs[p].nks));
+  std::stable_sort(tl.begin(), tl.end(), [](const int4& a, const int4& b) { return a.w > b.w; });
   tilesA = tA;
   tilesB = tB;
   rowsA = tA * BM;
-  rowsB = tB * BN;
+  rowsB = tB * bn;
   nrowsA = rowA_prefix.back();
   nrowsB = rowB_prefix.back();
   rowsRA = std::max<int64_t>(rA, 1);
@@ -732,6 +982,7 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   };
   up((void**)&d_probs, probs.data(), sizeof(Problem) * nprob);
   up((void**)&d_tile_prefix, tile_prefix.data(), sizeof(int64_t) * (nprob + 1));
+  up((void**)&d_tiles, tl.data(), sizeof(int4) * tl.size());
   up((void**)&d_packA_prefix, packA_prefix.data(), sizeof(int64_t) * (nprob + 1));
   up((void**)&d_packB_prefix, packB_prefix.data(), sizeof(int64_t) * (nprob + 1));
   up((void**)&d_rowA_prefix, rowA_prefix.data(), sizeof(int64_t) * (nprob + 1));
@@ -748,17 +999,18 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   MPSG_CUDA(cudaMalloc(&d_packB, std::max<int64_t>(S * rowsB * 64 * 2, 128 * 128)));
   MPSG_CUDA(cudaMalloc(&d_err, sizeof(int)));
   MPSG_CUDA(cudaMemset(d_err, 0, sizeof(int)));
-  make_map(&tmA, d_packA, std::max<int64_t>(rowsA, BM), S, BM);
-  make_map(&tmB, d_packB, std::max<int64_t>(rowsB, BN), S, BN);
+  make_map(&tmA, d_packA, std::max<int64_t>(rowsA, BM), S, BM, fast ? BKF : BK);
+  make_map(&tmB, d_packB, std::max<int64_t>(rowsB, bn), S, bn, fast ? BKF : BK);
   (void)ctx;
 }
 
 void SplitPlan::release() {
   void* ptrs[] = {d_probs, d_tile_prefix, d_packA_prefix, d_packB_prefix, d_rowA_prefix,
-                  d_rowB_prefix, d_RA, d_CB, d_EA, d_EB, d_packA, d_packB, d_err};
+                  d_rowB_prefix, d_RA, d_CB, d_EA, d_EB, d_packA, d_packB, d_err, d_tiles};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   d_probs = nullptr;
+  d_tiles = nullptr;
   d_tile_prefix = d_packA_prefix = d_packB_prefix = d_rowA_prefix = d_rowB_prefix = nullptr;
   d_RA = d_CB = nullptr;
   d_EA = d_EB = nullptr;
@@ -771,7 +1023,8 @@ template <int S>
 static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double* B, double* C,
                      int what) {
   using CF = Cfg<S>;
-  const int chunk = chunk_for(S);
+  using FCF = FastCfg<S <= 3 ? S : 3>;
+  const int chunk = sp.chunk;
   constexpr int kPackSmem = 128 * 65 * (int)sizeof(double);
   static bool pack_attr = false;
   if (!pack_attr) {
@@ -792,7 +1045,8 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
       KernelTimer timer(ctx, kKindPack);
       int g = (int)std::min<int64_t>(nitems, (int64_t)ctx->num_sms * 8);
       pack_exponents_kernel<<<g, 256, 0, ctx->stream>>>(
-          sp.d_probs, side ? sp.d_rowB_prefix : sp.d_rowA_prefix, sp.nprob, nitems, side, chunk,
+          sp.d_probs, side ? sp.d_rowB_prefix : sp.d_rowA_prefix, sp.nprob, nitems, side, sp.seg,
+          sp.fast ? 0 : 1,
           X, E, R);
       MPSG_CUDA(cudaGetLastError());
       ctx->kernel_launches++;
@@ -802,7 +1056,8 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
       int g = (int)std::min<int64_t>(ntile, (int64_t)ctx->num_sms * 6);
       pack_slices_kernel<S><<<g, 256, kPackSmem, ctx->stream>>>(
           sp.d_probs, side ? sp.d_packB_prefix : sp.d_packA_prefix, sp.nprob, ntile, side, chunk,
-          side ? BN : BM, side ? sp.rowsB : sp.rowsA, X, E, R,
+          sp.fast ? 1 : 0,
+          side ? sp.bn : BM, side ? sp.rowsB : sp.rowsA, X, E, R,
           (__nv_bfloat16*)(side ? sp.d_packB : sp.d_packA));
       MPSG_CUDA(cudaGetLastError());
       ctx->kernel_launches++;
@@ -813,13 +1068,21 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
   if (!attr_set) {
     MPSG_CUDA(cudaFuncSetAttribute(split_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    CF::kSmemBytes));
+    if (S <= 3)
+      MPSG_CUDA(cudaFuncSetAttribute(split_gemm_fast_kernel<S <= 3 ? S : 3>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, FCF::kSmemBytes));
     attr_set = true;
   }
   const int grid = (int)std::min<int64_t>(sp.ntiles, (int64_t)ctx->num_sms);
   KernelTimer timer(ctx, kKindGemmSplit, sp.flops);
-  split_gemm_kernel<S><<<grid, 192, CF::kSmemBytes, ctx->stream>>>(
-      sp.tmA, sp.tmB, sp.d_probs, sp.d_tile_prefix, sp.nprob, sp.ntiles, sp.d_RA, sp.d_CB, C,
-      sp.d_err);
+  if (sp.fast) {
+    if (S > 3) throw Error(kErrUnsupported, "fast split mode needs S <= 3");
+    split_gemm_fast_kernel<S <= 3 ? S : 3><<<grid, 192, FCF::kSmemBytes, ctx->stream>>>(
+        sp.tmA, sp.tmB, sp.d_probs, sp.d_tiles, sp.ntiles, sp.d_RA, sp.d_CB, C, sp.d_err);
+  } else {
+    split_gemm_kernel<S><<<grid, 192, CF::kSmemBytes, ctx->stream>>>(
+        sp.tmA, sp.tmB, sp.d_probs, sp.d_tiles, sp.ntiles, sp.d_RA, sp.d_CB, C, sp.d_err);
+  }
   MPSG_CUDA(cudaGetLastError());
   ctx->kernel_launches++;
   ctx->gemm_flops += sp.flops;

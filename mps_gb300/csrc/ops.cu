@@ -392,6 +392,38 @@ static const std::vector<int> kRW_A = {2, 4, -1, 3}, kRW_B = {1, -1, 5};
 static const std::vector<int> kX_A = {-1, -2, 1, 3, 2}, kX_B = {-1, -2, 4, 5};
 static const std::vector<int> kO_A = {1, 2, -1, -2, -3}, kO_B = {-3, -1, -2, 3, 4};
 
+FoldedHeffPlans plan_heff_folded(const TensorMeta& v, const TensorMeta& envL,
+                                 const TensorMeta& envR, const TensorMeta& W1,
+                                 const TensorMeta& W2) {
+  FoldedHeffPlans F;
+  F.lw = plan_contract(envL, kLW_A, W1, kLW_B);
+  F.rw = plan_contract(W2, kRW_A, envR, kRW_B);
+  F.c1 = plan_contract(F.lw->split.out, kX_A, v, kX_B);
+  F.c2 = plan_contract(F.c1->split.out, kO_A, F.rw->split.out, kO_B);
+  std::vector<BlockMap> src_of_x, dst_of_x;
+  const ContractPlan& c1 = *F.c1;
+  const ContractPlan& c2 = *F.c2;
+  plan_split_permute_rec(c1.mm.out, c1.rlegs, c1.clegs, c1.perm, &src_of_x);
+  plan_symmatrix_rec(c1.split.out, c2.rowsA, c2.colsA, &dst_of_x);
+  F.x2a = compose_through(c1.split.out, src_of_x, dst_of_x);
+  return F;
+}
+
+void check_heff_folded(const TensorMeta& v, const TensorMeta& envL, const TensorMeta& envR,
+                       const TensorMeta& W1, const TensorMeta& W2) {
+  FoldedHeffPlans F = plan_heff_folded(v, envL, envR, W1, W2);
+  for (auto* c : {F.lw.get(), F.rw.get(), F.c1.get(), F.c2.get()}) {
+    const TensorMeta* A = c == F.lw.get() ? &envL : c == F.rw.get() ? &W2
+                          : c == F.c1.get() ? &F.lw->split.out : &F.c1->split.out;
+    const TensorMeta* B = c == F.lw.get() ? &W1 : c == F.rw.get() ? &envR
+                          : c == F.c1.get() ? &v : &F.rw->split.out;
+    validate_contract(*c, *A, *B);
+  }
+  check_composition(F.c1->split.tasks, F.c1->mm.out.total, F.c1->split.out.total,
+                    F.c2->fa.tasks, F.c2->fa.out.total, F.x2a);
+  if (!same_meta(F.c2->split.out, v)) throw Error(kErrSpaceMismatch, "folded H_eff changes v's structure");
+}
+
 std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const DeviceTensor& envL,
                                     const DeviceTensor& envR, const DeviceTensor& W1,
                                     const DeviceTensor& W2, int precision) {
@@ -413,6 +445,14 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
   op->envRW = contract(ctx, W2, kRW_A, envR, kRW_B, 0, nullptr);
   op->c1 = private_contract_plan(op->envLW.meta, kX_A, vmeta, kX_B);
   op->c2 = private_contract_plan(op->c1->host->split.out, kO_A, op->envRW.meta, kO_B);
+  {
+    const ContractPlan& h1 = *op->c1->host;
+    const ContractPlan& h2 = *op->c2->host;
+    std::vector<BlockMap> src_of_x, dst_of_x;
+    plan_split_permute_rec(h1.mm.out, h1.rlegs, h1.clegs, h1.perm, &src_of_x);
+    plan_symmatrix_rec(h1.split.out, h2.rowsA, h2.colsA, &dst_of_x);
+    op->x2a.upload(compose_through(h1.split.out, src_of_x, dst_of_x), false);
+  }
   // constant operands: fuse once, slice once
   op->fusedA1 = alloc_buffer(ctx, op->c1->host->fa.out.total);
   launch_copy(ctx, op->c1->fa, op->envLW.data(), op->fusedA1->ptr);
@@ -443,28 +483,14 @@ DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v) {
   auto fc1 = alloc_buffer(ctx, c1.host->mm.out.total);
   split::launch_split_gemm(ctx, *c1.mm.splitp[S], nullptr, fb->ptr, fc1->ptr,
                            split::kPackB | split::kRunGemm);
-  DeviceTensor X;
-  X.ctx = ctx;
-  X.meta = c1.host->split.out;
-  if (c1.split.identity) {
-    X.buf = fc1;
-  } else {
-    X.buf = alloc_buffer(ctx, X.meta.total);
-    launch_copy(ctx, c1.split, fc1->ptr, X.data());
-  }
   fb.reset();
-  fc1.reset();
-  // v' = X . envRW
+  // v' = X . envRW, with GEMM 1's fused output moved straight into GEMM 2's fused A operand
   DevContract& c2 = *op.c2;
-  std::shared_ptr<Buffer> fa;
-  const double* pa = X.data();
-  if (!c2.fa.identity) {
-    fa = alloc_buffer(ctx, c2.host->fa.out.total);
-    launch_copy(ctx, c2.fa, X.data(), fa->ptr);
-    pa = fa->ptr;
-  }
+  auto fa = alloc_buffer(ctx, c2.host->fa.out.total);
+  launch_copy(ctx, op.x2a, fc1->ptr, fa->ptr);
+  fc1.reset();
   auto fc2 = alloc_buffer(ctx, c2.host->mm.out.total);
-  split::launch_split_gemm(ctx, *c2.mm.splitp[S], pa, nullptr, fc2->ptr,
+  split::launch_split_gemm(ctx, *c2.mm.splitp[S], fa->ptr, nullptr, fc2->ptr,
                            split::kPackA | split::kRunGemm);
   DeviceTensor out;
   out.ctx = ctx;

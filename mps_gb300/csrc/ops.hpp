@@ -54,9 +54,24 @@ struct HeffOp {
   DeviceTensor envLW, envRW;         // precision >= 2
   TensorMeta vmeta;
   std::shared_ptr<DevContract> c1, c2;
+  DevCopyPlan x2a;                   // fused X of GEMM 1 -> fused A of GEMM 2 (X never built)
   std::shared_ptr<Buffer> fusedA1, fusedB2;
   double ref_flops = 0;  // algorithmic flops of the reference contraction order
+  ~HeffOp() { x2a.release(); }
 };
+
+// Host plans of the W-folded H_eff: the two folding contractions, the two GEMM contractions and
+// the composed copy list from GEMM 1's fused output to GEMM 2's fused A operand.
+struct FoldedHeffPlans {
+  std::shared_ptr<ContractPlan> lw, rw, c1, c2;
+  std::vector<CopyTask> x2a;
+};
+FoldedHeffPlans plan_heff_folded(const TensorMeta& v, const TensorMeta& envL,
+                                 const TensorMeta& envR, const TensorMeta& W1,
+                                 const TensorMeta& W2);
+// Host self-check of those plans (bounds, coverage, composition == two steps).
+void check_heff_folded(const TensorMeta& v, const TensorMeta& envL, const TensorMeta& envR,
+                       const TensorMeta& W1, const TensorMeta& W2);
 std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const DeviceTensor& envL,
                                     const DeviceTensor& envR, const DeviceTensor& W1,
                                     const DeviceTensor& W2, int precision);

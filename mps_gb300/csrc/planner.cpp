@@ -441,7 +441,13 @@ RelegPlan plan_splitleg(const TensorMeta& A, int l1, const std::vector<Space>& s
 // ------------------------------------------------------------------------------------------
 FusePlan plan_symmatrix(const TensorMeta& A, const std::vector<int>& rows1,
                         const std::vector<int>& cols1) {
+  return plan_symmatrix_rec(A, rows1, cols1, nullptr);
+}
+
+FusePlan plan_symmatrix_rec(const TensorMeta& A, const std::vector<int>& rows1,
+                            const std::vector<int>& cols1, std::vector<BlockMap>* rec) {
   const int N = A.N();
+  if (rec) rec->assign(A.nblocks(), BlockMap());
   std::vector<int> idxperm = rows1;
   idxperm.insert(idxperm.end(), cols1.begin(), cols1.end());
   {
@@ -507,6 +513,11 @@ FusePlan plan_symmatrix(const TensorMeta& A, const std::vector<int>& rows1,
         }
         t.soff = A.off[b];
         t.doff = P.out.off[f] + pr + pc * rlim;
+        if (rec) {  // destination of source block b in its natural axis order
+          BlockMap& m = (*rec)[b];
+          m.off = t.doff;
+          for (int k = 0; k < N; ++k) m.str[idxperm[k] - 1] = t.dstr[k];
+        }
         t.simplify();
         P.tasks.push_back(t);
         pr += fdr;
@@ -572,6 +583,12 @@ MatmulPlan plan_matmul(const TensorMeta& A, const TensorMeta& B) {
 // ------------------------------------------------------------------------------------------
 RelegPlan plan_split_permute(const TensorMeta& C, const std::vector<Space>& rlegs,
                              const std::vector<Space>& clegs, const std::vector<int>& perm1) {
+  return plan_split_permute_rec(C, rlegs, clegs, perm1, nullptr);
+}
+
+RelegPlan plan_split_permute_rec(const TensorMeta& C, const std::vector<Space>& rlegs,
+                                 const std::vector<Space>& clegs, const std::vector<int>& perm1,
+                                 std::vector<BlockMap>* rec) {
   const int nr = (int)rlegs.size(), nc = (int)clegs.size(), N = nr + nc;
   if (N > kMaxLegs) fail(kErrArgument, "too many legs");
   check_perm(perm1, N);
@@ -581,6 +598,7 @@ RelegPlan plan_split_permute(const TensorMeta& C, const std::vector<Space>& rleg
   for (int i = 0; i < N; ++i) fsp[i] = inter[perm1[i] - 1];
   RelegPlan P;
   P.out = TensorMeta::build(C.charge, fsp);
+  if (rec) rec->assign(P.out.nblocks(), BlockMap());
   size_t produced = 0;
   for (size_t b = 0; b < C.nblocks(); ++b) {
     int c1 = eff(C.sec.labels(b)[0], C.space[0].dual);
@@ -624,6 +642,11 @@ RelegPlan plan_split_permute(const TensorMeta& C, const std::vector<Space>& rleg
         for (int k = 0; k < N; ++k) t.dstr[perm1[k] - 1] = fstr[k];
         t.soff = C.off[b] + pr + pc * ld;
         t.doff = P.out.off[ob];
+        if (rec) {  // source of output block ob in its natural axis order
+          BlockMap& m = (*rec)[ob];
+          m.off = t.soff;
+          for (int k = 0; k < N; ++k) m.str[k] = sstr[perm1[k] - 1];
+        }
         t.simplify();
         P.tasks.push_back(t);
         ++produced;
@@ -637,6 +660,29 @@ RelegPlan plan_split_permute(const TensorMeta& C, const std::vector<Space>& rleg
   if (produced != P.out.nblocks()) fail(kErrSpaceMismatch, "split: sectors not covered");
   P.identity = tasks_identity(P.tasks, C.total);
   return P;
+}
+
+std::vector<CopyTask> compose_through(const TensorMeta& X, const std::vector<BlockMap>& src_of_x,
+                                      const std::vector<BlockMap>& dst_of_x) {
+  if (src_of_x.size() != X.nblocks() || dst_of_x.size() != X.nblocks())
+    fail(kErrArgument, "compose_through: block maps do not match the intermediate");
+  std::vector<CopyTask> out;
+  out.reserve(X.nblocks());
+  const int N = X.N();
+  for (size_t b = 0; b < X.nblocks(); ++b) {
+    CopyTask t;
+    t.nd = N;
+    for (int k = 0; k < N; ++k) {
+      t.ext[k] = X.sec.sizes(b)[k];
+      t.sstr[k] = src_of_x[b].str[k];
+      t.dstr[k] = dst_of_x[b].str[k];
+    }
+    t.soff = src_of_x[b].off;
+    t.doff = dst_of_x[b].off;
+    t.simplify();
+    out.push_back(t);
+  }
+  return out;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -692,6 +738,10 @@ std::shared_ptr<ContractPlan> plan_contract(const TensorMeta& A, const std::vect
   }
   P->fa = plan_symmatrix(A, remsA, consA);
   P->fb = plan_symmatrix(B, consB, remsB);
+  P->rowsA = remsA;
+  P->colsA = consA;
+  P->rowsB = consB;
+  P->colsB = remsB;
   P->mm = plan_matmul(P->fa.out, P->fb.out);
   std::vector<Space> rl, cl;
   for (int r : remsA) rl.push_back(A.space[r - 1]);
@@ -705,7 +755,47 @@ std::shared_ptr<ContractPlan> plan_contract(const TensorMeta& A, const std::vect
   }
   P->split = plan_split_permute(P->mm.out, rl, cl, inv);
   P->flops = P->mm.flops;
+  P->rlegs = rl;
+  P->clegs = cl;
+  P->perm = inv;
   return P;
+}
+
+static void apply_tasks_host(const std::vector<CopyTask>& tasks, const std::vector<int64_t>& src,
+                             std::vector<int64_t>& dst) {
+  for (const CopyTask& t : tasks) {
+    int64_t idx[kMaxTaskDims] = {0};
+    int64_t s = t.soff, d = t.doff;
+    for (;;) {
+      dst[d] = src[s];
+      int i = 0;
+      for (; i < t.nd; ++i) {
+        if (++idx[i] < t.ext[i]) {
+          s += t.sstr[i];
+          d += t.dstr[i];
+          break;
+        }
+        s -= (t.ext[i] - 1) * t.sstr[i];
+        d -= (t.ext[i] - 1) * t.dstr[i];
+        idx[i] = 0;
+      }
+      if (i == t.nd) break;
+    }
+  }
+}
+
+void check_composition(const std::vector<CopyTask>& step1, int64_t n_src, int64_t n_mid,
+                       const std::vector<CopyTask>& step2, int64_t n_dst,
+                       const std::vector<CopyTask>& composed) {
+  validate_copy_tasks(step1, n_src, n_mid);
+  validate_copy_tasks(step2, n_mid, n_dst);
+  validate_copy_tasks(composed, n_src, n_dst);
+  std::vector<int64_t> src(n_src), mid(n_mid, -1), a(n_dst, -1), b(n_dst, -2);
+  for (int64_t i = 0; i < n_src; ++i) src[i] = i;
+  apply_tasks_host(step1, src, mid);
+  apply_tasks_host(step2, mid, a);
+  apply_tasks_host(composed, src, b);
+  if (a != b) fail(kErrArgument, "composed copy plan differs from the two-step plan");
 }
 
 // ------------------------------------------------------------------------------------------

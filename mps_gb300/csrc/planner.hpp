@@ -148,6 +148,24 @@ RelegPlan plan_splitleg(const TensorMeta& A, int l1, const std::vector<Space>& s
 RelegPlan plan_split_permute(const TensorMeta& C, const std::vector<Space>& rlegs,
                              const std::vector<Space>& clegs, const std::vector<int>& perm1);
 
+// Affine map of one block of an intermediate tensor X, in X's own (column-major) axis order:
+// element i of the block sits at off + sum_k i_k * str[k] of the other buffer.
+struct BlockMap {
+  int64_t off = 0;
+  int64_t str[kMaxLegs] = {0};
+};
+// Same plans, also recording per X block where it comes from (split: fused C -> X) or where it
+// goes (symmatrix: X -> fused matrix).
+RelegPlan plan_split_permute_rec(const TensorMeta& C, const std::vector<Space>& rlegs,
+                                 const std::vector<Space>& clegs, const std::vector<int>& perm1,
+                                 std::vector<BlockMap>* src_of_x);
+FusePlan plan_symmatrix_rec(const TensorMeta& X, const std::vector<int>& rows1,
+                            const std::vector<int>& cols1, std::vector<BlockMap>* dst_of_x);
+// Compose "split C into X" with "fuse X into a matrix" into one copy list C -> matrix, so X is
+// never materialised.  X is the output structure of the split plan.
+std::vector<CopyTask> compose_through(const TensorMeta& X, const std::vector<BlockMap>& src_of_x,
+                                      const std::vector<BlockMap>& dst_of_x);
+
 // _contract_index_perm (contract.jl:82-99): 1-based positions.
 void contract_index_perm(const std::vector<int>& idx, std::vector<int>& rems,
                          std::vector<int>& cons, std::vector<int>& tofinals);
@@ -159,7 +177,17 @@ struct ContractPlan {
   RelegPlan split;
   bool scalar = false;  // every leg contracted: result is a number
   double flops = 0;
+  // arguments of the pieces, kept to compose plans of chained contractions
+  std::vector<int> rowsA, colsA, rowsB, colsB;  // SymMatrix index lists (1-based)
+  std::vector<Space> rlegs, clegs;              // legs of the split
+  std::vector<int> perm;                        // final permutation (1-based)
 };
+
+// Host check of a composed plan: moves element indices through the two-step plan and through
+// the composed list and compares (used by tests; throws Error on mismatch).
+void check_composition(const std::vector<CopyTask>& step1, int64_t n_src, int64_t n_mid,
+                       const std::vector<CopyTask>& step2, int64_t n_dst,
+                       const std::vector<CopyTask>& composed);
 std::shared_ptr<ContractPlan> plan_contract(const TensorMeta& A, const std::vector<int>& idxA,
                                             const TensorMeta& B, const std::vector<int>& idxB);
 

@@ -52,7 +52,7 @@ struct DevCopyPlan {
   bool identity = false;
   CopyTask* d_tasks = nullptr;
   int64_t* d_prefix = nullptr;   // ntasks+1 tile prefix
-  int32_t* d_mode = nullptr;     // per task: packed (mode, axis a, axis b)
+  void* d_aux = nullptr;         // per task: tile shape, axis roles, division constants
   void upload(const std::vector<CopyTask>& tasks, bool identity_);
   void release();
 };

@@ -24,6 +24,10 @@ struct Problem {
 // Device tables, packed-slice scratch and TMA descriptors of one grouped GEMM at S slices.
 struct SplitPlan {
   int S = 0;
+  bool fast = false;   // one FP32 accumulator, 128 x 256 tiles (S <= 3); else exact chunked mode
+  int bn = 64;         // rows of a packed B tile = N of an output tile
+  int chunk = 0;       // K columns per exact chunk (whole K in fast mode)
+  int seg = 0;         // K columns per exponent-pass work item
   int nprob = 0;
   int64_t ntiles = 0, tilesA = 0, tilesB = 0, rowsA = 0, rowsB = 0, nrowsA = 0, nrowsB = 0;
   int64_t rowsRA = 0, rowsCB = 0;  // entries of the row-reference exponent arrays
@@ -36,6 +40,7 @@ struct SplitPlan {
   int16_t *d_EA = nullptr, *d_EB = nullptr;
   void *d_packA = nullptr, *d_packB = nullptr;
   int* d_err = nullptr;
+  int4* d_tiles = nullptr;  // output tiles (problem, M tile, N tile, K steps), descending K
   alignas(64) CUtensorMap tmA;
   alignas(64) CUtensorMap tmB;
   void build(Context* ctx, const std::vector<GemmTask>& g, int S);

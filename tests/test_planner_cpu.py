@@ -153,6 +153,16 @@ def binomial_space(chi, ncharges=25, offset=0):
     return mg.VectorSpace([(offset + k, d) for k, d in enumerate(binomial_profile(chi, ncharges))])
 
 
+@pytest.mark.parametrize("chi,nq", [(64, 9), (2048, 25)])
+def test_folded_heff_plans_self_check(chi, nq):
+    """The tensor-core H_eff (W folded into the environments, intermediate never materialised):
+    every copy/GEMM window in bounds, every element written once, and the composed copy of the
+    intermediate equal to split-then-fuse, element by element."""
+    from mps_gb300 import dmrg
+    prob = dmrg.heff_problem(chi, meta_only=True, ncharges=nq)
+    _lib.call("mpsg_plan_heff2_check", *[t.handle for t in prob])
+
+
 def test_heff_chain_structure_at_chi2048():
     """The chi=2048 H_eff workload: v has 96 blocks and 1.8 M elements, and the planned flops
     of the four contractions add up to about 9.7 GFLOP."""
