@@ -166,6 +166,10 @@ int mpsg_plan_matmul(const mpsg_tensor* a, const mpsg_tensor* b, mpsg_tensor** o
 /* *out is NULL for a full contraction (scalar result). */
 int mpsg_plan_contract(const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
                        const int32_t* idxb, mpsg_tensor** out, double* flops);
+/* Sector GEMM shapes (M, N, K per GEMM, 3*count values) of contract(A, idxA, B, idxB); call
+ * with mnk = NULL to get the count (diagnostics and tile tuning). */
+int mpsg_plan_contract_gemms(const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
+                             const int32_t* idxb, int64_t* count, int64_t* mnk);
 /* Number of copy tasks and GEMM tasks the planner emits for contract (diagnostics). */
 int mpsg_plan_contract_tasks(const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
                              const int32_t* idxb, int64_t* copy_tasks, int64_t* gemm_tasks);

@@ -102,6 +102,7 @@ SIGNATURES = {
     "mpsg_plan_matmul": [P, P, PP, PF64],
     "mpsg_plan_contract": [P, PI32, P, PI32, PP, PF64],
     "mpsg_plan_contract_tasks": [P, PI32, P, PI32, PI64, PI64],
+    "mpsg_plan_contract_gemms": [P, PI32, P, PI32, PI64, PI64],
     "mpsg_fill": [P, P, F64],
     "mpsg_rmul": [P, P, F64],
     "mpsg_mul": [P, P, P, F64],

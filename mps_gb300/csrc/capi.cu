@@ -661,6 +661,26 @@ int mpsg_plan_contract(const mpsg_tensor* a, const int32_t* idxa, const mpsg_ten
   });
 }
 
+int mpsg_plan_contract_gemms(const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
+                             const int32_t* idxb, int64_t* count, int64_t* mnk) {
+  return guarded([&] {
+    need(a, "a");
+    need(b, "b");
+    need(idxa, "idxa");
+    need(idxb, "idxb");
+    need(count, "count");
+    auto p = mpsg::plan_contract(a->t.meta, ivec(idxa, a->t.meta.N()), b->t.meta,
+                                 ivec(idxb, b->t.meta.N()));
+    *count = (int64_t)p->mm.gemms.size();
+    if (mnk)
+      for (size_t i = 0; i < p->mm.gemms.size(); ++i) {
+        mnk[3 * i] = p->mm.gemms[i].M;
+        mnk[3 * i + 1] = p->mm.gemms[i].N;
+        mnk[3 * i + 2] = p->mm.gemms[i].K;
+      }
+  });
+}
+
 int mpsg_plan_contract_tasks(const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
                              const int32_t* idxb, int64_t* copy_tasks, int64_t* gemm_tasks) {
   return guarded([&] {
