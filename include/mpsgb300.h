@@ -105,6 +105,18 @@ int mpsg_matmul(mpsg_ctx* ctx, const mpsg_tensor* a, const mpsg_tensor* b, int32
  * *scalar and *out is set to NULL. */
 int mpsg_contract(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
                   const int32_t* idxb, int32_t precision, mpsg_tensor** out, double* scalar);
+/* The same FP64 contraction into a caller-provided result, allocating no device memory (no
+ * counterpart in the reference). For hosts that cannot let a library allocate during a call,
+ * e.g. one that handed the GPU's memory to its own arena up front. `out` must already exist
+ * with the result's charge and spaces (MPSG_ERR_SPACE_MISMATCH otherwise) and must not share
+ * storage with a or b. Every temporary lives in one fixed 64 MiB device array that each GPU
+ * loading the library holds until exit; a contraction needing more is rejected with
+ * MPSG_ERR_UNSUPPORTED, a fully contracted (scalar) one too. The first call on a device looks
+ * up that array's address: make it before any stream capture. Calls share the array, so calls
+ * whose kernels overlap on the GPU (different streams or contexts of one device) race; calls
+ * on one context are ordered. Returns when the result is complete. */
+int mpsg_contract_noalloc(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa,
+                          const mpsg_tensor* b, const int32_t* idxb, mpsg_tensor* out);
 /* Algorithmic flops of contract(A, idxA, B, idxB) as planned (sum of 2*M*N*K over sectors). */
 int mpsg_contract_flops(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa,
                         const mpsg_tensor* b, const int32_t* idxb, double* flops);

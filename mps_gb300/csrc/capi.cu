@@ -3,44 +3,20 @@
 #include <cstring>
 #include <sstream>
 
-#include "../../include/mpsgb300.h"
+#include "capi_internal.hpp"
 #include "linalg.hpp"
 
-// The handle holds one reference to the context; device buffers hold the others, so
-// mpsg_ctx_destroy never leaves a live tensor with a dangling stream.
-struct mpsg_ctx {
-  std::shared_ptr<mpsg::Context> owner;
-  mpsg::Context& c;
-  explicit mpsg_ctx(std::shared_ptr<mpsg::Context> p) : owner(std::move(p)), c(*owner) {}
-};
-struct mpsg_tensor {
-  mpsg::DeviceTensor t;
-};
+namespace {
+thread_local std::string g_last_error;
+}  // namespace
+
+void mpsg_capi::set_last_error(const std::string& msg) { g_last_error = msg; }
 
 namespace {
 
-thread_local std::string g_last_error;
-
-template <class F>
-int guarded(F&& f) {
-  try {
-    f();
-    return mpsg::kOk;
-  } catch (const mpsg::Error& e) {
-    g_last_error = e.what();
-    return e.code;
-  } catch (const std::bad_alloc&) {
-    g_last_error = "host allocation failed";
-    return mpsg::kErrArgument;
-  } catch (const std::exception& e) {
-    g_last_error = e.what();
-    return mpsg::kErrArgument;
-  }
-}
-
-void need(const void* p, const char* what) {
-  if (!p) throw mpsg::Error(mpsg::kErrArgument, std::string("null argument: ") + what);
-}
+using mpsg_capi::guarded;
+using mpsg_capi::ivec;
+using mpsg_capi::need;
 
 std::vector<mpsg::Space> parse_spaces(int32_t nlegs, const int32_t* nsect, const int32_t* charges,
                                       const int64_t* dims, const int32_t* isdual) {
@@ -66,8 +42,6 @@ mpsg_tensor* wrap(mpsg::DeviceTensor&& t) {
   h->t = std::move(t);
   return h;
 }
-
-std::vector<int> ivec(const int32_t* p, int n) { return std::vector<int>(p, p + n); }
 
 }  // namespace
 

@@ -11,6 +11,8 @@
 //            destination axis.
 // The kernel is persistent: a grid sized to the SM count walks a global tile index and finds its
 // task by binary search in the per-task tile prefix sums.
+#include <cstring>
+
 #include "runtime.hpp"
 
 namespace mpsg {
@@ -149,11 +151,28 @@ void magic_u31(uint32_t d, uint32_t& m, uint32_t& s) {
 
 }  // namespace
 
+size_t copy_aux_bytes() { return sizeof(TaskAux); }
+
 void DevCopyPlan::upload(const std::vector<CopyTask>& tasks, bool identity_) {
   release();
+  std::vector<int64_t> prefix;
+  std::vector<unsigned char> aux;
+  build_host(tasks, identity_, prefix, aux);
+  if (ntasks == 0) return;
+  MPSG_CUDA(cudaMalloc(&d_tasks, sizeof(CopyTask) * ntasks));
+  MPSG_CUDA(cudaMalloc(&d_prefix, sizeof(int64_t) * (ntasks + 1)));
+  MPSG_CUDA(cudaMalloc(&d_aux, aux.size()));
+  MPSG_CUDA(cudaMemcpy(d_tasks, tasks.data(), sizeof(CopyTask) * ntasks, cudaMemcpyHostToDevice));
+  MPSG_CUDA(cudaMemcpy(d_prefix, prefix.data(), sizeof(int64_t) * (ntasks + 1),
+                       cudaMemcpyHostToDevice));
+  MPSG_CUDA(cudaMemcpy(d_aux, aux.data(), aux.size(), cudaMemcpyHostToDevice));
+}
+
+void DevCopyPlan::build_host(const std::vector<CopyTask>& tasks, bool identity_,
+                             std::vector<int64_t>& prefix, std::vector<unsigned char>& aux_bytes) {
   identity = identity_;
   ntasks = (int)tasks.size();
-  std::vector<int64_t> prefix(ntasks + 1, 0);
+  prefix.assign(ntasks + 1, 0);
   std::vector<TaskAux> aux(ntasks);
   elems = 0;
   for (int k = 0; k < ntasks; ++k) {
@@ -186,14 +205,8 @@ void DevCopyPlan::upload(const std::vector<CopyTask>& tasks, bool identity_) {
     prefix[k + 1] = prefix[k] + tiles;
   }
   ntiles = prefix[ntasks];
-  if (ntasks == 0) return;
-  MPSG_CUDA(cudaMalloc(&d_tasks, sizeof(CopyTask) * ntasks));
-  MPSG_CUDA(cudaMalloc(&d_prefix, sizeof(int64_t) * (ntasks + 1)));
-  MPSG_CUDA(cudaMalloc(&d_aux, sizeof(TaskAux) * ntasks));
-  MPSG_CUDA(cudaMemcpy(d_tasks, tasks.data(), sizeof(CopyTask) * ntasks, cudaMemcpyHostToDevice));
-  MPSG_CUDA(cudaMemcpy(d_prefix, prefix.data(), sizeof(int64_t) * (ntasks + 1),
-                       cudaMemcpyHostToDevice));
-  MPSG_CUDA(cudaMemcpy(d_aux, aux.data(), sizeof(TaskAux) * ntasks, cudaMemcpyHostToDevice));
+  aux_bytes.resize(sizeof(TaskAux) * ntasks);
+  if (ntasks) std::memcpy(aux_bytes.data(), aux.data(), aux_bytes.size());
 }
 
 void DevCopyPlan::release() {

@@ -144,17 +144,23 @@ int vec_grid(Context* ctx, int64_t n) {
 
 }  // namespace
 
-void DevGemmPlan::upload(const std::vector<GemmTask>& g, double flops_) {
-  release();
+void DevGemmPlan::build_host(const std::vector<GemmTask>& g, double flops_,
+                             std::vector<int64_t>& prefix) {
   host = g;
   flops = flops_;
   n = (int)g.size();
-  std::vector<int64_t> prefix(n + 1, 0);
+  prefix.assign(n + 1, 0);
   for (int k = 0; k < n; ++k) {
     int64_t tiles = ((g[k].M + BM - 1) / BM) * ((g[k].N + BN - 1) / BN);
     prefix[k + 1] = prefix[k] + tiles;
   }
   ntiles = prefix[n];
+}
+
+void DevGemmPlan::upload(const std::vector<GemmTask>& g, double flops_) {
+  release();
+  std::vector<int64_t> prefix;
+  build_host(g, flops_, prefix);
   if (n == 0) return;
   MPSG_CUDA(cudaMalloc(&d_tasks, sizeof(GemmTask) * n));
   MPSG_CUDA(cudaMalloc(&d_prefix, sizeof(int64_t) * (n + 1)));

@@ -54,8 +54,13 @@ struct DevCopyPlan {
   int64_t* d_prefix = nullptr;   // ntasks+1 tile prefix
   void* d_aux = nullptr;         // per task: tile shape, axis roles, division constants
   void upload(const std::vector<CopyTask>& tasks, bool identity_);
+  // Host half of upload: tile prefix sums and per-task launch data; sets every field except the
+  // device pointers (used by callers that place the tables in memory they own).
+  void build_host(const std::vector<CopyTask>& tasks, bool identity_,
+                  std::vector<int64_t>& prefix, std::vector<unsigned char>& aux_bytes);
   void release();
 };
+size_t copy_aux_bytes();  // bytes of launch data per copy task
 
 struct DevGemmPlan {
   int n = 0;
@@ -67,6 +72,8 @@ struct DevGemmPlan {
   std::vector<GemmTask> host;
   std::shared_ptr<split::SplitPlan> splitp[8];  // split-precision plans by slice count
   void upload(const std::vector<GemmTask>& g, double flops_);
+  // Host half of upload: every field except the device pointers, plus the tile prefix sums.
+  void build_host(const std::vector<GemmTask>& g, double flops_, std::vector<int64_t>& prefix);
   void release();
 };
 
