@@ -143,6 +143,15 @@ int mpsg_svd(mpsg_ctx* ctx, const mpsg_tensor* a, mpsg_tensor** u, mpsg_tensor**
  * treats values within tieband*max as equal (0 = the reference rule). */
 int mpsg_svdtrunc(mpsg_ctx* ctx, const mpsg_tensor* a, int64_t maxdim, double tol,
                   double tieband, mpsg_tensor** u, mpsg_tensor** s, mpsg_tensor** v);
+/* svdtrunc by the density-matrix method (no counterpart in the reference; same truncation rule
+ * and output spaces as mpsg_svdtrunc). Per sector, the FP64 eigen-decomposition of A A^T
+ * (side 0: u orthonormal) or A^T A (side 1: v orthonormal) replaces the SVD; the other factor is
+ * S^-1 times the projection of A, so u*s*v equals the projection of A on the kept singular
+ * subspace. Singular values carry an absolute error of about eps * max(S)^2 / S. For sweeps,
+ * which keep the orthonormal side as the new site tensor and absorb s*v (or u*s) into the next. */
+int mpsg_svdtrunc_gram(mpsg_ctx* ctx, const mpsg_tensor* a, int64_t maxdim, double tol,
+                       double tieband, int32_t side, mpsg_tensor** u, mpsg_tensor** s,
+                       mpsg_tensor** v);
 /* truncatedsizes (src/mpsutils.jl:89-112) on host arrays: nsect sectors, lens[i] descending values
  * each, concatenated in `values`; writes the kept count per sector to ns. */
 int mpsg_truncatedsizes(int32_t nsect, const int64_t* lens, const double* values, int64_t maxdim,

@@ -427,6 +427,24 @@ int mpsg_svdtrunc(mpsg_ctx* ctx, const mpsg_tensor* a, int64_t maxdim, double to
   });
 }
 
+int mpsg_svdtrunc_gram(mpsg_ctx* ctx, const mpsg_tensor* a, int64_t maxdim, double tol,
+                       double tieband, int32_t side, mpsg_tensor** u, mpsg_tensor** s,
+                       mpsg_tensor** v) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a, "a");
+    need(u, "u");
+    need(s, "s");
+    need(v, "v");
+    if (side != 0 && side != 1) throw mpsg::Error(mpsg::kErrArgument, "side must be 0 or 1");
+    auto R = mpsg::svd_blocks(&ctx->c, a->t, true, maxdim, tol, tieband,
+                              side == 0 ? mpsg::kSvdGramLeft : mpsg::kSvdGramRight);
+    *u = wrap(std::move(R.u));
+    *s = wrap(std::move(R.s));
+    *v = wrap(std::move(R.v));
+  });
+}
+
 int mpsg_truncatedsizes(int32_t nsect, const int64_t* lens, const double* values, int64_t maxdim,
                         double tol, double tieband, int64_t* ns) {
   return guarded([&] {

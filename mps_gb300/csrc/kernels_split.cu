@@ -20,7 +20,8 @@
 //     (hi + lo) * 2^(R(i) + C(j)) as an FP64 number with integer instructions only.
 //
 // Accuracy: slicing error <= 2^(-beta*S) relative to the row/column scale, so S = 2 is the
-// classic "bf16x3" (3 products), S = 3 gives about 21 bits (6 products), S = 4 about 28 bits.
+// classic "bf16x3" (3 products), S = 3 gives about 21 bits (6 products), S = 4 about 28 bits,
+// S = 6 about 42 bits and S = 7 about 49 bits (28 products), the FP64-class setting.
 //
 // Kernel layout: persistent, one CTA per SM, 6 warps: warp 0 = TMA producer (one elected
 // thread, cp.async.bulk.tensor 3-d loads of pre-packed K-major tiles with 128B swizzle), warp 1
@@ -32,6 +33,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 #include "split.hpp"
 
@@ -392,8 +394,11 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
           const int k = e - Rr - kBeta * (q + 1);
           scale[q] = k >= -126 ? __uint_as_float((uint32_t)(k + 127) << 23) : 0.f;
         }
-        // F = round(x * 2^(beta S - e)) needs at most beta*S + 1 <= 29 bits: 32-bit integer
-        // work on the top 32 bits of the significand (hi word 20 bits, lo word 11, implicit 1)
+        // F = round(x * 2^(beta S - e)) needs at most beta*S + 1 bits. Up to 4 slices (<= 29
+        // bits) that is 32-bit integer work on the top 32 bits of the significand (hi word 20
+        // bits, lo word 11, implicit 1); with more slices, 64-bit work on all 53 bits.
+        constexpr bool kWide = kBeta * S + 1 > 31;
+        using IntF = typename std::conditional<kWide, long long, int>::type;
         const int sbase = 1054 + e - kBeta * S;  // F = m32 >> (sbase - eb), rounded
         uint32_t packed[S][4];
 #pragma unroll
@@ -402,20 +407,30 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
           const int hw = __double2hiint(x);
           const uint32_t lw = (uint32_t)__double2loint(x);
           const int eb = (hw >> 20) & 0x7ff;
-          const uint32_t m32 = (((uint32_t)hw << 11) | (lw >> 21)) | 0x80000000u;
-          const int s = sbase - eb;  // >= 32 - beta*S > 0 for every element of the row chunk
-          int F = 0;
-          if (eb != 0 && s <= 32 && r < rows) {
-            F = (int)(((m32 >> (s - 1)) + 1u) >> 1);  // round half up
-            if (hw < 0) F = -F;
+          IntF F = 0;
+          if constexpr (!kWide) {
+            const uint32_t m32 = (((uint32_t)hw << 11) | (lw >> 21)) | 0x80000000u;
+            const int s = sbase - eb;  // >= 32 - beta*S > 0 for every element of the row chunk
+            if (eb != 0 && s <= 32 && r < rows) {
+              F = (int)(((m32 >> (s - 1)) + 1u) >> 1);  // round half up
+              if (hw < 0) F = -F;
+            }
+          } else {
+            const uint64_t m53 = ((uint64_t)(((uint32_t)hw & 0xfffffu) | 0x100000u) << 32) | lw;
+            const int s = sbase + 21 - eb;  // >= 53 - beta*S >= 4 for up to 7 slices
+            if (eb != 0 && s <= 54 && r < rows) {
+              F = (long long)(((m53 >> (s - 1)) + 1ull) >> 1);  // round half up
+              if (hw < 0) F = -F;
+            }
           }
 #pragma unroll
           for (int q = 0; q < S; ++q) {
             const int shq = kBeta * (S - 1 - q);
-            int tq = F;
+            int tq = (int)F;
             if (shq > 0) {
-              tq = (F + (1 << (shq - 1))) >> shq;
-              F -= tq * (1 << shq);
+              const IntF t = (F + ((IntF)1 << (shq - 1))) >> shq;
+              F -= t * ((IntF)1 << shq);
+              tq = (int)t;
             }
             const float v = (float)tq * scale[q];  // exact: |tq| <= 2^beta
             const uint16_t h = __bfloat16_as_ushort(__float2bfloat16_rn(v));
@@ -438,12 +453,30 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
 // ------------------------------------------------------------------------------------------
 // the GEMM kernel
 // ------------------------------------------------------------------------------------------
+// K-major tile with 64-byte swizzle (rows of 32 bf16), 8-row groups 512 B apart
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;           // stride byte offset: 8 rows x 64 B
+  d |= (uint64_t)1 << 46;                    // descriptor version
+  d |= (uint64_t)4 << 61;                    // 64-byte swizzle
+  return d;
+}
+
+// Exact mode. The K step is 64 (128-byte swizzle) up to 4 slices; with 5..7 slices it is 32
+// (64-byte swizzle) so that a pipeline stage holding all S slices of both operands still fits
+// twice in shared memory. A chunk (the K range between exact FP32 flushes) is a multiple of 64:
+// chunk * (pairs in a group <= S) * 2^14 <= 2^24 keeps every TMEM sum an exact integer.
 template <int S>
 struct Cfg {
+  static constexpr int kBK = S <= 4 ? 64 : 32;
+  static constexpr int kPerRow = 64 / kBK;  // K steps per 64-wide packed row
   static constexpr int kPairs = S * (S + 1) / 2;
-  static constexpr int kChunkSteps = (1024 / S) / BK;
-  static constexpr int kABytes = BM * BK * 2;
-  static constexpr int kBBytes = BN * BK * 2;
+  static constexpr int kChunk = ((1024 / S) / 64) * 64;
+  static constexpr int kChunkSteps = kChunk / kBK;
+  static constexpr int kABytes = BM * kBK * 2;
+  static constexpr int kBBytes = BN * kBK * 2;
   static constexpr int kStageBytes = S * (kABytes + kBBytes);
   static constexpr int kStages = (220 * 1024) / kStageBytes > 4 ? 4 : (220 * 1024) / kStageBytes;
   static constexpr int kAccCols = S * BN;
@@ -509,17 +542,18 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
         const int nks = probs[tr.x].nks;
         const int64_t baseA = (probs[tr.x].tA + (int64_t)tr.y * nks) * BM;
         const int64_t baseB = (probs[tr.x].tB + (int64_t)tr.z * nks) * BN;
-        for (int ks = 0; ks < nks; ++ks) {
+        for (int ks = 0; ks < nks * CF::kPerRow; ++ks) {
           if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) break;
           uint8_t* sA = smem + stage * CF::kStageBytes;
           uint8_t* sB = sA + S * CF::kABytes;
           mbar_expect_tx(&full[stage], CF::kStageBytes);
-          const int rowA = (int)(baseA + (int64_t)ks * BM);
-          const int rowB = (int)(baseB + (int64_t)ks * BN);
+          const int x = (ks % CF::kPerRow) * CF::kBK;
+          const int rowA = (int)(baseA + (int64_t)(ks / CF::kPerRow) * BM);
+          const int rowB = (int)(baseB + (int64_t)(ks / CF::kPerRow) * BN);
 #pragma unroll
-          for (int s = 0; s < S; ++s) tma_load_3d(sA + s * CF::kABytes, &tmA, &full[stage], 0, rowA, s);
+          for (int s = 0; s < S; ++s) tma_load_3d(sA + s * CF::kABytes, &tmA, &full[stage], x, rowA, s);
 #pragma unroll
-          for (int s = 0; s < S; ++s) tma_load_3d(sB + s * CF::kBBytes, &tmB, &full[stage], 0, rowB, s);
+          for (int s = 0; s < S; ++s) tma_load_3d(sB + s * CF::kBBytes, &tmB, &full[stage], x, rowB, s);
           if (++stage == CF::kStages) {
             stage = 0;
             phase ^= 1;
@@ -538,14 +572,14 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
       for (int64_t i = 0; !*abort_flag; ++i) {
         const int64_t pos = sched_pos(i, gridDim.x, blockIdx.x);
         if (pos >= ntiles) break;
-        const int nks = probs[tiles[pos].x].nks;
-        for (int c0 = 0; c0 < nks && !*abort_flag; c0 += CF::kChunkSteps) {
+        const int nsteps = probs[tiles[pos].x].nks * CF::kPerRow;
+        for (int c0 = 0; c0 < nsteps && !*abort_flag; c0 += CF::kChunkSteps) {
           const int buf = (int)(use % CF::kBufs);
           const uint32_t bph = (uint32_t)((use / CF::kBufs) & 1);
           if (!mbar_wait(&tempty[buf], bph ^ 1, abort_flag, err, 2)) break;
           tc_fence_after();
           uint32_t init = 0;  // bit g: accumulator g already written in this chunk
-          const int c1 = min(nks, c0 + CF::kChunkSteps);
+          const int c1 = min(nsteps, c0 + CF::kChunkSteps);
           for (int ks = c0; ks < c1; ++ks) {
             if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) break;
             tc_fence_after();
@@ -557,10 +591,12 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
               for (int qb = 0; qb < S - pa; ++qb) {
                 const int g = pa + qb;
                 const uint32_t dcol = tmem_base + (uint32_t)((buf * S + g) * BN);
-                const uint64_t ad = sw128_desc(sA + pa * CF::kABytes);
-                const uint64_t bd = sw128_desc(sB + qb * CF::kBBytes);
+                const uint64_t ad = CF::kBK == 64 ? sw128_desc(sA + pa * CF::kABytes)
+                                                  : sw64_desc(sA + pa * CF::kABytes);
+                const uint64_t bd = CF::kBK == 64 ? sw128_desc(sB + qb * CF::kBBytes)
+                                                  : sw64_desc(sB + qb * CF::kBBytes);
 #pragma unroll
-                for (int kk = 0; kk < BK / 16; ++kk) {
+                for (int kk = 0; kk < CF::kBK / 16; ++kk) {
                   umma_bf16(dcol, ad + 2 * kk, bd + 2 * kk, idesc, (init >> g) & 1u);
                   init |= 1u << g;
                 }
@@ -601,7 +637,7 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
         lo[j] = 0.f;
       }
       bool ok = true;
-      for (int c0 = 0; c0 < P.nks; c0 += CF::kChunkSteps) {
+      for (int c0 = 0; c0 < P.nks * CF::kPerRow; c0 += CF::kChunkSteps) {
         const int buf = (int)(use % CF::kBufs);
         const uint32_t bph = (uint32_t)((use / CF::kBufs) & 1);
         if (!mbar_wait(&tfull[buf], bph, abort_flag, err, 5)) {
@@ -659,16 +695,6 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
 // 128 x 256 (double-buffered: 2 x 256 TMEM columns) and the K step shrink to 32 (64-byte
 // swizzle), doubling the MMA work per byte staged in shared memory.
 constexpr int BNF = 256, BKF = 32;
-
-__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
-  d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(512 >> 4) << 32;           // stride byte offset: 8 rows x 64 B
-  d |= (uint64_t)1 << 46;                    // descriptor version
-  d |= (uint64_t)4 << 61;                    // 64-byte swizzle
-  return d;
-}
 
 // v * 2^E as FP64 from the FP32 bit pattern (integer instructions only)
 __device__ __forceinline__ double f32_to_f64_scaled(float v, int E) {
@@ -909,7 +935,8 @@ int chunk_for(int S) { return ((1024 / S) / BK) * BK; }
 void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   release();
   S = S_;
-  if (S < 2 || S > 4) throw Error(kErrUnsupported, "split precision supports 2..4 slices");
+  if (S < 2 || S > kMaxSlices)
+    throw Error(kErrUnsupported, "split precision supports 2..7 slices");
   const char* ex = std::getenv("MPSG_SPLIT_EXACT");
   fast = S <= 3 && !(ex && ex[0] == '1');
   bn = fast ? BNF : BN;
@@ -999,8 +1026,9 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   MPSG_CUDA(cudaMalloc(&d_packB, std::max<int64_t>(S * rowsB * 64 * 2, 128 * 128)));
   MPSG_CUDA(cudaMalloc(&d_err, sizeof(int)));
   MPSG_CUDA(cudaMemset(d_err, 0, sizeof(int)));
-  make_map(&tmA, d_packA, std::max<int64_t>(rowsA, BM), S, BM, fast ? BKF : BK);
-  make_map(&tmB, d_packB, std::max<int64_t>(rowsB, bn), S, bn, fast ? BKF : BK);
+  const int box_x = (fast || S > 4) ? 32 : BK;  // K step of the kernel that reads the slices
+  make_map(&tmA, d_packA, std::max<int64_t>(rowsA, BM), S, BM, box_x);
+  make_map(&tmB, d_packB, std::max<int64_t>(rowsB, bn), S, bn, box_x);
   (void)ctx;
 }
 
@@ -1100,7 +1128,10 @@ void launch_split_gemm(Context* ctx, SplitPlan& sp, const double* A, const doubl
     case 2: launch_t<2>(ctx, sp, A, B, C, what); break;
     case 3: launch_t<3>(ctx, sp, A, B, C, what); break;
     case 4: launch_t<4>(ctx, sp, A, B, C, what); break;
-    default: throw Error(kErrUnsupported, "split precision supports 2..4 slices");
+    case 5: launch_t<5>(ctx, sp, A, B, C, what); break;
+    case 6: launch_t<6>(ctx, sp, A, B, C, what); break;
+    case 7: launch_t<7>(ctx, sp, A, B, C, what); break;
+    default: throw Error(kErrUnsupported, "split precision supports 2..7 slices");
   }
 }
 

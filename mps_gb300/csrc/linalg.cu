@@ -2,6 +2,7 @@
 // thick-restart Lanczos eigensolver that drives the two-site effective Hamiltonian (the role of
 // KrylovKit.eigsolve at src/dmrg.jl:77-82).  Everything stays FP64 on the GPU; the host only
 // sees singular values (for the truncation choice) and the small projected matrix.
+#include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include <algorithm>
@@ -18,17 +19,54 @@ namespace mpsg {
       throw ::mpsg::Error(::mpsg::kErrCuda, std::string(#call) + " failed: " + std::to_string((int)s_)); \
   } while (0)
 
+#define MPSG_BLAS(call)                                                                     \
+  do {                                                                                      \
+    cublasStatus_t s_ = (call);                                                             \
+    if (s_ != CUBLAS_STATUS_SUCCESS)                                                        \
+      throw ::mpsg::Error(::mpsg::kErrCuda, std::string(#call) + " failed: " + std::to_string((int)s_)); \
+  } while (0)
+
 namespace {
 
-cusolverDnHandle_t solver(Context* ctx) {
-  if (!ctx->solver) {
-    cusolverDnHandle_t h;
-    MPSG_SOLVER(cusolverDnCreate(&h));
-    MPSG_SOLVER(cusolverDnSetStream(h, ctx->stream));
-    ctx->solver = h;
-    ctx->solver_destroy = [](void* p) { cusolverDnDestroy((cusolverDnHandle_t)p); };
+constexpr int kLanes = 4;
+
+// Side streams with their own cuSOLVER and cuBLAS handles. The per-sector factorisations of one
+// call are independent, so they run concurrently on these lanes, forked from the context stream
+// by an event and joined back into it before anything downstream (or the host) reads them.
+struct SolverLanes {
+  cudaStream_t st[kLanes] = {};
+  cusolverDnHandle_t sol[kLanes] = {};
+  cublasHandle_t blas[kLanes] = {};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join[kLanes] = {};
+  ~SolverLanes() {
+    for (int i = 0; i < kLanes; ++i) {
+      if (st[i]) cudaStreamSynchronize(st[i]);
+      if (sol[i]) cusolverDnDestroy(sol[i]);
+      if (blas[i]) cublasDestroy(blas[i]);
+      if (join[i]) cudaEventDestroy(join[i]);
+      if (st[i]) cudaStreamDestroy(st[i]);
+    }
+    if (fork) cudaEventDestroy(fork);
   }
-  return (cusolverDnHandle_t)ctx->solver;
+};
+
+SolverLanes& lanes(Context* ctx) {
+  if (!ctx->solver) {
+    auto* L = new SolverLanes();
+    ctx->solver = L;
+    ctx->solver_destroy = [](void* p) { delete (SolverLanes*)p; };
+    MPSG_CUDA(cudaEventCreateWithFlags(&L->fork, cudaEventDisableTiming));
+    for (int i = 0; i < kLanes; ++i) {
+      MPSG_CUDA(cudaStreamCreateWithFlags(&L->st[i], cudaStreamNonBlocking));
+      MPSG_CUDA(cudaEventCreateWithFlags(&L->join[i], cudaEventDisableTiming));
+      MPSG_SOLVER(cusolverDnCreate(&L->sol[i]));
+      MPSG_SOLVER(cusolverDnSetStream(L->sol[i], L->st[i]));
+      MPSG_BLAS(cublasCreate(&L->blas[i]));
+      MPSG_BLAS(cublasSetStream(L->blas[i], L->st[i]));
+    }
+  }
+  return *(SolverLanes*)ctx->solver;
 }
 
 // dst[i + ld*i] = s[i] on a zeroed k x k block
@@ -54,79 +92,158 @@ __global__ void transpose_prefix_kernel(double* __restrict__ dst, const double* 
   }
 }
 
+// The k largest eigenpairs of an n x n Gram matrix in descending order: X[:, i] = Q[:, n-1-i] and
+// S[i] = sqrt(max(w[n-1-i], 0)), where (w, Q) is the ascending eigen-decomposition.
+__global__ void top_eigpairs_kernel(double* __restrict__ X, double* __restrict__ S,
+                                    const double* __restrict__ Q, const double* __restrict__ w,
+                                    int64_t n, int64_t k) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / n, r = t - i * n;
+    X[t] = Q[r + n * (n - 1 - i)];
+    if (r == 0) S[i] = sqrt(fmax(w[n - 1 - i], 0.0));
+  }
+}
+
+// X[:, i] /= S[i] (columns with S[i] == 0 become zero)
+__global__ void scale_cols_inv_kernel(double* __restrict__ X, const double* __restrict__ S,
+                                      int64_t rows, int64_t k) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * k;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double s = S[t / rows];
+    X[t] = s > 0.0 ? X[t] / s : 0.0;
+  }
+}
+
+unsigned grid_for(int64_t n) { return (unsigned)std::min<int64_t>((n + 255) / 256, 1184); }
+
 struct BlockSVD {
   int c1, c2;
   int64_t M, N, k;
   std::shared_ptr<Buffer> U, S, V;  // U: M x k, S: k, V: N x k (all column-major)
+  std::shared_ptr<Buffer> work, aux, wbuf;  // temporaries, kept until the lanes are joined
+  int lwork = 0;
 };
 
-// Thin SVD of one column-major M x N block with cuSOLVER's Jacobi SVD; on non-convergence it
-// falls back to the QR-iteration SVD, as the reference falls back to LAPACK QRIteration
-// (src/symtools.jl:14-19).
-void block_svd(Context* ctx, const double* A, BlockSVD& out) {
-  auto h = solver(ctx);
-  const int64_t M = out.M, N = out.N, k = std::min(M, N);
-  out.k = k;
-  out.U = alloc_buffer(ctx, M * k);
-  out.S = alloc_buffer(ctx, k);
-  out.V = alloc_buffer(ctx, N * k);
-  auto work = alloc_buffer(ctx, M * N);  // gesvdj overwrites its input
+// Exact thin SVD of one column-major M x N block with cuSOLVER's QR-iteration SVD (gesvd, the
+// method of the reference's fallback, src/symtools.jl:14-19). gesvd wants M >= N, so a wide
+// block is factorised through its transpose. Buffers are allocated by the caller (prepare_exact)
+// on the context stream; this only enqueues work on the lane's stream.
+void prepare_exact(Context* ctx, cusolverDnHandle_t h, BlockSVD& B) {
+  const int64_t M = B.M, N = B.N, k = B.k;
+  B.U = alloc_buffer(ctx, M * k);
+  B.S = alloc_buffer(ctx, k);
+  B.V = alloc_buffer(ctx, N * k);
+  B.work = alloc_buffer(ctx, M * N);
+  B.aux = alloc_buffer(ctx, k * k);
+  const int64_t m = std::max(M, N), n = std::min(M, N);
+  MPSG_SOLVER(cusolverDnDgesvd_bufferSize(h, (int)m, (int)n, &B.lwork));
+  B.wbuf = alloc_buffer(ctx, std::max(B.lwork, 1));
+}
+
+void run_exact(Context* ctx, cudaStream_t st, cusolverDnHandle_t h, const double* A, BlockSVD& B,
+               int* dinfo) {
+  const int64_t M = B.M, N = B.N, k = B.k;
+  if (M >= N) {
+    MPSG_CUDA(cudaMemcpyAsync(B.work->ptr, A, sizeof(double) * M * N, cudaMemcpyDeviceToDevice,
+                              st));
+    // A = U S VT with VT (N x N) in aux; V = VT^T
+    MPSG_SOLVER(cusolverDnDgesvd(h, 'S', 'S', (int)M, (int)N, B.work->ptr, (int)M, B.S->ptr,
+                                 B.U->ptr, (int)M, B.aux->ptr, (int)N, B.wbuf->ptr, B.lwork,
+                                 nullptr, dinfo));
+    dim3 g((unsigned)((N + 31) / 32), (unsigned)((N + 31) / 32));
+    transpose_prefix_kernel<<<g, dim3(32, 8), 0, st>>>(B.V->ptr, B.aux->ptr, N, N);
+  } else {
+    // A^T (N x M) = U' S V'^T  =>  A = V' S U'^T: V = U' (N x M), U = V'^T^T from aux (M x M)
+    dim3 g((unsigned)((N + 31) / 32), (unsigned)((M + 31) / 32));
+    transpose_prefix_kernel<<<g, dim3(32, 8), 0, st>>>(B.work->ptr, A, N, M);
+    MPSG_SOLVER(cusolverDnDgesvd(h, 'S', 'S', (int)N, (int)M, B.work->ptr, (int)N, B.S->ptr,
+                                 B.V->ptr, (int)N, B.aux->ptr, (int)M, B.wbuf->ptr, B.lwork,
+                                 nullptr, dinfo));
+    dim3 g2((unsigned)((M + 31) / 32), (unsigned)((M + 31) / 32));
+    transpose_prefix_kernel<<<g2, dim3(32, 8), 0, st>>>(B.U->ptr, B.aux->ptr, M, M);
+  }
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches += 1;
+  (void)k;
+}
+
+// Jacobi SVD of one block on the context stream: the second method tried when QR iteration
+// reports non-convergence.
+void run_jacobi(Context* ctx, const double* A, BlockSVD& B) {
+  cusolverDnHandle_t h = lanes(ctx).sol[0];
+  const int64_t M = B.M, N = B.N, k = B.k;
+  cudaStream_t st = lanes(ctx).st[0];
+  MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  auto work = alloc_buffer(ctx, M * N);
   MPSG_CUDA(cudaMemcpyAsync(work->ptr, A, sizeof(double) * M * N, cudaMemcpyDeviceToDevice,
                             ctx->stream));
+  MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
   gesvdjInfo_t params;
   MPSG_SOLVER(cusolverDnCreateGesvdjInfo(&params));
   int lwork = 0;
   MPSG_SOLVER(cusolverDnDgesvdj_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)M, (int)N,
-                                           work->ptr, (int)M, out.S->ptr, out.U->ptr, (int)M,
-                                           out.V->ptr, (int)N, &lwork, params));
+                                           work->ptr, (int)M, B.S->ptr, B.U->ptr, (int)M,
+                                           B.V->ptr, (int)N, &lwork, params));
   auto wbuf = alloc_buffer(ctx, std::max(lwork, 1));
   int* dinfo = nullptr;
   MPSG_CUDA(cudaMallocAsync((void**)&dinfo, sizeof(int), ctx->stream));
-  MPSG_SOLVER(cusolverDnDgesvdj(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)M, (int)N, work->ptr,
-                                (int)M, out.S->ptr, out.U->ptr, (int)M, out.V->ptr, (int)N,
-                                wbuf->ptr, lwork, dinfo, params));
-  int info = 0;
-  MPSG_CUDA(cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  MPSG_SOLVER(cusolverDnDgesvdj(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)M, (int)N, work->ptr,
+                                (int)M, B.S->ptr, B.U->ptr, (int)M, B.V->ptr, (int)N, wbuf->ptr,
+                                lwork, dinfo, params));
+  int info = 0;
+  MPSG_CUDA(cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MPSG_CUDA(cudaStreamSynchronize(st));
   cusolverDnDestroyGesvdjInfo(params);
-  if (info != 0) {
-    // QR-iteration fallback (needs M >= N: run on the transpose otherwise)
-    MPSG_CUDA(cudaMemcpyAsync(work->ptr, A, sizeof(double) * M * N, cudaMemcpyDeviceToDevice,
-                              ctx->stream));
-    if (M >= N) {
-      auto vt = alloc_buffer(ctx, N * N);
-      MPSG_SOLVER(cusolverDnDgesvd_bufferSize(h, (int)M, (int)N, &lwork));
-      auto w2 = alloc_buffer(ctx, std::max(lwork, 1));
-      MPSG_SOLVER(cusolverDnDgesvd(h, 'S', 'S', (int)M, (int)N, work->ptr, (int)M, out.S->ptr,
-                                   out.U->ptr, (int)M, vt->ptr, (int)N, w2->ptr, lwork, nullptr,
-                                   dinfo));
-      // V = VT^T
-      dim3 g((unsigned)((N + 31) / 32), (unsigned)((N + 31) / 32));
-      transpose_prefix_kernel<<<g, dim3(32, 8), 0, ctx->stream>>>(out.V->ptr, vt->ptr, N, N);
-    } else {
-      auto at = alloc_buffer(ctx, M * N);
-      dim3 g((unsigned)((N + 31) / 32), (unsigned)((M + 31) / 32));
-      // at (N x M) = A^T : rows of at = columns of A
-      transpose_prefix_kernel<<<g, dim3(32, 8), 0, ctx->stream>>>(at->ptr, A, N, M);
-      auto vt = alloc_buffer(ctx, M * M);
-      MPSG_SOLVER(cusolverDnDgesvd_bufferSize(h, (int)N, (int)M, &lwork));
-      auto w2 = alloc_buffer(ctx, std::max(lwork, 1));
-      // A^T = U' S V'^T  =>  A = V' S U'^T: U = V' (M x M), V = U' (N x M)
-      MPSG_SOLVER(cusolverDnDgesvd(h, 'S', 'S', (int)N, (int)M, at->ptr, (int)N, out.S->ptr,
-                                   out.V->ptr, (int)N, vt->ptr, (int)M, w2->ptr, lwork, nullptr,
-                                   dinfo));
-      dim3 g2((unsigned)((M + 31) / 32), (unsigned)((M + 31) / 32));
-      transpose_prefix_kernel<<<g2, dim3(32, 8), 0, ctx->stream>>>(out.U->ptr, vt->ptr, M, M);
-    }
-    MPSG_CUDA(cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (info != 0) {
-      cudaFreeAsync(dinfo, ctx->stream);
-      throw Error(kErrNoConvergence, "block SVD did not converge");
-    }
-  }
   cudaFreeAsync(dinfo, ctx->stream);
-  ctx->kernel_launches += 1;
+  if (info != 0) throw Error(kErrNoConvergence, "block SVD did not converge");
+  (void)k;
+}
+
+// Density-matrix factorisation of one block: the eigen-decomposition of the Gram matrix on the
+// side whose factor must be orthonormal. Left: A A^T = U S^2 U^T, then V = A^T U S^-1. Right:
+// A^T A = V S^2 V^T, then U = A V S^-1. The orthonormal factor is exact to rounding; the other
+// satisfies U S V^T = U U^T A (left) or A V V^T (right) exactly, i.e. the product is the
+// projection of A on the kept singular subspace, which is all a sweep uses of it.
+void prepare_gram(Context* ctx, cusolverDnHandle_t h, BlockSVD& B, bool left) {
+  const int64_t M = B.M, N = B.N, k = B.k, n = left ? M : N;
+  B.U = alloc_buffer(ctx, M * k);
+  B.S = alloc_buffer(ctx, k);
+  B.V = alloc_buffer(ctx, N * k);
+  B.work = alloc_buffer(ctx, n * n);
+  B.aux = alloc_buffer(ctx, n);
+  MPSG_SOLVER(cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                          (int)n, B.work->ptr, (int)n, B.aux->ptr, &B.lwork));
+  B.wbuf = alloc_buffer(ctx, std::max(B.lwork, 1));
+}
+
+void run_gram(Context* ctx, cudaStream_t st, cusolverDnHandle_t h, cublasHandle_t bl,
+              const double* A, BlockSVD& B, bool left, int* dinfo) {
+  const int64_t M = B.M, N = B.N, k = B.k, n = left ? M : N;
+  const double one = 1.0, zero = 0.0;
+  double* G = B.work->ptr;
+  if (left)
+    MPSG_BLAS(cublasDsyrk(bl, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, (int)M, (int)N, &one, A,
+                          (int)M, &zero, G, (int)M));
+  else
+    MPSG_BLAS(cublasDsyrk(bl, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, (int)N, (int)M, &one, A,
+                          (int)M, &zero, G, (int)N));
+  MPSG_SOLVER(cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)n, G,
+                               (int)n, B.aux->ptr, B.wbuf->ptr, B.lwork, dinfo));
+  double* X = left ? B.U->ptr : B.V->ptr;  // orthonormal factor
+  double* Y = left ? B.V->ptr : B.U->ptr;  // the other one
+  top_eigpairs_kernel<<<grid_for(n * k), 256, 0, st>>>(X, B.S->ptr, G, B.aux->ptr, n, k);
+  if (left)  // V (N x k) = A^T U
+    MPSG_BLAS(cublasDgemm(bl, CUBLAS_OP_T, CUBLAS_OP_N, (int)N, (int)k, (int)M, &one, A, (int)M,
+                          X, (int)M, &zero, Y, (int)N));
+  else  // U (M x k) = A V
+    MPSG_BLAS(cublasDgemm(bl, CUBLAS_OP_N, CUBLAS_OP_N, (int)M, (int)k, (int)N, &one, A, (int)M,
+                          X, (int)N, &zero, Y, (int)M));
+  const int64_t rows = left ? N : M;
+  scale_cols_inv_kernel<<<grid_for(rows * k), 256, 0, st>>>(Y, B.S->ptr, rows, k);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches += 2;
 }
 
 }  // namespace
@@ -178,22 +295,81 @@ std::vector<int64_t> truncatedsizes(const std::vector<std::vector<double>>& S, i
 }
 
 SVDResult svd_blocks(Context* ctx, const DeviceTensor& A, bool truncate, int64_t maxdim,
-                     double tol, double tieband) {
+                     double tol, double tieband, int method) {
   if (A.meta.N() != 2) throw Error(kErrArgument, "svd needs a rank-2 tensor (SymMatrix)");
+  if (method != kSvdExact && method != kSvdGramLeft && method != kSvdGramRight)
+    throw Error(kErrArgument, "unknown SVD method");
   const size_t nb = A.meta.nblocks();
+  SolverLanes& L = lanes(ctx);
   std::vector<BlockSVD> blocks(nb);
   std::vector<std::vector<double>> S(nb);
+  // all buffers first (stream-ordered on the context stream), then fork the lanes
   for (size_t b = 0; b < nb; ++b) {
-    blocks[b].c1 = A.meta.sec.labels(b)[0];
-    blocks[b].c2 = A.meta.sec.labels(b)[1];
-    blocks[b].M = A.meta.sec.sizes(b)[0];
-    blocks[b].N = A.meta.sec.sizes(b)[1];
-    block_svd(ctx, A.data() + A.meta.off[b], blocks[b]);
+    BlockSVD& B = blocks[b];
+    B.c1 = A.meta.sec.labels(b)[0];
+    B.c2 = A.meta.sec.labels(b)[1];
+    B.M = A.meta.sec.sizes(b)[0];
+    B.N = A.meta.sec.sizes(b)[1];
+    B.k = std::min(B.M, B.N);
+    if (method == kSvdExact) prepare_exact(ctx, L.sol[0], B);
+    else prepare_gram(ctx, L.sol[0], B, method == kSvdGramLeft);
+  }
+  int* dinfo = nullptr;
+  if (nb) {
+    MPSG_CUDA(cudaMallocAsync((void**)&dinfo, sizeof(int) * nb, ctx->stream));
+    MPSG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * nb, ctx->stream));
+  }
+  // largest blocks first, each to the least loaded lane
+  std::vector<size_t> order(nb);
+  for (size_t b = 0; b < nb; ++b) order[b] = b;
+  auto cost = [&](size_t b) {
+    const double m = (double)std::max(blocks[b].M, blocks[b].N);
+    const double n = (double)blocks[b].k;
+    return m * n * n + n * n * n;
+  };
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t x, size_t y) { return cost(x) > cost(y); });
+  MPSG_CUDA(cudaEventRecord(L.fork, ctx->stream));
+  double load[kLanes] = {0, 0, 0, 0};
+  bool used[kLanes] = {false, false, false, false};
+  for (size_t b : order) {
+    int lane = 0;
+    for (int i = 1; i < kLanes; ++i)
+      if (load[i] < load[lane]) lane = i;
+    if (!used[lane]) {
+      MPSG_CUDA(cudaStreamWaitEvent(L.st[lane], L.fork, 0));
+      used[lane] = true;
+    }
+    load[lane] += cost(b);
+    const double* Ab = A.data() + A.meta.off[b];
+    if (method == kSvdExact) run_exact(ctx, L.st[lane], L.sol[lane], Ab, blocks[b], dinfo + b);
+    else run_gram(ctx, L.st[lane], L.sol[lane], L.blas[lane], Ab, blocks[b],
+                  method == kSvdGramLeft, dinfo + b);
+  }
+  for (int i = 0; i < kLanes; ++i) {
+    if (!used[i]) continue;
+    MPSG_CUDA(cudaEventRecord(L.join[i], L.st[i]));
+    MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, L.join[i], 0));
+  }
+  std::vector<int> info(nb, 0);
+  if (nb)
+    MPSG_CUDA(cudaMemcpyAsync(info.data(), dinfo, sizeof(int) * nb, cudaMemcpyDeviceToHost,
+                              ctx->stream));
+  for (size_t b = 0; b < nb; ++b) {
     S[b].resize(blocks[b].k);
     MPSG_CUDA(cudaMemcpyAsync(S[b].data(), blocks[b].S->ptr, sizeof(double) * blocks[b].k,
                               cudaMemcpyDeviceToHost, ctx->stream));
   }
   MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (dinfo) cudaFreeAsync(dinfo, ctx->stream);
+  for (size_t b = 0; b < nb; ++b) {
+    if (info[b] == 0) continue;
+    if (method != kSvdExact)
+      throw Error(kErrNoConvergence, "symmetric eigensolver of a Gram block did not converge");
+    run_jacobi(ctx, A.data() + A.meta.off[b], blocks[b]);
+    MPSG_CUDA(cudaMemcpy(S[b].data(), blocks[b].S->ptr, sizeof(double) * blocks[b].k,
+                         cudaMemcpyDeviceToHost));
+  }
   std::vector<int64_t> ns(nb);
   if (truncate) {
     ns = truncatedsizes(S, maxdim, tol, tieband);

@@ -16,9 +16,15 @@ struct SVDResult {
   std::vector<std::pair<int, int>> kept_sectors;
 };
 
+// Per-block factorisation methods. Exact: thin SVD (QR iteration). Gram left / right: the
+// density-matrix truncation, eigen-decomposition of A A^T (u orthonormal) or A^T A (v
+// orthonormal); the other factor carries S^-1 times the projection of A, so u s v^T equals the
+// projection of A on the kept singular subspace.
+enum SvdMethod { kSvdExact = 0, kSvdGramLeft = 1, kSvdGramRight = 2 };
+
 // _svd_ (truncate=false, src/symtools.jl:1-35) and svdtrunc (src/mpsutils.jl:116-179).
 SVDResult svd_blocks(Context* ctx, const DeviceTensor& A, bool truncate, int64_t maxdim,
-                     double tol, double tieband);
+                     double tol, double tieband, int method = kSvdExact);
 
 struct EigResult {
   double value = 0;

@@ -217,8 +217,8 @@ static void run_gemm(Context* ctx, DevGemmPlan& g, const double* A, const double
     launch_gemm_f64(ctx, g, A, B, C);
     return;
   }
-  if (precision < 2 || precision > 4)
-    throw Error(kErrUnsupported, "precision must be 0 (FP64) or 2..4 bf16 slices");
+  if (precision < 2 || precision > split::kMaxSlices)
+    throw Error(kErrUnsupported, "precision must be 0 (FP64) or 2..7 bf16 slices");
   auto& sp = g.splitp[precision];
   if (!sp) {
     sp = std::make_shared<split::SplitPlan>();
@@ -439,8 +439,8 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
     op->W2 = W2;
     return op;
   }
-  if (precision < 2 || precision > 4)
-    throw Error(kErrUnsupported, "precision must be 0 (FP64) or 2..4 bf16 slices");
+  if (precision < 2 || precision > split::kMaxSlices)
+    throw Error(kErrUnsupported, "precision must be 0 (FP64) or 2..7 bf16 slices");
   op->envLW = contract(ctx, envL, kLW_A, W1, kLW_B, 0, nullptr);
   op->envRW = contract(ctx, W2, kRW_A, envR, kRW_B, 0, nullptr);
   op->c1 = private_contract_plan(op->envLW.meta, kX_A, vmeta, kX_B);

@@ -10,6 +10,7 @@ namespace split {
 
 constexpr int BM = 128, BN = 64, BK = 64;
 constexpr int kSliceBits = 7;  // beta: bits per bf16 slice digit
+constexpr int kMaxSlices = 7;  // 49 bits: the FP64-class setting
 
 // One sector GEMM as the split kernels see it (column-major A: M x K, B: K x N, C: M x N).
 struct Problem {

@@ -187,6 +187,34 @@ def random_mps_host(lx: int, M: int, chimax: int, seed: int = 1911):
     return out
 
 
+def binomial_bond_dims(lx, site, M, chimax):
+    """Charges of the bond right of ``site`` with a total dimension of about ``chimax``: each
+    charge c gets chimax * w_c / sum(w) states (w_c = C(site, c) C(lx - site, M - c), the number
+    of basis states through that charge), at least 1 and at most the exact count."""
+    exact = bond_dims(lx, site, M, 1 << 62)
+    if sum(d for _, d in exact) <= chimax:
+        return exact
+    w = [math.comb(site, c) * math.comb(lx - site, M - c) for c, _ in exact]
+    tot = float(sum(w))
+    return [(c, max(1, min(d, int(round(chimax * wc / tot))))) for (c, d), wc in zip(exact, w)]
+
+
+def binomial_mps_host(lx: int, M: int, chimax: int, seed: int = 1911):
+    """Like random_mps_host but with bond dimensions from binomial_bond_dims, so every bond
+    holds about chimax states in total (the workload of a sweep at fixed maximal chi)."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    d = U1Space(*SITE)
+    Vl = U1Space((0, 1))
+    out = []
+    for site in range(1, lx + 1):
+        Vr = VectorSpace(binomial_bond_dims(lx, site, M, chimax))
+        sp = (Vl, d, dual(Vr))
+        n = mg.meta(0, sp).numel()
+        out.append((0, sp, rng.standard_normal(n)))
+        Vl = Vr
+    return out
+
+
 def mps_from_host(sites, ctx=None) -> MPState:
     return MPState([mg.from_flat(c, sp, f, ctx) for c, sp, f in sites], center=0)
 
@@ -245,10 +273,15 @@ def initialenv(mps: MPState, Ws, at: int = 1, precision: int = 0):
 class SweepOptions:
     """Keyword arguments of ``dmrg2sitesweep!`` (src/dmrg.jl:58-66) plus the precision split:
     ``precision`` for the Krylov matvecs, ``energy_precision`` for the post-truncation energy
-    matvec (dmrg.jl:92-93) and ``env_precision`` for environment updates."""
+    matvec (dmrg.jl:92-93) and ``env_precision`` for environment updates. ``svd`` selects the
+    truncation: "exact" per-sector SVD (the reference's svdtrunc) or "gram", the density-matrix
+    truncation that keeps the new site tensor orthonormal (u going right, v going left)."""
 
     def __init__(self, maxdim=200, tol=1e-9, lanczostol=1e-7, krylovdim=5, krylovmaxiter=8,
-                 tieband=0.0, precision=0, energy_precision=0, env_precision=0):
+                 tieband=0.0, precision=0, energy_precision=0, env_precision=0, svd="exact"):
+        if svd not in ("exact", "gram"):
+            raise ValueError(f"svd must be 'exact' or 'gram', not {svd!r}")
+        self.svd = svd
         self.maxdim = maxdim
         self.tol = tol
         self.lanczostol = lanczostol
@@ -260,9 +293,12 @@ class SweepOptions:
         self.env_precision = env_precision
 
 
-def _truncate_and_energy(v, AA, env, Ws, l, o: SweepOptions):
+def _truncate_and_energy(v, AA, env, Ws, l, o: SweepOptions, keep="left"):
+    """svdtrunc + normalisation + post-truncation energy (dmrg.jl:88-93); ``keep`` names the
+    factor that becomes the new (orthonormal) site tensor."""
+    method = "exact" if o.svd == "exact" else "gram_" + keep
     u, s, vt = mg.svdtrunc(mg.SymMatrix(v, [1, 2], [3, 4]), maxdim=o.maxdim, tol=o.tol,
-                           tieband=o.tieband)
+                           tieband=o.tieband, method=method)
     ns = mg.norm(s)
     truncerr = 1.0 - ns
     mg.rmul(s, 1.0 / ns)
@@ -305,7 +341,7 @@ def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stat
     v = _eig(AA, env, Ws, l, o, stats)
     e = None
     for l in range(lx - 1, 1, -1):
-        u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o)
+        u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o, keep="right")
         energies.append(e)
         mps.As[l] = mg.splitleg(vt, 2, AA.space[2:4])
         env[l + 1] = mg.mpsupdateright(env[l + 2], mps.As[l], Ws[l], precision=o.env_precision)
@@ -314,7 +350,7 @@ def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stat
         v = _eig(AA, env, Ws, l - 1, o, stats)
         energies.append(e)
     l = 1
-    u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o)
+    u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o, keep="right")
     energies.append(e)
     mps.As[1] = mg.splitleg(vt, 2, AA.space[2:4])
     env[2] = mg.mpsupdateright(env[3], mps.As[1], Ws[1], precision=o.env_precision)

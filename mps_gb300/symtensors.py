@@ -585,14 +585,29 @@ def _svd_(A: SymTensor):
     return SymTensor(u, A.ctx), SymTensor(s, A.ctx), SymTensor(v, A.ctx)
 
 
-def svdtrunc(A: SymTensor, maxdim=None, tol: float = 1e-12, tieband: float = 0.0):
+SVD_METHODS = ("exact", "gram_left", "gram_right")
+
+
+def svdtrunc(A: SymTensor, maxdim=None, tol: float = 1e-12, tieband: float = 0.0,
+             method: str = "exact"):
     """``svdtrunc(A; maxdim, tol)`` (src/mpsutils.jl:116-179): absolute ``tol``, global greedy
-    ``maxdim``; ``tieband`` > 0 widens ties (0 = the reference rule)."""
+    ``maxdim``; ``tieband`` > 0 widens ties (0 = the reference rule).
+
+    ``method``: "exact" per-sector thin SVD; "gram_left" / "gram_right" the density-matrix
+    truncation (eigen-decomposition of A A^T / A^T A): u (resp. v) orthonormal, and u*s*v the
+    projection of A on the kept singular subspace."""
     if maxdim is None:
         maxdim = max(A.size())
+    if method not in SVD_METHODS:
+        raise MPSGError(_lib.ERR_ARGUMENT, f"unknown svd method {method!r}")
     u, s, v = C.c_void_p(), C.c_void_p(), C.c_void_p()
-    call("mpsg_svdtrunc", A.ctx.handle, A.handle, int(maxdim), float(tol), float(tieband),
-         C.byref(u), C.byref(s), C.byref(v))
+    if method == "exact":
+        call("mpsg_svdtrunc", A.ctx.handle, A.handle, int(maxdim), float(tol), float(tieband),
+             C.byref(u), C.byref(s), C.byref(v))
+    else:
+        call("mpsg_svdtrunc_gram", A.ctx.handle, A.handle, int(maxdim), float(tol),
+             float(tieband), 0 if method == "gram_left" else 1, C.byref(u), C.byref(s),
+             C.byref(v))
     return SymTensor(u, A.ctx), SymTensor(s, A.ctx), SymTensor(v, A.ctx)
 
 
