@@ -8,9 +8,12 @@ v -> envL . W1 . W2 . envR . v with every input resident in HBM.
 
 Metric: H_eff GFLOP/s = planner-counted algorithmic flops (sum over the sector GEMMs of the four
 contractions of 2*M*N*K) / seconds per step.  Every timed step is preceded by an L2 flush
-(a 512 MiB write on the library's stream) outside the timed events.
+(a 512 MiB write on the library's stream) outside the timed events.  The line also carries
+"sweep": one 2-site DMRG sweep at maxdim = chi, FP64 drop-in vs the mixed configuration, with
+the energy difference between the two.
 
     python bench.py [--steps K] [--warmup W] [--precision P] [--impl ours|reference]
+                    [--no-sweep] [--sweep-chi X]
 
 Multi-GPU (torchrun): one independent replica per rank (a DMRG chain does not shard), value =
 all ranks' flops / max-over-ranks time, "scaling": "weak".
@@ -32,7 +35,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "H_eff matvec GFLOP/s at chi=2048 (2-site DMRG hot path)"
 UNIT = "GFLOP/s"
-DEFAULT_SLICES = 3  # split precision used for the headline (0 = FP64)
+# split precision of the headline H_eff: the Krylov setting of the mixed sweep, the fewest
+# slices whose sweep energies stay within 1e-10 of the FP64 drop-in (0 = FP64)
+DEFAULT_SLICES = 4
 
 
 def parse():
@@ -45,6 +50,8 @@ def parse():
     p.add_argument("--precision", type=int, default=None,
                    help="0 = FP64; s >= 2 = split bf16 with s slices (default: best available)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-sweep", action="store_true", help="skip the DMRG sweep measurement")
+    p.add_argument("--sweep-chi", type=int, default=None, help="maxdim of the sweep (default chi)")
     return p.parse_args()
 
 
@@ -189,6 +196,52 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------------------------
+SWEEP_MIXED = dict(precision=4, energy_precision=7, env_precision=7, svd="gram")
+SWEEP_FP64 = dict(precision=0, energy_precision=0, env_precision=0, svd="exact")
+
+
+def sweep_bench(ctx, chi, lx=32, seed=7):
+    """One 2-site DMRG sweep (src/dmrg.jl:58-179) of the L=lx Heisenberg chain (J=1, OBC, Sz=0)
+    at maxdim=chi from a random MPS whose bonds hold about chi states (binomial charge profile),
+    canonicalised at site 1 with environments built (untimed). The sweep runs twice from copies
+    of that state: the plain FP64 drop-in (FP64 contractions, exact per-sector SVD) and the mixed
+    configuration (split-precision Krylov matvecs, FP64-class 7-slice energy and environment
+    contractions, density-matrix truncation). Both are timed end to end on the host around a
+    device synchronisation; |dE| compares every post-truncation energy of the two sweeps."""
+    import mps_gb300 as mg
+    from mps_gb300 import dmrg as gd
+    Ws = gd.xxz_u1mpo(lx, 1.0, ctx=ctx)
+    m0 = gd.mps_from_host(gd.binomial_mps_host(lx, lx // 2, chi, seed), ctx)
+    gd.center_at(m0, 1, svd="gram")
+    env0 = gd.initialenv(m0, Ws)
+    kw = dict(maxdim=chi, tol=1e-10, lanczostol=1e-7, krylovdim=4, krylovmaxiter=8)
+    out = {}
+    for name, cfg in (("fp64", SWEEP_FP64), ("mixed", SWEEP_MIXED)):
+        mps = gd.MPState([mg.copy(A) for A in m0.As], center=1)
+        env = [None if e is None else mg.copy(e) for e in env0]
+        stats = []
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        es = gd.dmrg2sitesweep(mps, Ws, env, stats=stats, **kw, **cfg)
+        ctx.synchronize()
+        out[name] = (time.perf_counter() - t0, es, sum(i.numops for i in stats))
+    t64, e64, n64 = out["fp64"]
+    tmx, emx, nmx = out["mixed"]
+    de = [abs(a - b) for a, b in zip(emx, e64)]
+    return {
+        "workload": f"one 2-site DMRG sweep, Heisenberg chain L={lx} (J=1, OBC, Sz=0), "
+                    f"maxdim={chi}, cutoff 1e-10, Krylov dim 4, maxiter 8, tol 1e-7; initial "
+                    f"MPS: N(0,1) blocks (Philox seed {seed}), binomial bond profile ~{chi}",
+        "fp64_s": t64, "mixed_s": tmx, "speedup_mixed_vs_fp64": t64 / tmx,
+        "mixed_config": {k: v for k, v in SWEEP_MIXED.items()},
+        "fp64_config": {k: v for k, v in SWEEP_FP64.items()},
+        "energy_fp64": e64[-1], "energy_mixed": emx[-1],
+        "dE_final": abs(emx[-1] - e64[-1]), "dE_max_over_sweep": max(de),
+        "dE_rel_final": abs(emx[-1] - e64[-1]) / abs(e64[-1]),
+        "matvecs_fp64": n64, "matvecs_mixed": nmx, "energies_per_sweep": len(e64),
+    }
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -316,15 +369,20 @@ def run_ours(args):
         peak_src = "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback 1.9 PFLOP/s"
         pipe = "bf16-tensor (tcgen05)"
         dtype = f"f64 via {S} bf16 slices ({S * (S + 1) // 2} tcgen05 products, fp32 TMEM accumulate)"
-        # achieved counts ALGORITHMIC flops (the reference's contraction order), not the
-        # executed slice products
-        achieved = flops * args.steps / (gem_ms / 1e3) / 1e12 if gem_n else None
-        kernel_desc = ("split-precision grouped block GEMM (2 launches per H_eff application; "
-                       "achieved = reference-order algorithmic flops / summed GEMM time)")
+        # achieved = the kernel's own algorithmic flops (sum of 2*M*N*K over the sector GEMMs of
+        # the two W-folded contractions it runs) per second, not the executed slice products
+        achieved = gem_f / (gem_ms / 1e3) / 1e12 if gem_n else None
+        kernel_desc = ("split-precision grouped block GEMM (2 launches per H_eff application, "
+                       "the W-folded contractions envLW.v and X.envRW; achieved = their sector "
+                       "GEMM flops / summed GEMM time)")
+    pairs = S * (S + 1) // 2 if S else 1
     roof = {"bound": "tensor", "pipe": pipe, "kernel": kernel_desc, "launches_timed": gem_n,
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if achieved else None, "peak_source": peak_src + " (of measured)"
             if peaks else peak_src,
+            # executed tensor work: every algorithmic flop costs `pairs` bf16 slice products
+            "executed_tflops": achieved * pairs if achieved else None,
+            "executed_frac": achieved * pairs / peak if achieved else None,
             "traffic": profile_traffic(f"gemm_p{S}_chi{args.chi}")}
     share = {k: round(v_[0] / args.steps / step_ms, 4) for k, v_ in kinds.items() if v_[1]}
 
@@ -349,6 +407,8 @@ def run_ours(args):
         "roofline": roof,
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_sweep and ws == 1:
+        line["sweep"] = sweep_bench(ctx, args.sweep_chi or args.chi)
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
         os.environ.setdefault("OPENBLAS_NUM_THREADS", str(os.cpu_count() or 1))
         vv, n, tm, cores = cpu_heff_rate(args.chi, flops)

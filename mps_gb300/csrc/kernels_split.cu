@@ -13,7 +13,7 @@
 //   * MMA.  For every slice pair (p, q) with p + q < S, tcgen05.mma (M=128, N=64, K=16, bf16
 //     in, FP32 out) accumulates into TMEM accumulator g = p + q.  Within one chunk every product
 //     of group g is an integer multiple of one power of two and the sum stays below 2^24 units
-//     (pairs(g) * chunk * 2^(2 beta) <= 2^24), so the FP32 accumulation is exact.
+//     (chunk * 2^12 * max(4, g + 3) <= 2^24, exact_chunk), so the FP32 accumulation is exact.
 //   * Epilogue.  After each chunk the 4 epilogue warps drain the S accumulators (tcgen05.ld)
 //     into a double-single (hi, lo) FP32 pair per output element (TwoSum, exact up to 2^-48),
 //     release TMEM to the MMA warp (double-buffered), and after the last chunk assemble
@@ -464,16 +464,16 @@ __device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
   return d;
 }
 
-// Exact mode. The K step is 64 (128-byte swizzle) up to 4 slices; with 5..7 slices it is 32
-// (64-byte swizzle) so that a pipeline stage holding all S slices of both operands still fits
-// twice in shared memory. A chunk (the K range between exact FP32 flushes) is a multiple of 64:
-// chunk * (pairs in a group <= S) * 2^14 <= 2^24 keeps every TMEM sum an exact integer.
+// Exact mode. The K step is 64 (128-byte swizzle) up to 3 slices; with 4..7 slices it is 32
+// (64-byte swizzle) so that a pipeline stage holding all S slices of both operands fits 2 to 4
+// times in shared memory. A chunk (the K range between exact FP32 flushes, exact_chunk) is a
+// multiple of 64.
 template <int S>
 struct Cfg {
-  static constexpr int kBK = S <= 4 ? 64 : 32;
+  static constexpr int kBK = S <= 3 ? 64 : 32;
   static constexpr int kPerRow = 64 / kBK;  // K steps per 64-wide packed row
   static constexpr int kPairs = S * (S + 1) / 2;
-  static constexpr int kChunk = ((1024 / S) / 64) * 64;
+  static constexpr int kChunk = exact_chunk(S);
   static constexpr int kChunkSteps = kChunk / kBK;
   static constexpr int kABytes = BM * kBK * 2;
   static constexpr int kBBytes = BN * kBK * 2;
@@ -930,7 +930,7 @@ static void make_map(CUtensorMap* map, void* base, int64_t rows_total, int S, in
   if (r != CUDA_SUCCESS) throw Error(kErrCuda, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-int chunk_for(int S) { return ((1024 / S) / BK) * BK; }
+int chunk_for(int S) { return exact_chunk(S); }
 
 void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   release();
@@ -1026,7 +1026,7 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   MPSG_CUDA(cudaMalloc(&d_packB, std::max<int64_t>(S * rowsB * 64 * 2, 128 * 128)));
   MPSG_CUDA(cudaMalloc(&d_err, sizeof(int)));
   MPSG_CUDA(cudaMemset(d_err, 0, sizeof(int)));
-  const int box_x = (fast || S > 4) ? 32 : BK;  // K step of the kernel that reads the slices
+  const int box_x = (fast || S > 3) ? 32 : BK;  // K step of the kernel that reads the slices
   make_map(&tmA, d_packA, std::max<int64_t>(rowsA, BM), S, BM, box_x);
   make_map(&tmB, d_packB, std::max<int64_t>(rowsB, bn), S, bn, box_x);
   (void)ctx;

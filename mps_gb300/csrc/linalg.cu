@@ -284,8 +284,10 @@ std::vector<int64_t> truncatedsizes(const std::vector<std::vector<double>>& S, i
       break;
     }
     if (ptr[index] + 1 >= (int64_t)S[index].size()) {
+      // exhausted sector: the reference sets 0.0 (below any tol > 0); -1 also keeps a tol <= 0
+      // walk from stepping past the sector's last value
       ptr[index] += 1;
-      c[index] = 0.0;
+      c[index] = -1.0;
     } else {
       ptr[index] += 1;
       c[index] = S[index][ptr[index]];
@@ -371,7 +373,12 @@ SVDResult svd_blocks(Context* ctx, const DeviceTensor& A, bool truncate, int64_t
                          cudaMemcpyDeviceToHost));
   }
   std::vector<int64_t> ns(nb);
-  if (truncate) {
+  int64_t total = 0;
+  for (size_t b = 0; b < nb; ++b) total += blocks[b].k;
+  // keep-everything requests (tol <= 0, maxdim >= total) skip the greedy walk, which with
+  // tol = 0 could step past an exhausted sector on zero values
+  const bool keep_all = tol <= 0.0 && maxdim >= total;
+  if (truncate && !keep_all) {
     ns = truncatedsizes(S, maxdim, tol, tieband);
   } else {
     for (size_t b = 0; b < nb; ++b) ns[b] = blocks[b].k;

@@ -12,6 +12,12 @@ constexpr int BM = 128, BN = 64, BK = 64;
 constexpr int kSliceBits = 7;  // beta: bits per bf16 slice digit
 constexpr int kMaxSlices = 7;  // 49 bits: the FP64-class setting
 
+// K chunk of the exact mode: the longest K range whose group sums stay exact FP32 integers.
+// Balanced digits satisfy |t_0| <= 2^7 and |t_p| <= 2^6 (p >= 1), so one K index adds at most
+// 2^14 to group 0 and 2 * 2^13 + (g - 1) * 2^12 = 2^12 (g + 3) to group g >= 1; with g <= S-1
+// the chunk is 2^24 / (2^12 max(4, S + 2)), rounded down to a multiple of 64 (one packed row).
+constexpr int exact_chunk(int S) { return ((4096 / (S + 2 > 4 ? S + 2 : 4)) / 64) * 64; }
+
 // One sector GEMM as the split kernels see it (column-major A: M x K, B: K x N, C: M x N).
 struct Problem {
   int64_t M, N, K;

@@ -219,33 +219,42 @@ def mps_from_host(sites, ctx=None) -> MPState:
     return MPState([mg.from_flat(c, sp, f, ctx) for c, sp, f in sites], center=0)
 
 
-def _pushleft(mps: MPState, l: int):
+def _factor(M, keep, svd):
+    """Full (untruncated) per-sector factorisation M = u s v with the ``keep`` factor
+    orthonormal: the exact SVD (_svd_) or the density-matrix method."""
+    if svd == "exact":
+        return mg._svd_(M)
+    return mg.svdtrunc(M, maxdim=max(M.size()), tol=0.0, method="gram_" + keep)
+
+
+def _pushleft(mps: MPState, l: int, svd="exact"):
     """``_pushleft!`` (src/symmps.jl:167-174), 1-based ``l``."""
     A = mps.As[l - 1]
-    u, s, v = mg._svd_(mg.fuselegs(A, 2, 2))
+    u, s, v = _factor(mg.fuselegs(A, 2, 2), "right", svd)
     mps.As[l - 1] = mg.splitleg(v, 2, A.space[1:3])
     mps.As[l - 2] = mg.contract(mps.As[l - 2], (1, 2, -1), mg.matmul(u, s, precision=0), (-1, 3),
                                 precision=0)
 
 
-def _pushright(mps: MPState, l: int):
+def _pushright(mps: MPState, l: int, svd="exact"):
     """``_pushright!`` (src/symmps.jl:176-183)."""
     A = mps.As[l - 1]
-    u, s, v = mg._svd_(mg.fuselegs(A, 1, 2))
+    u, s, v = _factor(mg.fuselegs(A, 1, 2), "left", svd)
     mps.As[l - 1] = mg.splitleg(u, 1, A.space[0:2])
     mps.As[l] = mg.contract(mg.matmul(s, v, precision=0), (1, -1), mps.As[l], (-1, 2, 3),
                             precision=0)
 
 
-def center_at(mps: MPState, center: int) -> MPState:
-    """``center_at!`` (src/symmps.jl:185-200)."""
+def center_at(mps: MPState, center: int, svd: str = "exact") -> MPState:
+    """``center_at!`` (src/symmps.jl:185-200). ``svd="gram"`` canonicalises with the
+    density-matrix factorisation (same bond spaces, orthonormal site tensors)."""
     x1, xL = 1, len(mps)
     if mps.center > 0:
         x1 = xL = mps.center
     for p in range(x1, center):
-        _pushright(mps, p)
+        _pushright(mps, p, svd)
     for p in range(xL, center, -1):
-        _pushleft(mps, p)
+        _pushleft(mps, p, svd)
     mps.center = center
     return mps
 

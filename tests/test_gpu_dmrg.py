@@ -139,6 +139,36 @@ def test_dmrg_sweep_small_chain():
         np.testing.assert_allclose(e_d, e_o, rtol=1e-10, atol=0)
 
 
+def test_mixed_sweep_energies_within_1e10_of_fp64():
+    """The mixed sweep configuration (4-slice Krylov matvecs, 7-slice energy and environment
+    contractions, density-matrix truncation) against the FP64 drop-in sweep (FP64 everywhere,
+    exact per-sector SVD) from the same canonical MPS: every post-truncation energy of the
+    second sweep within 1e-10 relative. In the first sweep from the random state some Lanczos
+    solves stop at maxiter before converging, so their energies depend on the Krylov trajectory
+    and only agree to 1e-8. Bond spaces are not compared: the Gram eigen-decomposition resolves
+    singular values only down to about 1e-8 of the largest, so where the absolute cutoff (1e-10)
+    decides, the two truncations may keep a few different states of weight below 1e-16."""
+    lx, chi = 20, 96
+    _, md, _, Wd, _, ed = heisenberg_setup(lx, chi, seed=11)
+    # SU(2) multiplets give exactly equal singular values in different charge sectors; the tie
+    # band makes the sector that keeps a state cut by maxdim independent of rounding noise
+    kw = dict(maxdim=chi, tol=1e-10, lanczostol=1e-8, krylovdim=4, krylovmaxiter=8,
+              tieband=1e-9)
+    cfgs = {"fp64": dict(precision=0, energy_precision=0, env_precision=0, svd="exact"),
+            "mixed": dict(precision=4, energy_precision=7, env_precision=7, svd="gram")}
+    res = {}
+    for name, cfg in cfgs.items():
+        mps = gd.MPState([mg.copy(A) for A in md.As], center=1)
+        env = [None if e is None else mg.copy(e) for e in ed]
+        es = [gd.dmrg2sitesweep(mps, Wd, env, **kw, **cfg) for _ in range(2)]
+        res[name] = (es, [A.space for A in mps.As])
+    (first_mx, last_mx), (first_64, last_64) = res["mixed"][0], res["fp64"][0]
+    np.testing.assert_allclose(first_mx, first_64, rtol=1e-8, atol=0)
+    np.testing.assert_allclose(last_mx, last_64, rtol=1e-10, atol=0)
+    for sp_mx, sp_64 in zip(res["mixed"][1], res["fp64"][1]):  # same charges, dims within 4
+        assert abs(sp_mx[2].dim() - sp_64[2].dim()) <= 4
+
+
 def test_dmrg_heisenberg_L32_chi64_four_sweeps():
     """The chi<=64 Heisenberg-chain workload: every post-truncation energy of every sweep within
     1e-10 relative of the oracle, final energy below the L=32 OBC ground energy bound."""

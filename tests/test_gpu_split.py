@@ -78,6 +78,30 @@ def test_split_exact_on_small_integers():
         assert np.array_equal(got, want), S
 
 
+def exact_chunk(S):
+    """K chunk of the exact mode: 2^24 / (2^12 max(4, S + 2)) rounded down to a multiple of 64."""
+    return ((4096 // max(4, S + 2)) // 64) * 64
+
+
+@pytest.mark.parametrize("S", ALL_S)
+def test_split_exact_accumulation_at_digit_bounds(S):
+    """x = 127.5/128 has the largest balanced digits (t_0 = 2^7, t_1 = -2^6): over one exact
+    chunk every group sum reaches its bound, and K x^2 (representable) must come out exact, also
+    across chunk boundaries. Pins the chunk length of the exact mode. (S = 2 keeps only p + q < 2,
+    so its t_1 t_1 term is truncated by design and the result is not exact.)"""
+    if S == 2:
+        pytest.skip("the t_1 t_1 product lies outside the S = 2 triangle")
+    if S <= 3 and not EXACT:
+        pytest.skip("S <= 3 runs the fast mode (one FP32 accumulator) unless MPSG_SPLIT_EXACT=1")
+    x = 127.5 / 128
+    for K in (exact_chunk(S), 3 * exact_chunk(S) + 64):
+        Vl, Vk, Vr = U1Space((0, 130)), U1Space((0, K)), U1Space((0, 70))
+        A = st.SymTensor(0, (Vl, dual(Vk)), {(0, 0): np.full((130, K), x)})
+        B = st.SymTensor(0, (Vk, dual(Vr)), {(0, 0): np.full((K, 70), -x)})
+        got = mg.matmul(to_device(A), to_device(B), precision=S).blocks[(0, 0)]
+        assert np.all(got == -K * x * x), (S, K)
+
+
 def test_split_zero_sectors_and_partner_free_blocks():
     rng = np.random.default_rng(3)
     # A has a row charge whose contracted partner does not exist in B's column space

@@ -104,7 +104,9 @@ def test_gram_truncation_all_below_tol_raises_like_reference():
 
 def test_sweep_with_gram_truncation_matches_exact_sweep():
     """Two sweeps of the L=16 Heisenberg chain (chi <= 32) with the density-matrix truncation
-    against the exact-SVD sweep on the device, from the same canonical MPS."""
+    against the exact-SVD sweep on the device, from the same canonical MPS. Here maxdim decides
+    every truncation (cut values far above the Gram resolution of ~1e-8 * max S), so the bond
+    spaces agree exactly; the tie band keeps SU(2) multiplets cut by maxdim out of the noise."""
     lx, chi = 16, 32
     Ws = gd.xxz_u1mpo(lx, 1.0)
     host = gd.random_mps_host(lx, lx // 2, chi, seed=3)
@@ -116,7 +118,7 @@ def test_sweep_with_gram_truncation_matches_exact_sweep():
         es = []
         for _ in range(2):
             es.append(gd.dmrg2sitesweep(mps, Ws, env, maxdim=chi, tol=1e-10, lanczostol=1e-9,
-                                        krylovdim=4, krylovmaxiter=8, svd=svd))
+                                        krylovdim=4, krylovmaxiter=8, svd=svd, tieband=1e-9))
         runs[svd] = (es, [A.space for A in mps.As])
     np.testing.assert_allclose(runs["gram"][0][-1], runs["exact"][0][-1], rtol=1e-9, atol=0)
     assert runs["gram"][1] == runs["exact"][1]
