@@ -158,6 +158,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// 16 consecutive FP32 columns of one TMEM lane per thread (shape 32x32b, 16 repetitions)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 // Shared-memory matrix descriptor: K-major operand tile, 128-byte swizzle, 8-row groups 1024 B
 // apart (stride byte offset), base 1024-byte aligned.
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
@@ -475,16 +487,22 @@ struct Cfg {
   static constexpr int kPairs = S * (S + 1) / 2;
   static constexpr int kChunk = exact_chunk(S);
   static constexpr int kChunkSteps = kChunk / kBK;
+  static constexpr int kBN = exact_bn(S);
   static constexpr int kABytes = BM * kBK * 2;
-  static constexpr int kBBytes = BN * kBK * 2;
+  static constexpr int kBBytes = kBN * kBK * 2;
   static constexpr int kStageBytes = S * (kABytes + kBBytes);
   static constexpr int kStages = (220 * 1024) / kStageBytes > 4 ? 4 : (220 * 1024) / kStageBytes;
-  static constexpr int kAccCols = S * BN;
+  static constexpr int kAccCols = S * kBN;
   static constexpr int kBufs = (2 * kAccCols <= 512) ? 2 : 1;
   static constexpr int kTmemCols = (kBufs * kAccCols <= 128) ? 128
                                    : (kBufs * kAccCols <= 256) ? 256 : 512;
   static constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+  // epilogue: four warps per TMEM lane quarter, each draining a quarter of the tile's columns
+  static constexpr int kEpiWarps = 16;
+  static constexpr int kEpiCols = kBN * 4 / kEpiWarps;
+  static constexpr int kThreads = 32 * (2 + kEpiWarps);
 };
+constexpr int kExactThreads = 576;  // Cfg<S>::kThreads (launch bound of the exact kernel)
 
 // Static schedule shared by the three roles: the host sorts output tiles by decreasing K and the
 // CTAs deal them out in snake order (b, 2G-1-b, 2G+b, ...), which balances ragged sectors.
@@ -492,13 +510,16 @@ __device__ __forceinline__ int64_t sched_pos(int64_t i, int G, int b) {
   return i * G + ((i & 1) ? (G - 1 - b) : b);
 }
 
+// 18 warps put 5 warps on one SM sub-partition (16K registers), which caps a thread at 96
+// registers; the epilogue drains TMEM in 16-column pieces to stay close to that
 template <int S>
-__global__ void __launch_bounds__(192, 1) split_gemm_kernel(
+__global__ void __launch_bounds__(kExactThreads, 1) split_gemm_kernel(
     const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
     const Problem* __restrict__ probs, const int4* __restrict__ tiles, int64_t ntiles,
     const int32_t* __restrict__ RA, const int32_t* __restrict__ CB, double* __restrict__ C,
     int* __restrict__ err) {
   using CF = Cfg<S>;
+  static_assert(CF::kThreads == kExactThreads, "launch bound and epilogue warp count disagree");
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* bars = (uint64_t*)(smem + CF::kStages * CF::kStageBytes);
@@ -518,7 +539,7 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], 128);
+      mbar_init(&tempty[b], 32 * CF::kEpiWarps);
     }
     mbar_init(drain, 1);
     *abort_flag = 0;
@@ -541,7 +562,7 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
         const int4 tr = tiles[pos];
         const int nks = probs[tr.x].nks;
         const int64_t baseA = (probs[tr.x].tA + (int64_t)tr.y * nks) * BM;
-        const int64_t baseB = (probs[tr.x].tB + (int64_t)tr.z * nks) * BN;
+        const int64_t baseB = (probs[tr.x].tB + (int64_t)tr.z * nks) * CF::kBN;
         for (int ks = 0; ks < nks * CF::kPerRow; ++ks) {
           if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) break;
           uint8_t* sA = smem + stage * CF::kStageBytes;
@@ -549,7 +570,7 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
           mbar_expect_tx(&full[stage], CF::kStageBytes);
           const int x = (ks % CF::kPerRow) * CF::kBK;
           const int rowA = (int)(baseA + (int64_t)(ks / CF::kPerRow) * BM);
-          const int rowB = (int)(baseB + (int64_t)(ks / CF::kPerRow) * BN);
+          const int rowB = (int)(baseB + (int64_t)(ks / CF::kPerRow) * CF::kBN);
 #pragma unroll
           for (int s = 0; s < S; ++s) tma_load_3d(sA + s * CF::kABytes, &tmA, &full[stage], x, rowA, s);
 #pragma unroll
@@ -564,7 +585,7 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      constexpr uint32_t idesc = make_idesc(BM, BN);
+      constexpr uint32_t idesc = make_idesc(BM, CF::kBN);
       int stage = 0;
       uint32_t phase = 0;
       int64_t use = 0;
@@ -590,7 +611,7 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
 #pragma unroll
               for (int qb = 0; qb < S - pa; ++qb) {
                 const int g = pa + qb;
-                const uint32_t dcol = tmem_base + (uint32_t)((buf * S + g) * BN);
+                const uint32_t dcol = tmem_base + (uint32_t)((buf * S + g) * CF::kBN);
                 const uint64_t ad = CF::kBK == 64 ? sw128_desc(sA + pa * CF::kABytes)
                                                   : sw64_desc(sA + pa * CF::kABytes);
                 const uint64_t bd = CF::kBK == 64 ? sw128_desc(sB + qb * CF::kBBytes)
@@ -620,8 +641,12 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
       }
     }
   } else {
-    // ---------------- epilogue: warps 2..5 ----------------
+    // ---------------- epilogue: warps 2..(2 + kEpiWarps - 1) ----------------
+    // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its lane quarter = 32 tile rows); the warps
+    // of one quarter split the tile's columns
+    constexpr int NC = CF::kEpiCols;
     const int lrow = 32 * (warp & 3) + lane;
+    const int col0 = ((warp - 2) >> 2) * NC;
     const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
     int64_t use = 0;
     for (int64_t i = 0;; ++i) {
@@ -630,9 +655,9 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
       const int4 tr = tiles[pos];
       const Problem P = probs[tr.x];
       const int64_t mi = tr.y, ni = tr.z;
-      float hi[BN], lo[BN];
+      float hi[NC], lo[NC];
 #pragma unroll
-      for (int j = 0; j < BN; ++j) {
+      for (int j = 0; j < NC; ++j) {
         hi[j] = 0.f;
         lo[j] = 0.f;
       }
@@ -645,14 +670,15 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
           break;
         }
         tc_fence_after();
+        static_assert(NC % 16 == 0, "epilogue column groups are multiples of 16");
 #pragma unroll
-        for (int h = 0; h < BN / 32; ++h) {
+        for (int h = 0; h < NC / 16; ++h) {  // 16-column pieces keep few registers live
 #pragma unroll
           for (int g = 0; g < S; ++g) {
-            uint32_t v[32];
-            tmem_ld32(tmem_base + lane_addr + (uint32_t)((buf * S + g) * BN + h * 32), v);
+            uint32_t v[16];
+            tmem_ld16(tmem_base + lane_addr + (uint32_t)((buf * S + g) * CF::kBN + col0 + h * 16), v);
 #pragma unroll
-            for (int j = 0; j < 32; ++j) two_sum_acc(hi[h * 32 + j], lo[h * 32 + j], __uint_as_float(v[j]));
+            for (int j = 0; j < 16; ++j) two_sum_acc(hi[h * 16 + j], lo[h * 16 + j], __uint_as_float(v[j]));
           }
         }
         tc_fence_before();
@@ -665,8 +691,8 @@ __global__ void __launch_bounds__(192, 1) split_gemm_kernel(
         const int Rr = RA[P.rA + row];
         double* Cp = C + P.offC + row;
 #pragma unroll
-        for (int j = 0; j < BN; ++j) {
-          const int64_t col = ni * BN + j;
+        for (int j = 0; j < NC; ++j) {
+          const int64_t col = ni * CF::kBN + col0 + j;
           if (col < P.N) {
             const int Cc = CB[P.rB + col];
             // a zero row or column (no exponent) contributes exact zeros
@@ -939,7 +965,7 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
     throw Error(kErrUnsupported, "split precision supports 2..7 slices");
   const char* ex = std::getenv("MPSG_SPLIT_EXACT");
   fast = S <= 3 && !(ex && ex[0] == '1');
-  bn = fast ? BNF : BN;
+  bn = fast ? BNF : exact_bn(S);
   chunk = fast ? (1 << 30) : chunk_for(S);
   seg = fast ? 256 : chunk;
   probs.clear();
@@ -1108,7 +1134,7 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
     split_gemm_fast_kernel<S <= 3 ? S : 3><<<grid, 192, FCF::kSmemBytes, ctx->stream>>>(
         sp.tmA, sp.tmB, sp.d_probs, sp.d_tiles, sp.ntiles, sp.d_RA, sp.d_CB, C, sp.d_err);
   } else {
-    split_gemm_kernel<S><<<grid, 192, CF::kSmemBytes, ctx->stream>>>(
+    split_gemm_kernel<S><<<grid, CF::kThreads, CF::kSmemBytes, ctx->stream>>>(
         sp.tmA, sp.tmB, sp.d_probs, sp.d_tiles, sp.ntiles, sp.d_RA, sp.d_CB, C, sp.d_err);
   }
   MPSG_CUDA(cudaGetLastError());

@@ -18,6 +18,10 @@ constexpr int kMaxSlices = 7;  // 49 bits: the FP64-class setting
 // the chunk is 2^24 / (2^12 max(4, S + 2)), rounded down to a multiple of 64 (one packed row).
 constexpr int exact_chunk(int S) { return ((4096 / (S + 2 > 4 ? S + 2 : 4)) / 64) * 64; }
 
+// N tile of the exact mode: S accumulators of exact_bn columns must fit the 512 TMEM columns;
+// 128-column MMAs halve the shared-memory operand traffic per MAC of 64-column ones.
+constexpr int exact_bn(int S) { return S <= 4 ? 128 : 64; }
+
 // One sector GEMM as the split kernels see it (column-major A: M x K, B: K x N, C: M x N).
 struct Problem {
   int64_t M, N, K;
