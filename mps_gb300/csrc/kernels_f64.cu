@@ -84,6 +84,68 @@ __global__ void __launch_bounds__(256) gemm_f64_grouped_kernel(
   }
 }
 
+// Thin sector GEMMs (the MPO steps and W folds: K and one of M, N at most kThin) are memory-
+// or DFMA-bound; padding them to 64 x 64 x 16 tiles wastes most of the FP64 pipe. One thread
+// computes one output row (N thin) or one output column (M thin); the thin operand is the same
+// for every thread of a task and reaches a warp as cache broadcasts.
+constexpr int kThin = 32;
+
+__device__ __forceinline__ int find_task(const int64_t* __restrict__ prefix, int n, int64_t u) {
+  int lo = 0, hi = n - 1;  // largest t with prefix[t] <= u
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(prefix + mid) <= u) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(256) gemm_f64_rows_kernel(
+    const GemmTask* __restrict__ tasks, const int64_t* __restrict__ prefix, int ntasks,
+    int64_t nunits, const double* __restrict__ A, const double* __restrict__ B,
+    double* __restrict__ C) {
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < nunits;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const int t = find_task(prefix, ntasks, u);
+    const GemmTask g = tasks[t];
+    const int64_t m = u - __ldg(prefix + t);
+    double a[kThin];
+#pragma unroll
+    for (int k = 0; k < kThin; ++k) a[k] = k < g.K ? __ldg(A + g.offA + m + k * g.lda) : 0.0;
+    for (int64_t j = 0; j < g.N; ++j) {
+      const double* b = B + g.offB + j * g.ldb;
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < kThin; ++k)
+        if (k < g.K) acc = fma(a[k], __ldg(b + k), acc);
+      C[g.offC + m + j * g.ldc] = acc;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) gemm_f64_cols_kernel(
+    const GemmTask* __restrict__ tasks, const int64_t* __restrict__ prefix, int ntasks,
+    int64_t nunits, const double* __restrict__ A, const double* __restrict__ B,
+    double* __restrict__ C) {
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < nunits;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const int t = find_task(prefix, ntasks, u);
+    const GemmTask g = tasks[t];
+    const int64_t j = u - __ldg(prefix + t);
+    double b[kThin];
+#pragma unroll
+    for (int k = 0; k < kThin; ++k) b[k] = k < g.K ? __ldg(B + g.offB + k + j * g.ldb) : 0.0;
+    for (int64_t m = 0; m < g.M; ++m) {
+      const double* a = A + g.offA + m;
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < kThin; ++k)
+        if (k < g.K) acc = fma(__ldg(a + k * g.lda), b[k], acc);
+      C[g.offC + m + j * g.ldc] = acc;
+    }
+  }
+}
+
 __global__ void fill_kernel(double* __restrict__ x, int64_t n, double v) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -144,34 +206,56 @@ int vec_grid(Context* ctx, int64_t n) {
 
 }  // namespace
 
-void DevGemmPlan::build_host(const std::vector<GemmTask>& g, double flops_,
-                             std::vector<int64_t>& prefix) {
+void DevGemmPlan::build_host(const std::vector<GemmTask>& g, double flops_, GemmTables& t) {
   host = g;
   flops = flops_;
-  n = (int)g.size();
-  prefix.assign(n + 1, 0);
-  for (int k = 0; k < n; ++k) {
-    int64_t tiles = ((g[k].M + BM - 1) / BM) * ((g[k].N + BN - 1) / BN);
-    prefix[k + 1] = prefix[k] + tiles;
+  t = GemmTables();
+  for (const GemmTask& x : g) {
+    if (x.K <= kThin && x.N <= kThin && x.M >= x.N) t.part[kRows].push_back(x);
+    else if (x.K <= kThin && x.M <= kThin) t.part[kCols].push_back(x);
+    else t.part[kTiled].push_back(x);
   }
-  ntiles = prefix[n];
+  for (int q = 0; q < 3; ++q) {
+    const auto& v = t.part[q];
+    auto& pre = t.prefix[q];
+    pre.assign(v.size() + 1, 0);
+    for (size_t k = 0; k < v.size(); ++k) {
+      int64_t units = q == kTiled ? ((v[k].M + BM - 1) / BM) * ((v[k].N + BN - 1) / BN)
+                      : q == kRows ? v[k].M : v[k].N;
+      pre[k + 1] = pre[k] + units;
+    }
+    count[q] = (int)v.size();
+    units[q] = pre.back();
+  }
+  n = count[kTiled];
+  ntiles = units[kTiled];
 }
 
 void DevGemmPlan::upload(const std::vector<GemmTask>& g, double flops_) {
   release();
-  std::vector<int64_t> prefix;
-  build_host(g, flops_, prefix);
-  if (n == 0) return;
-  MPSG_CUDA(cudaMalloc(&d_tasks, sizeof(GemmTask) * n));
-  MPSG_CUDA(cudaMalloc(&d_prefix, sizeof(int64_t) * (n + 1)));
-  MPSG_CUDA(cudaMemcpy(d_tasks, g.data(), sizeof(GemmTask) * n, cudaMemcpyHostToDevice));
-  MPSG_CUDA(cudaMemcpy(d_prefix, prefix.data(), sizeof(int64_t) * (n + 1),
-                       cudaMemcpyHostToDevice));
+  GemmTables t;
+  build_host(g, flops_, t);
+  for (int q = 0; q < 3; ++q) {
+    if (count[q] == 0) continue;
+    const size_t bt = sizeof(GemmTask) * count[q], bp = sizeof(int64_t) * (count[q] + 1);
+    MPSG_CUDA(cudaMalloc(&d_part[q], bt));
+    MPSG_CUDA(cudaMalloc(&d_part_prefix[q], bp));
+    MPSG_CUDA(cudaMemcpy(d_part[q], t.part[q].data(), bt, cudaMemcpyHostToDevice));
+    MPSG_CUDA(cudaMemcpy(d_part_prefix[q], t.prefix[q].data(), bp, cudaMemcpyHostToDevice));
+  }
+  d_tasks = d_part[kTiled];
+  d_prefix = d_part_prefix[kTiled];
 }
 
 void DevGemmPlan::release() {
-  if (d_tasks) cudaFree(d_tasks);
-  if (d_prefix) cudaFree(d_prefix);
+  for (int q = 0; q < 3; ++q) {
+    if (d_part[q]) cudaFree(d_part[q]);
+    if (d_part_prefix[q]) cudaFree(d_part_prefix[q]);
+    d_part[q] = nullptr;
+    d_part_prefix[q] = nullptr;
+    count[q] = 0;
+    units[q] = 0;
+  }
   d_tasks = nullptr;
   d_prefix = nullptr;
   n = 0;
@@ -180,13 +264,24 @@ void DevGemmPlan::release() {
 
 void launch_gemm_f64(Context* ctx, const DevGemmPlan& p, const double* A, const double* B,
                      double* C) {
-  if (p.ntiles == 0) return;
-  int64_t grid = std::min<int64_t>(p.ntiles, (int64_t)ctx->num_sms * 4);
+  if (p.units[kTiled] + p.units[kRows] + p.units[kCols] == 0) return;
   KernelTimer timer(ctx, kKindGemmF64, p.flops);
-  gemm_f64_grouped_kernel<<<(unsigned)grid, 256, 0, ctx->stream>>>(p.d_tasks, p.d_prefix, p.n,
-                                                                   p.ntiles, A, B, C);
-  MPSG_CUDA(cudaGetLastError());
-  ctx->kernel_launches++;
+  if (p.units[kTiled]) {
+    int64_t grid = std::min<int64_t>(p.units[kTiled], (int64_t)ctx->num_sms * 4);
+    gemm_f64_grouped_kernel<<<(unsigned)grid, 256, 0, ctx->stream>>>(
+        p.d_part[kTiled], p.d_part_prefix[kTiled], p.count[kTiled], p.units[kTiled], A, B, C);
+    MPSG_CUDA(cudaGetLastError());
+    ctx->kernel_launches++;
+  }
+  for (int q : {kRows, kCols}) {
+    if (!p.units[q]) continue;
+    int64_t grid = std::min<int64_t>((p.units[q] + 255) / 256, (int64_t)ctx->num_sms * 8);
+    auto kern = q == kRows ? gemm_f64_rows_kernel : gemm_f64_cols_kernel;
+    kern<<<(unsigned)grid, 256, 0, ctx->stream>>>(p.d_part[q], p.d_part_prefix[q], p.count[q],
+                                                  p.units[q], A, B, C);
+    MPSG_CUDA(cudaGetLastError());
+    ctx->kernel_launches++;
+  }
   ctx->gemm_flops += p.flops;
 }
 

@@ -120,20 +120,22 @@ extern "C" int mpsg_contract_noalloc(mpsg_ctx* ctx, const mpsg_tensor* a, const 
     stage_copy(fa, plan->fa.tasks, plan->fa.identity, img, cur, dev);
     stage_copy(fb, plan->fb.tasks, plan->fb.identity, img, cur, dev);
     stage_copy(split, plan->split.tasks, plan->split.identity, img, cur, dev);
-    std::vector<int64_t> gprefix;
-    mm.build_host(plan->mm.gemms, plan->mm.flops, gprefix);
-    if (mm.n > 0) {
-      const size_t bt = sizeof(GemmTask) * mm.n, bp = sizeof(int64_t) * gprefix.size();
+    GemmTables gt;
+    mm.build_host(plan->mm.gemms, plan->mm.flops, gt);
+    for (int q = 0; q < 3; ++q) {  // tiled, thin-N and thin-M task tables
+      if (mm.count[q] == 0) continue;
+      const size_t bt = sizeof(GemmTask) * mm.count[q], bp = sizeof(int64_t) * gt.prefix[q].size();
       const size_t o1 = cur, o2 = align256(o1 + bt);
       cur = align256(o2 + bp);
-      if (cur <= kScratchBytes) {
-        img.resize(cur);
-        std::memcpy(img.data() + o1, plan->mm.gemms.data(), bt);
-        std::memcpy(img.data() + o2, gprefix.data(), bp);
-        mm.d_tasks = (GemmTask*)(dev + o1);
-        mm.d_prefix = (int64_t*)(dev + o2);
-      }
+      if (cur > kScratchBytes) continue;  // reported by the size check below
+      img.resize(cur);
+      std::memcpy(img.data() + o1, gt.part[q].data(), bt);
+      std::memcpy(img.data() + o2, gt.prefix[q].data(), bp);
+      mm.d_part[q] = (GemmTask*)(dev + o1);
+      mm.d_part_prefix[q] = (int64_t*)(dev + o2);
     }
+    mm.d_tasks = mm.d_part[kTiled];
+    mm.d_prefix = mm.d_part_prefix[kTiled];
     const size_t tables = cur;
     auto take = [&](int64_t doubles) {
       const size_t o = cur;

@@ -62,18 +62,29 @@ struct DevCopyPlan {
 };
 size_t copy_aux_bytes();  // bytes of launch data per copy task
 
+// FP64 GEMM tasks split by shape: tiled (64 x 64 tiles), thin-N (one thread per output row) and
+// thin-M (one thread per output column), each with its work-unit prefix sums.
+enum GemmPart { kTiled = 0, kRows = 1, kCols = 2 };
+struct GemmTables {
+  std::vector<GemmTask> part[3];
+  std::vector<int64_t> prefix[3];
+};
+
 struct DevGemmPlan {
-  int n = 0;
+  int n = 0;          // tiled tasks
   int64_t ntiles = 0;
   double flops = 0;
-  GemmTask* d_tasks = nullptr;
-  int64_t* d_prefix = nullptr;
-  int64_t max_ld = 0;
+  GemmTask* d_tasks = nullptr;   // = d_part[kTiled]
+  int64_t* d_prefix = nullptr;   // = d_part_prefix[kTiled]
+  int count[3] = {0, 0, 0};      // tasks per part
+  int64_t units[3] = {0, 0, 0};  // work units per part (tiles, rows, columns)
+  GemmTask* d_part[3] = {nullptr, nullptr, nullptr};
+  int64_t* d_part_prefix[3] = {nullptr, nullptr, nullptr};
   std::vector<GemmTask> host;
   std::shared_ptr<split::SplitPlan> splitp[8];  // split-precision plans by slice count
   void upload(const std::vector<GemmTask>& g, double flops_);
-  // Host half of upload: every field except the device pointers, plus the tile prefix sums.
-  void build_host(const std::vector<GemmTask>& g, double flops_, std::vector<int64_t>& prefix);
+  // Host half of upload: every field except the device pointers, plus the per-part tables.
+  void build_host(const std::vector<GemmTask>& g, double flops_, GemmTables& t);
   void release();
 };
 
