@@ -1,16 +1,21 @@
 // Block-permute engine: executes a list of strided N-d copy tasks (permutelegs, fuselegs,
 // splitleg, SymMatrix fusion and the split+permute of contraction outputs are all such lists).
 //
-// Two tile shapes, chosen per task on the host:
-//   * rows : source and destination share their unit-stride axis a (or one side has none);
-//            the task is walked as rows along axis a: each warp decodes a row's multi-index once
-//            (magic-number division, no per-element div/mod) and its lanes stream the row, so
-//            reads and writes are coalesced along a;
-//   * tile : the unit-stride axes differ (a transpose); a 32x32 tile is staged in shared
-//            memory so that reads are coalesced along the source axis and writes along the
-//            destination axis.
-// The kernel is persistent: a grid sized to the SM count walks a global tile index and finds its
-// task by binary search in the per-task tile prefix sums.
+// Work is dealt out per warp (no block-wide barriers): a persistent grid walks a global unit
+// index, each warp finds its task by binary search in the per-task unit prefix sums and keeps
+// the task's extents, strides and division constants in a per-warp slot of shared memory.
+// One of three unit shapes is chosen per task on the host:
+//   * row    : source and destination share their unit-stride axis a and it holds at least 32
+//              elements; a unit is a group of rows along a, each row's multi-index is decoded
+//              once (magic-number division) and the lanes stream it, coalesced on both sides;
+//   * tile   : the unit-stride axes differ (a transpose) and both hold at least 16 elements; a
+//              unit is a 32 x 32 tile staged in the warp's shared-memory slot, read coalesced
+//              along the source axis and written coalesced along the destination axis;
+//   * gather : everything else (short runs, e.g. the MPO and physical legs of size 1..12); a
+//              unit is 256 consecutive destination positions in destination-stride order, one
+//              per lane and step, each decoded to its source address. Writes stay coalesced and
+//              reads follow the source's short runs through the caches.
+#include <algorithm>
 #include <cstring>
 
 #include "runtime.hpp"
@@ -19,126 +24,181 @@ namespace mpsg {
 
 namespace {
 
-constexpr int kRowTile = 2048;  // target elements per row-mode tile
-constexpr int kT = 32;
+constexpr int kWarps = 8;          // warps per CTA
+constexpr int kRowElems = 1024;    // target elements per row-mode unit
+constexpr int kGatherUnit = 256;   // destination positions per gather unit
+constexpr int kT = 32;             // transpose tile edge
 
-// Per-task launch data: axis roles, tiling and division constants (q = (umulhi(n,m)+n) >> s
-// equals n / ext for every n < 2^31).
+enum CopyMode { kModeRow = 0, kModeTile = 1, kModeGather = 2 };
+
+// Per-task launch data: mode, axis roles, tiling, gather order and division constants
+// (q = (umulhi(n,m)+n) >> s equals n / ext for every n < 2^31).
 struct TaskAux {
-  int32_t mode, a, b, rows_per_tile;
-  int64_t outer;                  // rows (row mode)
+  int32_t mode, a, b, rows_per_unit;
+  int64_t outer;  // row mode: rows; tile mode: tiles
+  int32_t order[kMaxTaskDims];  // gather mode: axes by ascending destination stride
   uint32_t mag[kMaxTaskDims];
   uint32_t shf[kMaxTaskDims];
 };
 
-struct TaskView {
-  int nd, a, b, mode, rpt;
-  int64_t outer;
+struct WarpView {
+  int task, nd, mode, a, b, rpu;
+  int64_t outer, soff, doff, first;
   int64_t ext[kMaxTaskDims], sstr[kMaxTaskDims], dstr[kMaxTaskDims];
   uint32_t mag[kMaxTaskDims], shf[kMaxTaskDims];
-  int64_t soff, doff, first_tile;
+  int32_t order[kMaxTaskDims];
 };
+
+typedef double TileBuf[kT][kT + 1];
 
 __device__ __forceinline__ uint32_t fdiv(uint32_t n, uint32_t m, uint32_t s) {
   return (__umulhi(n, m) + n) >> s;
 }
 
-__global__ void __launch_bounds__(256) copy_tasks_kernel(
+// Dynamic shared memory: kWarps task views, then (only for plans with tile-mode tasks) kWarps
+// transpose tiles; plans without tiles launch with the views alone. 64 registers per thread
+// keep 4 CTAs (32 warps) resident per SM.
+__global__ void __launch_bounds__(32 * kWarps, 4) copy_tasks_kernel(
     const CopyTask* __restrict__ tasks, const int64_t* __restrict__ prefix,
-    const TaskAux* __restrict__ aux, int ntasks, int64_t ntiles, const double* __restrict__ src,
+    const TaskAux* __restrict__ aux, int ntasks, int64_t nunits, const double* __restrict__ src,
     double* __restrict__ dst) {
-  __shared__ double tile[kT][kT + 1];
-  __shared__ TaskView tv;
-  __shared__ int cur_task;
-  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  const int warp = tid >> 5, lane = tid & 31;
-  if (tid == 0) cur_task = -1;
-  __syncthreads();
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    if (tid == 0) {
-      int lo = 0, hi = ntasks - 1;  // largest k with prefix[k] <= t
-      while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (prefix[mid] <= t) lo = mid;
-        else hi = mid - 1;
-      }
-      if (lo != cur_task) {
-        const CopyTask& T = tasks[lo];
-        const TaskAux& X = aux[lo];
-        tv.nd = T.nd;
-        for (int i = 0; i < T.nd; ++i) {
-          tv.ext[i] = T.ext[i];
-          tv.sstr[i] = T.sstr[i];
-          tv.dstr[i] = T.dstr[i];
-          tv.mag[i] = X.mag[i];
-          tv.shf[i] = X.shf[i];
-        }
-        tv.soff = T.soff;
-        tv.doff = T.doff;
-        tv.mode = X.mode;
-        tv.a = X.a;
-        tv.b = X.b;
-        tv.rpt = X.rows_per_tile;
-        tv.outer = X.outer;
-        tv.first_tile = prefix[lo];
-        cur_task = lo;
-      }
+  extern __shared__ __align__(16) unsigned char copy_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WarpView& v = reinterpret_cast<WarpView*>(copy_smem)[warp];
+  TileBuf& tile = reinterpret_cast<TileBuf*>(copy_smem + sizeof(WarpView) * kWarps)[warp];
+  if (lane == 0) v.task = -1;
+  __syncwarp();
+  const int64_t stride = (int64_t)gridDim.x * kWarps;
+  for (int64_t u = (int64_t)blockIdx.x * kWarps + warp; u < nunits; u += stride) {
+    int lo = 0, hi = ntasks - 1;  // largest k with prefix[k] <= u (same answer in every lane)
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(prefix + mid) <= u) lo = mid;
+      else hi = mid - 1;
     }
-    __syncthreads();
-    const int64_t lt = t - tv.first_tile;
-    const int nd = tv.nd;
-    if (tv.mode == 0) {
-      // row walk along axis a
-      const int a = tv.a;
-      const int64_t ea = tv.ext[a];
-      const int64_t sa = tv.sstr[a], da = tv.dstr[a];
-      const int64_t r0 = lt * tv.rpt;
-      const int64_t r1 = min(r0 + tv.rpt, tv.outer);
-      for (int64_t row = r0 + warp; row < r1; row += 8) {
+    if (lo != v.task) {
+      __syncwarp();
+      const CopyTask& T = tasks[lo];
+      const TaskAux& X = aux[lo];
+      const int nd = T.nd;
+      if (lane < nd) {
+        v.ext[lane] = T.ext[lane];
+        v.sstr[lane] = T.sstr[lane];
+        v.dstr[lane] = T.dstr[lane];
+        v.mag[lane] = X.mag[lane];
+        v.shf[lane] = X.shf[lane];
+        v.order[lane] = X.order[lane];
+      }
+      if (lane == 0) {
+        v.nd = nd;
+        v.mode = X.mode;
+        v.a = X.a;
+        v.b = X.b;
+        v.rpu = X.rows_per_unit;
+        v.outer = X.outer;
+        v.soff = T.soff;
+        v.doff = T.doff;
+        v.first = prefix[lo];
+        v.task = lo;
+      }
+      __syncwarp();
+    }
+    const int64_t lu = u - v.first;
+    const int nd = v.nd;
+    if (v.mode == kModeRow) {
+      const int a = v.a;
+      const int64_t ea = v.ext[a];
+      // rpu > 0: rows_per_unit whole rows; rpu < 0: each row is cut into -rpu chunks
+      int64_t r0, r1, c0 = 0, c1 = ea;
+      if (v.rpu > 0) {
+        r0 = lu * v.rpu;
+        r1 = min(r0 + v.rpu, v.outer);
+      } else {
+        r0 = lu / (-v.rpu);
+        r1 = r0 + 1;
+        c0 = (lu - r0 * (-v.rpu)) * kRowElems;
+        c1 = min(c0 + kRowElems, ea);
+      }
+      for (int64_t row = r0; row < r1; ++row) {
         uint32_t q = (uint32_t)row;
-        int64_t so = tv.soff, dof = tv.doff;
+        int64_t so = v.soff, dof = v.doff;
         for (int i = 0; i < nd; ++i) {
           if (i == a) continue;
-          const uint32_t qi = fdiv(q, tv.mag[i], tv.shf[i]);
-          const int64_t ii = (int64_t)(q - qi * (uint32_t)tv.ext[i]);
+          const uint32_t qi = fdiv(q, v.mag[i], v.shf[i]);
+          const int64_t ii = (int64_t)(q - qi * (uint32_t)v.ext[i]);
           q = qi;
-          so += ii * tv.sstr[i];
-          dof += ii * tv.dstr[i];
+          so += ii * v.sstr[i];
+          dof += ii * v.dstr[i];
         }
-        for (int64_t ia = lane; ia < ea; ia += 32) dst[dof + ia * da] = __ldg(src + so + ia * sa);
+        // four loads in flight per lane before the stores
+        for (int64_t ia = c0 + lane; ia < c1; ia += 128) {
+          double x[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (ia + 32 * k < c1) x[k] = __ldg(src + so + ia + 32 * k);
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (ia + 32 * k < c1) dst[dof + ia + 32 * k] = x[k];
+        }
       }
-    } else {
-      const int a = tv.a, b = tv.b;
-      const int64_t ea = tv.ext[a], eb = tv.ext[b];
+    } else if (v.mode == kModeTile) {
+      const int a = v.a, b = v.b;
+      const int64_t ea = v.ext[a], eb = v.ext[b];
       const int64_t ta = (ea + kT - 1) / kT, tb = (eb + kT - 1) / kT;
-      int64_t q = lt;
+      int64_t q = lu;
       const int64_t ia = q % ta;
       q /= ta;
       const int64_t ib = q % tb;
       q /= tb;
-      int64_t so = tv.soff, dof = tv.doff;
+      int64_t so = v.soff, dof = v.doff;
       uint32_t q32 = (uint32_t)q;
       for (int i = 0; i < nd; ++i) {
         if (i == a || i == b) continue;
-        const uint32_t qi = fdiv(q32, tv.mag[i], tv.shf[i]);
-        const int64_t ii = (int64_t)(q32 - qi * (uint32_t)tv.ext[i]);
+        const uint32_t qi = fdiv(q32, v.mag[i], v.shf[i]);
+        const int64_t ii = (int64_t)(q32 - qi * (uint32_t)v.ext[i]);
         q32 = qi;
-        so += ii * tv.sstr[i];
-        dof += ii * tv.dstr[i];
+        so += ii * v.sstr[i];
+        dof += ii * v.dstr[i];
       }
       const int64_t a0 = ia * kT, b0 = ib * kT;
-      const int tx = threadIdx.x, ty = threadIdx.y;
-      for (int j = ty; j < kT; j += 8) {
-        if (a0 + j < ea && b0 + tx < eb)
-          tile[j][tx] = __ldg(src + so + (a0 + j) * tv.sstr[a] + (b0 + tx) * tv.sstr[b]);
+      const int64_t sa = v.sstr[a], db = v.dstr[b];
+#pragma unroll 8
+      for (int r = 0; r < kT; ++r)  // rows along a, lanes along b (source-contiguous)
+        if (a0 + r < ea && b0 + lane < eb) tile[r][lane] = __ldg(src + so + (a0 + r) * sa + b0 + lane);
+      __syncwarp();
+#pragma unroll 8
+      for (int c = 0; c < kT; ++c)  // columns along b, lanes along a (destination-contiguous)
+        if (a0 + lane < ea && b0 + c < eb) dst[dof + a0 + lane + (b0 + c) * db] = tile[lane][c];
+      __syncwarp();
+    } else {
+      // decode all of this lane's positions first, then issue every load, then every store
+      constexpr int kPer = kGatherUnit / 32;
+      const int64_t n = v.outer;
+      const int64_t p0 = lu * kGatherUnit;
+      int64_t so[kPer], dof[kPer];
+#pragma unroll
+      for (int k = 0; k < kPer; ++k) {
+        const int64_t p = p0 + k * 32 + lane;
+        uint32_t q = (uint32_t)(p < n ? p : 0);
+        so[k] = v.soff;
+        dof[k] = p < n ? v.doff : -1;
+        for (int j = 0; j < nd; ++j) {
+          const int i = v.order[j];
+          const uint32_t qi = fdiv(q, v.mag[i], v.shf[i]);
+          const int64_t ii = (int64_t)(q - qi * (uint32_t)v.ext[i]);
+          q = qi;
+          so[k] += ii * v.sstr[i];
+          if (dof[k] >= 0) dof[k] += ii * v.dstr[i];
+        }
       }
-      __syncthreads();
-      for (int j = ty; j < kT; j += 8) {
-        if (a0 + tx < ea && b0 + j < eb)
-          dst[dof + (a0 + tx) * tv.dstr[a] + (b0 + j) * tv.dstr[b]] = tile[tx][j];
-      }
+      double x[kPer];
+#pragma unroll
+      for (int k = 0; k < kPer; ++k)
+        if (dof[k] >= 0) x[k] = __ldg(src + so[k]);
+#pragma unroll
+      for (int k = 0; k < kPer; ++k)
+        if (dof[k] >= 0) dst[dof[k]] = x[k];
     }
-    __syncthreads();
   }
 }
 
@@ -148,6 +208,9 @@ void magic_u31(uint32_t d, uint32_t& m, uint32_t& s) {
   m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << l) - d)) / d + 1);
   s = l;
 }
+
+constexpr size_t kViewSmem = sizeof(WarpView) * kWarps;
+constexpr size_t kTileSmem = kViewSmem + sizeof(TileBuf) * kWarps;
 
 }  // namespace
 
@@ -171,12 +234,15 @@ void DevCopyPlan::upload(const std::vector<CopyTask>& tasks, bool identity_) {
 void DevCopyPlan::build_host(const std::vector<CopyTask>& tasks, bool identity_,
                              std::vector<int64_t>& prefix, std::vector<unsigned char>& aux_bytes) {
   identity = identity_;
+  has_tile = false;
   ntasks = (int)tasks.size();
   prefix.assign(ntasks + 1, 0);
   std::vector<TaskAux> aux(ntasks);
   elems = 0;
   for (int k = 0; k < ntasks; ++k) {
     const CopyTask& T = tasks[k];
+    TaskAux& X = aux[k];
+    std::memset(&X, 0, sizeof(X));
     int a = 0, b = 0;
     for (int i = 1; i < T.nd; ++i) {
       if (T.dstr[i] < T.dstr[a]) a = i;
@@ -185,24 +251,38 @@ void DevCopyPlan::build_host(const std::vector<CopyTask>& tasks, bool identity_,
     const int64_t n = T.numel();
     if (n >= ((int64_t)1 << 31)) throw Error(kErrUnsupported, "copy task above 2^31 elements");
     elems += n;
-    TaskAux& X = aux[k];
     for (int i = 0; i < T.nd; ++i) magic_u31((uint32_t)T.ext[i], X.mag[i], X.shf[i]);
-    int64_t tiles;
-    if (a == b || T.nd == 1 || T.sstr[b] != 1 || T.dstr[a] != 1) {
-      X.mode = 0;
+    const bool unit_a = T.dstr[a] == 1, unit_b = T.sstr[b] == 1;
+    int64_t units;
+    if (a == b && unit_a && unit_b && T.ext[a] >= 32) {
+      X.mode = kModeRow;
       X.outer = n / T.ext[a];
-      X.rows_per_tile = (int)std::max<int64_t>(1, std::min<int64_t>(X.outer, kRowTile / T.ext[a]));
-      tiles = (X.outer + X.rows_per_tile - 1) / X.rows_per_tile;
+      if (T.ext[a] > kRowElems) {  // long rows: several warps share a row
+        const int64_t cpr = (T.ext[a] + kRowElems - 1) / kRowElems;
+        X.rows_per_unit = -(int32_t)cpr;
+        units = X.outer * cpr;
+      } else {
+        X.rows_per_unit =
+            (int)std::max<int64_t>(1, std::min<int64_t>(X.outer, kRowElems / T.ext[a]));
+        units = (X.outer + X.rows_per_unit - 1) / X.rows_per_unit;
+      }
+    } else if (a != b && unit_a && unit_b && T.ext[a] >= 16 && T.ext[b] >= 16) {
+      X.mode = kModeTile;
+      has_tile = true;
+      const int64_t rest = n / (T.ext[a] * T.ext[b]);
+      X.outer = ((T.ext[a] + kT - 1) / kT) * ((T.ext[b] + kT - 1) / kT) * rest;
+      units = X.outer;
     } else {
-      X.mode = 1;
-      X.outer = 0;
-      X.rows_per_tile = 0;
-      int64_t rest = n / (T.ext[a] * T.ext[b]);
-      tiles = ((T.ext[a] + kT - 1) / kT) * ((T.ext[b] + kT - 1) / kT) * rest;
+      X.mode = kModeGather;
+      X.outer = n;
+      for (int i = 0; i < T.nd; ++i) X.order[i] = i;
+      std::stable_sort(X.order, X.order + T.nd,
+                       [&](int x, int y) { return T.dstr[x] < T.dstr[y]; });
+      units = (n + kGatherUnit - 1) / kGatherUnit;
     }
     X.a = a;
     X.b = b;
-    prefix[k + 1] = prefix[k] + tiles;
+    prefix[k + 1] = prefix[k] + units;
   }
   ntiles = prefix[ntasks];
   aux_bytes.resize(sizeof(TaskAux) * ntasks);
@@ -228,9 +308,17 @@ void launch_copy(Context* ctx, const DevCopyPlan& p, const double* src, double* 
                                 ctx->stream));
     return;
   }
-  int64_t grid = std::min<int64_t>(p.ntiles, (int64_t)ctx->num_sms * 8);
+  static bool attr = false;  // per process: the attribute belongs to the kernel, not a device
+  if (!attr) {
+    MPSG_CUDA(cudaFuncSetAttribute(copy_tasks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kTileSmem));
+    attr = true;
+  }
+  const size_t smem = p.has_tile ? kTileSmem : kViewSmem;
+  const int64_t ctas = (p.ntiles + kWarps - 1) / kWarps;
+  const int64_t grid = std::min<int64_t>(ctas, (int64_t)ctx->num_sms * (p.has_tile ? 3 : 8));
   KernelTimer timer(ctx, kKindCopy);
-  copy_tasks_kernel<<<(unsigned)grid, dim3(32, 8), 0, ctx->stream>>>(
+  copy_tasks_kernel<<<(unsigned)grid, 32 * kWarps, smem, ctx->stream>>>(
       p.d_tasks, p.d_prefix, (const TaskAux*)p.d_aux, p.ntasks, p.ntiles, src, dst);
   MPSG_CUDA(cudaGetLastError());
   ctx->kernel_launches++;

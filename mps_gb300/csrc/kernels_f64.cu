@@ -100,6 +100,60 @@ __device__ __forceinline__ int find_task(const int64_t* __restrict__ prefix, int
   return lo;
 }
 
+// Bodies with the contraction length as a template parameter: exactly K FMAs per output (an
+// unrolled loop to kThin with a k < K guard would make the compiler issue all kThin of them, and
+// FP64 issue rate is what bounds these kernels).
+template <int K>
+__device__ __forceinline__ void thin_row(const GemmTask& g, int64_t m, const double* __restrict__ A,
+                                         const double* __restrict__ B, double* __restrict__ C) {
+  double a[K > 0 ? K : 1];
+#pragma unroll
+  for (int k = 0; k < K; ++k) a[k] = __ldg(A + g.offA + m + k * g.lda);
+  for (int64_t j = 0; j < g.N; ++j) {
+    const double* b = B + g.offB + j * g.ldb;
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc = fma(a[k], __ldg(b + k), acc);
+    C[g.offC + m + j * g.ldc] = acc;
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void thin_col(const GemmTask& g, int64_t j, const double* __restrict__ A,
+                                         const double* __restrict__ B, double* __restrict__ C) {
+  double b[K > 0 ? K : 1];
+#pragma unroll
+  for (int k = 0; k < K; ++k) b[k] = __ldg(B + g.offB + k + j * g.ldb);
+  for (int64_t m = 0; m < g.M; ++m) {
+    const double* a = A + g.offA + m;
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc = fma(__ldg(a + k * g.lda), b[k], acc);
+    C[g.offC + m + j * g.ldc] = acc;
+  }
+}
+
+#define MPSG_THIN_CASES(F, g, i, A, B, C)                                                      \
+  switch ((int)(g).K) {                                                                        \
+    case 0: F<0>(g, i, A, B, C); break;   case 1: F<1>(g, i, A, B, C); break;                 \
+    case 2: F<2>(g, i, A, B, C); break;   case 3: F<3>(g, i, A, B, C); break;                 \
+    case 4: F<4>(g, i, A, B, C); break;   case 5: F<5>(g, i, A, B, C); break;                 \
+    case 6: F<6>(g, i, A, B, C); break;   case 7: F<7>(g, i, A, B, C); break;                 \
+    case 8: F<8>(g, i, A, B, C); break;   case 9: F<9>(g, i, A, B, C); break;                 \
+    case 10: F<10>(g, i, A, B, C); break; case 11: F<11>(g, i, A, B, C); break;               \
+    case 12: F<12>(g, i, A, B, C); break; case 13: F<13>(g, i, A, B, C); break;               \
+    case 14: F<14>(g, i, A, B, C); break; case 15: F<15>(g, i, A, B, C); break;               \
+    case 16: F<16>(g, i, A, B, C); break; case 17: F<17>(g, i, A, B, C); break;               \
+    case 18: F<18>(g, i, A, B, C); break; case 19: F<19>(g, i, A, B, C); break;               \
+    case 20: F<20>(g, i, A, B, C); break; case 21: F<21>(g, i, A, B, C); break;               \
+    case 22: F<22>(g, i, A, B, C); break; case 23: F<23>(g, i, A, B, C); break;               \
+    case 24: F<24>(g, i, A, B, C); break; case 25: F<25>(g, i, A, B, C); break;               \
+    case 26: F<26>(g, i, A, B, C); break; case 27: F<27>(g, i, A, B, C); break;               \
+    case 28: F<28>(g, i, A, B, C); break; case 29: F<29>(g, i, A, B, C); break;               \
+    case 30: F<30>(g, i, A, B, C); break; case 31: F<31>(g, i, A, B, C); break;               \
+    default: F<32>(g, i, A, B, C); break;                                                      \
+  }
+
 __global__ void __launch_bounds__(256) gemm_f64_rows_kernel(
     const GemmTask* __restrict__ tasks, const int64_t* __restrict__ prefix, int ntasks,
     int64_t nunits, const double* __restrict__ A, const double* __restrict__ B,
@@ -109,17 +163,7 @@ __global__ void __launch_bounds__(256) gemm_f64_rows_kernel(
     const int t = find_task(prefix, ntasks, u);
     const GemmTask g = tasks[t];
     const int64_t m = u - __ldg(prefix + t);
-    double a[kThin];
-#pragma unroll
-    for (int k = 0; k < kThin; ++k) a[k] = k < g.K ? __ldg(A + g.offA + m + k * g.lda) : 0.0;
-    for (int64_t j = 0; j < g.N; ++j) {
-      const double* b = B + g.offB + j * g.ldb;
-      double acc = 0.0;
-#pragma unroll
-      for (int k = 0; k < kThin; ++k)
-        if (k < g.K) acc = fma(a[k], __ldg(b + k), acc);
-      C[g.offC + m + j * g.ldc] = acc;
-    }
+    MPSG_THIN_CASES(thin_row, g, m, A, B, C)
   }
 }
 
@@ -132,17 +176,7 @@ __global__ void __launch_bounds__(256) gemm_f64_cols_kernel(
     const int t = find_task(prefix, ntasks, u);
     const GemmTask g = tasks[t];
     const int64_t j = u - __ldg(prefix + t);
-    double b[kThin];
-#pragma unroll
-    for (int k = 0; k < kThin; ++k) b[k] = k < g.K ? __ldg(B + g.offB + k + j * g.ldb) : 0.0;
-    for (int64_t m = 0; m < g.M; ++m) {
-      const double* a = A + g.offA + m;
-      double acc = 0.0;
-#pragma unroll
-      for (int k = 0; k < kThin; ++k)
-        if (k < g.K) acc = fma(__ldg(a + k * g.lda), b[k], acc);
-      C[g.offC + m + j * g.ldc] = acc;
-    }
+    MPSG_THIN_CASES(thin_col, g, j, A, B, C)
   }
 }
 

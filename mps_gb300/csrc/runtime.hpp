@@ -50,6 +50,7 @@ struct DevCopyPlan {
   int64_t ntiles = 0;
   int64_t elems = 0;
   bool identity = false;
+  bool has_tile = false;         // some task is a transpose staged through shared memory
   CopyTask* d_tasks = nullptr;
   int64_t* d_prefix = nullptr;   // ntasks+1 tile prefix
   void* d_aux = nullptr;         // per task: tile shape, axis roles, division constants
