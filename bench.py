@@ -51,6 +51,9 @@ def parse():
                    help="0 = FP64; s >= 2 = split bf16 with s slices (default: best available)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-sweep", action="store_true", help="skip the DMRG sweep measurement")
+    p.add_argument("--gradient", action="store_true",
+                   help="instead of the H_eff line: energy gradients of a converged L=64, "
+                        "chi=512 XXZ chain (dE/dDelta and dE/dA by adjoint contractions)")
     p.add_argument("--sweep-chi", type=int, default=None, help="maxdim of the sweep (default chi)")
     return p.parse_args()
 
@@ -421,9 +424,60 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_gradient(args):
+    """Energy gradients by adjoint contractions on a DMRG-converged XXZ chain (L=64, Delta=0.5,
+    maxdim 512): dE/dDelta (Hellmann-Feynman through the MPO cotangents) and dE/dA for every
+    site tensor, from one forward and one backward sweep of FP64 contractions. Checked against
+    central differences (h = 1e-5) of <psi|H(Delta)|psi> for the same state, and the gradient at
+    the orthogonality center against 2 E A (stationarity)."""
+    import numpy as np
+    import mps_gb300 as mg
+    from mps_gb300 import dmrg as gd
+    from mps_gb300 import grad as gr
+    lx, chi, delta = 64, 512, 0.5
+    ctx = mg.get_context(0)
+    Ws = gd.xxz_u1mpo(lx, delta, ctx=ctx)
+    mps = gd.mps_from_host(gd.binomial_mps_host(lx, lx // 2, chi, 11), ctx)
+    gd.center_at(mps, 1, svd="gram")
+    env = gd.initialenv(mps, Ws)
+    t0 = time.perf_counter()
+    es = []
+    for _ in range(4):
+        es = gd.dmrg2sitesweep(mps, Ws, env, maxdim=chi, tol=1e-10, lanczostol=1e-9, krylovdim=4,
+                               krylovmaxiter=8, precision=4, energy_precision=7,
+                               env_precision=7, svd="gram")
+    ctx.synchronize()
+    t_dmrg = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    E, g = gr.energy_gradients(mps.As, Ws)
+    dEd = gr.xxz_delta_derivative(g, Ws, lx)
+    grads = [g(A) for A in mps.As]
+    ctx.synchronize()
+    t_grad = time.perf_counter() - t0
+    h = 1e-5
+    ep = gr.energy_gradients(mps.As, gd.xxz_u1mpo(lx, delta + h, ctx=ctx))[0]
+    em = gr.energy_gradients(mps.As, gd.xxz_u1mpo(lx, delta - h, ctx=ctx))[0]
+    fd = (ep - em) / (2 * h)
+    A1 = mps.As[0].to_flat()
+    stat = float(np.linalg.norm(grads[0].to_flat() - 2 * E * A1) / np.linalg.norm(2 * E * A1))
+    line = {
+        "metric": "energy gradient s (dE/dDelta + dE/dA, adjoint contractions)",
+        "value": t_grad, "unit": "s", "higher_is_better": False, "n_gpus": 1,
+        "data": "synthetic (seeded Philox N(0,1) initial MPS)",
+        "config": {"workload": f"XXZ chain L={lx}, Delta={delta}, maxdim {chi}, converged by 4 "
+                               "mixed 2-site sweeps (Krylov 4 slices, energy/env 7 slices)",
+                   "dtype": "f64"},
+        "energy": E, "dE_dDelta": dEd, "dE_dDelta_fd": fd, "fd_abs_diff": abs(dEd - fd),
+        "center_stationarity_relerr": stat, "dmrg_s": t_dmrg, "last_sweep_energy": es[-1],
+    }
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.gradient:
+        run_gradient(a)
     else:
         run_ours(a)

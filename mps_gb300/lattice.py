@@ -1,0 +1,181 @@
+"""U(1) MPOs of spin-1/2 Hamiltonians on lattices (the role of ``_generatempo_sym``,
+src/mpogen.jl:153-352), built on the host as sector blocks.
+
+A Hamiltonian is a list of terms, each a product of single-site operators (S+, S-, Sz, with
+U(1) charges +1, -1, 0 on the site space (0 => down, 1 => up)) on increasing sites with an
+amplitude. The MPO is a finite-state machine on the bond: a "done" channel (charge 0, all terms
+finished), a "start" channel (charge 0, nothing placed yet) and one channel per term that has
+started and not finished, carrying the charge of the operators placed so far. At each site a
+term starts (start -> its channel), passes (identity), continues (operator, channel -> channel)
+or finishes (operator, channel -> done); single-site terms go from start to done. The bond
+dimension is 2 + the number of terms crossing the bond, as in the reference (one channel per
+open term, no compression). Channels are ordered by charge, and within a charge: done first,
+open terms in the order they started, start last.
+
+``cylinder_heisenberg_terms`` gives the J1 Heisenberg model on a W x L cylinder (periodic
+around the circumference, open along the length) with the column-major site order of the
+reference (y fastest, src/model3.jl:86-87): bond dimension 2 + 3 W.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+SZ = np.diag([-0.5, 0.5])             # basis (down, up) = charges (0, 1)
+SP = np.array([[0.0, 0.0], [1.0, 0.0]])  # down -> up, charge +1
+SM = SP.T.copy()                      # charge -1
+EYE = np.eye(2)
+OPS = {"Z": (SZ, 0), "P": (SP, 1), "M": (SM, -1), "I": (EYE, 0)}
+
+
+def heisenberg_bond_terms(i, j, J=1.0, delta=1.0):
+    """J (S+_i S-_j / 2 + S-_i S+_j / 2 + delta Sz_i Sz_j) with i < j."""
+    if i > j:
+        i, j = j, i
+    return [((i, j), ("P", "M"), 0.5 * J), ((i, j), ("M", "P"), 0.5 * J),
+            ((i, j), ("Z", "Z"), J * delta)]
+
+
+def cylinder_heisenberg_terms(width, length, J=1.0):
+    """J1 Heisenberg terms on a width x length cylinder, sites numbered x*width + y (0-based)."""
+    site = lambda x, y: x * width + y
+    terms = []
+    for x in range(length):
+        for y in range(width):
+            if width > 2 or y + 1 < width:  # around the circumference (a 2-wide ring is one bond)
+                terms += heisenberg_bond_terms(site(x, y), site(x, (y + 1) % width), J)
+            if x + 1 < length:
+                terms += heisenberg_bond_terms(site(x, y), site(x + 1, y), J)
+    return terms
+
+
+def chain_xxz_terms(lx, delta):
+    terms = []
+    for i in range(lx - 1):
+        terms += heisenberg_bond_terms(i, i + 1, 1.0, delta)
+    return terms
+
+
+def mpo_blocks(n_sites, terms):
+    """Per site: (space, {sector: block}) of the MPO tensor W(Vl, d, dual(Vr), dual(d)).
+    Spaces are (charges, dims, isdual) triples per leg, usable with VectorSpace."""
+    terms = sorted(((tuple(s), tuple(o), float(a)) for s, o, a in terms), key=lambda t: t[0])
+    for s, o, _ in terms:
+        if len(s) != len(o) or list(s) != sorted(s) or len(set(s)) != len(s):
+            raise ValueError(f"term sites must increase: {s}")
+        if s[-1] >= n_sites:
+            raise ValueError(f"term beyond the lattice: {s}")
+    open_terms = []  # (term index, next op position, accumulated charge), in start order
+    out = []
+    ti = 0
+    for n in range(n_sites):
+        # left channels: [(charge, name)]: done, open terms, start
+        left = []
+        if n > 0:
+            left.append((0, "done"))
+            left += [(c, ("t", k)) for (k, p, c) in open_terms]
+        left.append((0, "start"))
+        trans = []  # (left name, right name, op, amplitude)
+        new_open = []
+        if n > 0:
+            trans.append(("done", "done", "I", 1.0))
+        for (k, p, c) in open_terms:
+            s, o, a = terms[k]
+            if s[p] == n:
+                if p == len(s) - 1:
+                    trans.append((("t", k), "done", o[p], a))
+                else:
+                    trans.append((("t", k), ("t", k), o[p], 1.0))
+                    new_open.append((k, p + 1, c + OPS[o[p]][1]))
+            else:
+                trans.append((("t", k), ("t", k), "I", 1.0))
+                new_open.append((k, p, c))
+        while ti < len(terms) and terms[ti][0][0] == n:
+            s, o, a = terms[ti]
+            if len(s) == 1:
+                trans.append(("start", "done", o[0], a))
+            else:
+                trans.append(("start", ("t", ti), o[0], 1.0))
+                new_open.append((ti, 1, OPS[o[0]][1]))
+            ti += 1
+        if n < n_sites - 1:
+            trans.append(("start", "start", "I", 1.0))
+        open_terms = new_open
+        right = [(0, "done")] + [(c, ("t", k)) for (k, p, c) in open_terms]
+        if n < n_sites - 1:
+            right.append((0, "start"))
+        else:
+            if open_terms:
+                raise ValueError("terms still open at the last site")
+            right = [(0, "done")]
+        if n == 0:
+            left = [(0, "start")]
+        out.append(_site_tensor(left, right, trans))
+    return out
+
+
+def _index(channels):
+    """charge -> ordered names, and name -> (charge, position within the charge)."""
+    by = {}
+    for c, name in channels:
+        by.setdefault(c, []).append(name)
+    pos = {name: (c, by[c].index(name)) for c, names in by.items() for name in names}
+    return by, pos
+
+
+def _site_tensor(left, right, trans):
+    lby, lpos = _index(left)
+    rby, rpos = _index(right)
+    Vl = (sorted(lby), [len(lby[c]) for c in sorted(lby)], False)
+    Vr = (sorted(rby), [len(rby[c]) for c in sorted(rby)], True)
+    d = ([0, 1], [1, 1], False)
+    dd = ([0, 1], [1, 1], True)
+    blocks = {}
+    for ln, rn, opname, amp in trans:
+        op, q = OPS[opname]
+        cl, il = lpos[ln]
+        cr, ir = rpos[rn]
+        if cr != cl + q:
+            raise ValueError("channel charge does not follow the operator charge")
+        for s in (0, 1):
+            for sp in (0, 1):
+                v = op[s, sp]
+                if v == 0.0:
+                    continue
+                sec = (cl, s, cr, sp)
+                if sec not in blocks:
+                    blocks[sec] = np.zeros((len(lby[cl]), 1, len(rby[cr]), 1))
+                blocks[sec][il, 0, ir, 0] += amp * v
+    return (Vl, d, Vr, dd), blocks
+
+
+def device_mpo(n_sites, terms, ctx=None, meta_only=False):
+    """The MPO of ``terms`` as library tensors W(Vl, d, dual(Vr), dual(d)) (zero blocks for the
+    allowed sectors no term touches)."""
+    from . import symtensors as mg
+    from .dmrg import _tensor_from_partial_blocks
+    out = []
+    for legs, blocks in mpo_blocks(n_sites, terms):
+        sp = tuple(mg.VectorSpace(list(zip(c, dims)), isd) for c, dims, isd in legs)
+        out.append(_tensor_from_partial_blocks(sp, blocks, ctx=ctx, meta_only=meta_only))
+    return out
+
+
+def dense_mpo(site_tensors):
+    """The full 2^n x 2^n matrix of an MPO given as mpo_blocks output (host check, small n).
+    Basis index bits: site 0 is the most significant, 1 = up."""
+    mats = []
+    for (Vl, _, Vr, _), blocks in site_tensors:
+        lo = {c: o for c, o in zip(Vl[0], np.cumsum([0] + Vl[1][:-1]))}
+        ro = {c: o for c, o in zip(Vr[0], np.cumsum([0] + Vr[1][:-1]))}
+        W = np.zeros((sum(Vl[1]), 2, sum(Vr[1]), 2))
+        for (cl, s, cr, sp), b in blocks.items():
+            W[lo[cl]:lo[cl] + b.shape[0], s, ro[cr]:ro[cr] + b.shape[2], sp] = b[:, 0, :, 0]
+        mats.append(W)
+    # contract: T[a, s..., b, s'...]; basis up = index 1 in the site space
+    T = mats[0][0]  # (s, b, s')
+    H = np.einsum("sbt->bst", T)  # (b, s, s')
+    for W in mats[1:]:
+        H = np.einsum("bIJ,bscp->cIsJp", H, W)
+        nb = H.shape[0]
+        H = H.reshape(nb, H.shape[1] * 2, H.shape[3] * 2)
+    return H[0]
