@@ -54,6 +54,10 @@ def parse():
     p.add_argument("--gradient", action="store_true",
                    help="instead of the H_eff line: energy gradients of a converged L=64, "
                         "chi=512 XXZ chain (dE/dDelta and dE/dA by adjoint contractions)")
+    p.add_argument("--cylinder", action="store_true",
+                   help="instead of the H_eff line: mixed-precision 2-site DMRG sweeps of the "
+                        "J1 Heisenberg 6 x 24 cylinder at maxdim --sweep-chi (default 1024)")
+    p.add_argument("--sweeps", type=int, default=2, help="sweeps of the --cylinder run")
     p.add_argument("--sweep-chi", type=int, default=None, help="maxdim of the sweep (default chi)")
     return p.parse_args()
 
@@ -473,11 +477,55 @@ def run_gradient(args):
     print(json.dumps(line), flush=True)
 
 
+def run_cylinder(args):
+    """2-site DMRG on the J1 Heisenberg cylinder (width 6, length 24, periodic around the
+    circumference, column-major sites; MPO from the lattice generator, 20-26 channels) at
+    maxdim chi from a random binomial-profile MPS: wall time of each mixed sweep (Krylov 4
+    slices, energy/environments 7 slices, density-matrix truncation) and the energies."""
+    import mps_gb300 as mg
+    from mps_gb300 import dmrg as gd
+    from mps_gb300 import lattice as lt
+    width, length = 6, 24
+    n = width * length
+    chi = args.sweep_chi or 1024
+    ctx = mg.get_context(0)
+    Ws = lt.device_mpo(n, lt.cylinder_heisenberg_terms(width, length), ctx=ctx)
+    mps = gd.mps_from_host(gd.binomial_mps_host(n, n // 2, chi, 13), ctx)
+    t0 = time.perf_counter()
+    gd.center_at(mps, 1, svd="gram")
+    env = gd.initialenv(mps, Ws)
+    ctx.synchronize()
+    t_init = time.perf_counter() - t0
+    times, energies, matvecs = [], [], []
+    for _ in range(args.sweeps):
+        stats = []
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        es = gd.dmrg2sitesweep(mps, Ws, env, maxdim=chi, tol=1e-10, lanczostol=1e-7,
+                               krylovdim=4, krylovmaxiter=8, stats=stats, **SWEEP_MIXED)
+        ctx.synchronize()
+        times.append(time.perf_counter() - t0)
+        energies.append(es[-1])
+        matvecs.append(sum(i.numops for i in stats))
+    line = {
+        "metric": "DMRG sweep s, J1 Heisenberg 6x24 cylinder", "value": times[-1], "unit": "s",
+        "higher_is_better": False, "n_gpus": 1, "data": "synthetic (seeded Philox initial MPS)",
+        "config": {"workload": f"6x24 cylinder (PBC around, OBC along), J1=1, Sz=0, maxdim {chi}, "
+                               "cutoff 1e-10, Krylov dim 4, maxiter 8", "mixed": SWEEP_MIXED},
+        "sweep_s": times, "energy_per_sweep": energies, "energy_per_site": energies[-1] / n,
+        "matvecs_per_sweep": matvecs, "init_s": t_init,
+        "max_mpo_bond": max(W.space[2].dim() for W in Ws),
+    }
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
     elif a.gradient:
         run_gradient(a)
+    elif a.cylinder:
+        run_cylinder(a)
     else:
         run_ours(a)
