@@ -278,9 +278,13 @@ __device__ __forceinline__ int exp_bound(unsigned long long absbits) {
 
 constexpr int kNoExponent = (int)0x80808080;  // byte pattern of the reset: "row entirely zero"
 
-// One CTA per (problem, block of 32 operand rows, K chunk): chunk exponents e(r,c), and the row
+// One CTA per (problem, block of operand rows, K chunk): chunk exponents e(r,c), and the row
 // reference R(r) = max_c e(r,c) by atomicMax (R is reset to kNoExponent before the pass).
-// Loads are coalesced along whichever operand axis is contiguous.
+// Loads are coalesced along whichever operand axis is contiguous. Row blocks of 32 rows: for A
+// operands (row-contiguous) 32 rows x 8 K groups per CTA, for B operands (K-contiguous) one
+// warp per row, four rows per warp.
+constexpr int kExpRowsA = 32, kExpRowsB = 32;
+
 __global__ void __launch_bounds__(256) pack_exponents_kernel(
     const Problem* __restrict__ probs, const int64_t* __restrict__ item_prefix, int nprob,
     int64_t nitems, int is_b, int chunk, int write_e, const double* __restrict__ X,
@@ -288,14 +292,15 @@ __global__ void __launch_bounds__(256) pack_exponents_kernel(
     int32_t* __restrict__ R) {
   __shared__ unsigned long long red[8][33];
   const int t = threadIdx.x;
+  const int rb = is_b ? kExpRowsB : kExpRowsA;
   for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int p = find_problem(item_prefix, nprob, it);
     const Problem P = probs[p];
     const int64_t lt = it - item_prefix[p];
     int64_t rows, off, rs, ks;
     operand_geom(P, is_b, rows, off, rs, ks);
-    const int64_t nrb = (rows + 31) / 32;
-    const int64_t r0 = (lt % nrb) * 32;
+    const int64_t nrb = (rows + rb - 1) / rb;
+    const int64_t r0 = (lt % nrb) * rb;
     const int c = (int)(lt / nrb);
     const int64_t k0 = (int64_t)c * chunk, k1 = min(k0 + chunk, P.K);
     const int64_t rbase = is_b ? P.rB : P.rA;
@@ -323,9 +328,9 @@ __global__ void __launch_bounds__(256) pack_exponents_kernel(
       }
       __syncthreads();
     } else {
-      // one row per warp at a time, lanes along the contiguous K axis
+      // one row per warp, lanes along the contiguous K axis
       const int lane = t & 31, w = t >> 5;
-      for (int rr = w; rr < 32; rr += 8) {
+      for (int rr = w; rr < rb; rr += 8) {
         const int64_t r = r0 + rr;
         if (r >= rows) break;
         unsigned long long m = 0;
@@ -350,6 +355,8 @@ __global__ void __launch_bounds__(256) pack_exponents_kernel(
 }
 
 // One CTA per packed tile (rows_per_tile x 64 K).  Writes S slices, row-major 128-byte rows.
+// A thread owns 8 consecutive K of one row and reads them straight from global memory (no
+// shared-memory staging, no barrier).
 template <int S>
 __global__ void __launch_bounds__(256) pack_slices_kernel(
     const Problem* __restrict__ probs, const int64_t* __restrict__ tile_prefix, int nprob,
@@ -357,8 +364,6 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
     const double* __restrict__ X, const int16_t* __restrict__ E, const int32_t* __restrict__ R,
     __nv_bfloat16* __restrict__ out) {
   constexpr int kBeta = kSliceBits;
-  extern __shared__ double pack_smem[];  // [128][65] doubles, dynamic (above the static limit)
-  double(*tile)[65] = reinterpret_cast<double(*)[65]>(pack_smem);
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int p = find_problem(tile_prefix, nprob, t);
     const Problem P = probs[p];
@@ -371,28 +376,21 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
     const int64_t ebase = is_b ? P.eB : P.eA;
     const int c = (int)(k0 / chunk);
     const int64_t tile_row0 = (is_b ? P.tB : P.tA) * rows_per_tile + lt * rows_per_tile;
-    // tiles of up to 256 rows are processed in halves of 128 rows through shared memory
-    for (int h0 = 0; h0 < rows_per_tile; h0 += 128) {
-      const int hrows = min(128, rows_per_tile - h0);  // rows of this tile handled in this pass
-      const int64_t r0 = ri * rows_per_tile + h0;
-      // stage the FP64 half tile in shared memory, coalesced along the contiguous axis
-      if (rs == 1) {
-        for (int i = threadIdx.x; i < hrows * 64; i += 256) {
-          const int rr = i % hrows, kk = i / hrows;
-          const int64_t r = r0 + rr, k = k0 + kk;
-          tile[rr][kk] = (r < rows && k < P.K) ? X[off + r * rs + k * ks] : 0.0;
-        }
-      } else {
-        for (int i = threadIdx.x; i < hrows * 64; i += 256) {
-          const int kk = i % 64, rr = i / 64;
-          const int64_t r = r0 + rr, k = k0 + kk;
-          tile[rr][kk] = (r < rows && k < P.K) ? X[off + r * rs + k * ks] : 0.0;
-        }
-      }
-      __syncthreads();
-      for (int i = threadIdx.x; i < hrows * 8; i += 256) {
-        const int g8 = i % 8, rr = i / 8;
+    {
+      const int64_t r0 = ri * rows_per_tile;
+      const int h0 = 0;
+      for (int i = threadIdx.x; i < rows_per_tile * 8; i += 256) {
+        // 8 threads along one row: their slice stores form one contiguous 128-byte row; loads
+        // are 64 contiguous bytes per thread (K-contiguous) or 4 rows x 32 bytes per column
+        // across the warp (row-contiguous), full sectors either way
+        const int g8 = i & 7, rr = i >> 3;
         const int64_t r = r0 + rr;
+        double xv[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int64_t k = k0 + g8 * 8 + j;
+          xv[j] = (r < rows && k < P.K) ? __ldg(X + off + r * rs + k * ks) : 0.0;
+        }
         int e = 0, Rr = 0;
         if (r < rows) {
           e = use_r ? R[rbase + r] : E[ebase + r * P.nch + c];
@@ -415,7 +413,7 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
         uint32_t packed[S][4];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          const double x = tile[rr][g8 * 8 + j];
+          const double x = xv[j];
           const int hw = __double2hiint(x);
           const uint32_t lw = (uint32_t)__double2loint(x);
           const int eb = (hw >> 20) & 0x7ff;
@@ -457,7 +455,6 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
           *reinterpret_cast<uint4*>(out + idx) = w;
         }
       }
-      __syncthreads();
     }
   }
 }
@@ -1006,8 +1003,10 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
     // exponent work items: (32-row block, K chunk) pairs
     // (in fast mode the K range is only split for parallelism: segments of `seg` columns)
     const int64_t nseg = fast ? ((int64_t)t.K + seg - 1) / seg : P.nch;
-    rowA_prefix.push_back(rowA_prefix.back() + (P.nks ? ((P.M + 31) / 32) * nseg : 0));
-    rowB_prefix.push_back(rowB_prefix.back() + (P.nks ? ((P.N + 31) / 32) * nseg : 0));
+    rowA_prefix.push_back(rowA_prefix.back() +
+                          (P.nks ? ((P.M + kExpRowsA - 1) / kExpRowsA) * nseg : 0));
+    rowB_prefix.push_back(rowB_prefix.back() +
+                          (P.nks ? ((P.N + kExpRowsB - 1) / kExpRowsB) * nseg : 0));
     flops += 2.0 * t.M * t.N * t.K;
     probs.push_back(P);
   }
@@ -1079,13 +1078,6 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
   using CF = Cfg<S>;
   using FCF = FastCfg<S <= 3 ? S : 3>;
   const int chunk = sp.chunk;
-  constexpr int kPackSmem = 128 * 65 * (int)sizeof(double);
-  static bool pack_attr = false;
-  if (!pack_attr) {
-    MPSG_CUDA(cudaFuncSetAttribute(pack_slices_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   kPackSmem));
-    pack_attr = true;
-  }
   for (int side = 0; side < 2; ++side) {
     if (!(what & (side ? kPackB : kPackA))) continue;
     const int64_t nitems = side ? sp.nrowsB : sp.nrowsA;
@@ -1107,8 +1099,8 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
     }
     if (ntile) {
       KernelTimer timer(ctx, kKindPackSlices);
-      int g = (int)std::min<int64_t>(ntile, (int64_t)ctx->num_sms * 6);
-      pack_slices_kernel<S><<<g, 256, kPackSmem, ctx->stream>>>(
+      int g = (int)std::min<int64_t>(ntile, (int64_t)ctx->num_sms * 8);
+      pack_slices_kernel<S><<<g, 256, 0, ctx->stream>>>(
           sp.d_probs, side ? sp.d_packB_prefix : sp.d_packA_prefix, sp.nprob, ntile, side, chunk,
           sp.fast ? 1 : 0,
           side ? sp.bn : BM, side ? sp.rowsB : sp.rowsA, X, E, R,
