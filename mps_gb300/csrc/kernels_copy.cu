@@ -25,7 +25,9 @@ namespace mpsg {
 namespace {
 
 constexpr int kWarps = 8;          // warps per CTA
-constexpr int kRowElems = 1024;    // target elements per row-mode unit
+// target elements per row-mode unit: small enough that a copy of a few MB spreads over every
+// resident warp and each warp's chain of dependent load batches stays short
+constexpr int kRowElems = 256;
 constexpr int kGatherUnit = 256;   // destination positions per gather unit
 constexpr int kT = 32;             // transpose tile edge
 
