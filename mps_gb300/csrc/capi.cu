@@ -90,6 +90,9 @@ int mpsg_ctx_clear_caches(mpsg_ctx* ctx) {
     ctx->c.contract_cache.clear();
     ctx->c.releg_cache.clear();
     ctx->c.matmul_cache.clear();
+    ctx->c.heff_cache.clear();
+    ctx->c.heff_lru.clear();
+    ctx->c.heff_bytes = 0;
   });
 }
 

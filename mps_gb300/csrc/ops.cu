@@ -1,5 +1,6 @@
 // Tensor-level operations: plan lookup (cached per structure), scratch management and the
 // launch sequences of each SymTensors operation.
+#include <algorithm>
 #include <sstream>
 
 #include "ops.hpp"
@@ -78,6 +79,8 @@ void collect_kernel_times(Context* ctx) {
 }
 
 Context::~Context() {
+  heff_cache.clear();
+  heff_lru.clear();
   contract_cache.clear();
   releg_cache.clear();
   matmul_cache.clear();
@@ -443,31 +446,64 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
     throw Error(kErrUnsupported, "precision must be 0 (FP64) or 2..7 bf16 slices");
   op->envLW = contract(ctx, envL, kLW_A, W1, kLW_B, 0, nullptr);
   op->envRW = contract(ctx, W2, kRW_A, envR, kRW_B, 0, nullptr);
-  op->c1 = private_contract_plan(op->envLW.meta, kX_A, vmeta, kX_B);
-  op->c2 = private_contract_plan(op->c1->host->split.out, kO_A, op->envRW.meta, kO_B);
-  {
-    const ContractPlan& h1 = *op->c1->host;
-    const ContractPlan& h2 = *op->c2->host;
+  op->plan_key = "H" + std::to_string(precision) + "|" + meta_key(vmeta) + "|" +
+                 meta_key(envL.meta) + "|" + meta_key(envR.meta) + "|" + meta_key(W1.meta) +
+                 "|" + meta_key(W2.meta);
+  auto hit = ctx->heff_cache.find(op->plan_key);
+  if (hit != ctx->heff_cache.end()) {  // take the idle plans of this structure
+    op->plans = hit->second;
+    ctx->heff_cache.erase(hit);
+    auto& lru = ctx->heff_lru;
+    lru.erase(std::find(lru.begin(), lru.end(), op->plan_key));
+    ctx->heff_bytes -= op->plans->bytes;
+  } else {
+    auto P = std::make_shared<HeffPlans>();
+    P->c1 = private_contract_plan(op->envLW.meta, kX_A, vmeta, kX_B);
+    P->c2 = private_contract_plan(P->c1->host->split.out, kO_A, op->envRW.meta, kO_B);
+    const ContractPlan& h1 = *P->c1->host;
+    const ContractPlan& h2 = *P->c2->host;
     std::vector<BlockMap> src_of_x, dst_of_x;
     plan_split_permute_rec(h1.mm.out, h1.rlegs, h1.clegs, h1.perm, &src_of_x);
     plan_symmatrix_rec(h1.split.out, h2.rowsA, h2.colsA, &dst_of_x);
-    op->x2a.upload(compose_through(h1.split.out, src_of_x, dst_of_x), false);
+    P->x2a.upload(compose_through(h1.split.out, src_of_x, dst_of_x), false);
+    for (auto* c : {P->c1.get(), P->c2.get()}) {
+      auto& sp = c->mm.splitp[precision];
+      sp = std::make_shared<split::SplitPlan>();
+      sp->build(ctx, c->mm.host, precision);
+      P->bytes += (size_t)sp->S * (size_t)(sp->rowsA + sp->rowsB) * 128;
+    }
+    op->plans = P;
   }
   // constant operands: fuse once, slice once
-  op->fusedA1 = alloc_buffer(ctx, op->c1->host->fa.out.total);
-  launch_copy(ctx, op->c1->fa, op->envLW.data(), op->fusedA1->ptr);
-  op->fusedB2 = alloc_buffer(ctx, op->c2->host->fb.out.total);
-  launch_copy(ctx, op->c2->fb, op->envRW.data(), op->fusedB2->ptr);
-  for (auto* c : {op->c1.get(), op->c2.get()}) {
-    auto& sp = c->mm.splitp[precision];
-    sp = std::make_shared<split::SplitPlan>();
-    sp->build(ctx, c->mm.host, precision);
-  }
-  split::launch_split_gemm(ctx, *op->c1->mm.splitp[precision], op->fusedA1->ptr, nullptr, nullptr,
+  DevContract& c1 = *op->plans->c1;
+  DevContract& c2 = *op->plans->c2;
+  op->fusedA1 = alloc_buffer(ctx, c1.host->fa.out.total);
+  launch_copy(ctx, c1.fa, op->envLW.data(), op->fusedA1->ptr);
+  op->fusedB2 = alloc_buffer(ctx, c2.host->fb.out.total);
+  launch_copy(ctx, c2.fb, op->envRW.data(), op->fusedB2->ptr);
+  split::launch_split_gemm(ctx, *c1.mm.splitp[precision], op->fusedA1->ptr, nullptr, nullptr,
                            split::kPackA);
-  split::launch_split_gemm(ctx, *op->c2->mm.splitp[precision], nullptr, op->fusedB2->ptr, nullptr,
+  split::launch_split_gemm(ctx, *c2.mm.splitp[precision], nullptr, op->fusedB2->ptr, nullptr,
                            split::kPackB);
   return op;
+}
+
+HeffOp::~HeffOp() {
+  if (!plans || plan_key.empty() || !ctx) return;
+  constexpr size_t kBudget = size_t(8) << 30;  // idle plans kept per context (device bytes)
+  if (ctx->heff_cache.count(plan_key)) return;  // an idle copy exists already: drop this one
+  ctx->heff_cache[plan_key] = plans;
+  ctx->heff_lru.push_back(plan_key);
+  ctx->heff_bytes += plans->bytes;
+  while (ctx->heff_bytes > kBudget && !ctx->heff_lru.empty()) {
+    const std::string k = ctx->heff_lru.front();
+    ctx->heff_lru.erase(ctx->heff_lru.begin());
+    auto it = ctx->heff_cache.find(k);
+    if (it != ctx->heff_cache.end()) {
+      ctx->heff_bytes -= it->second->bytes;
+      ctx->heff_cache.erase(it);
+    }
+  }
 }
 
 DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v) {
@@ -477,7 +513,7 @@ DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v) {
   if (op.precision == 0) return applymps2site(ctx, v, op.envL, op.envR, op.W1, op.W2, 0);
   const int S = op.precision;
   // X = envLW . v
-  DevContract& c1 = *op.c1;
+  DevContract& c1 = *op.plans->c1;
   auto fb = alloc_buffer(ctx, c1.host->fb.out.total);
   launch_copy(ctx, c1.fb, v.data(), fb->ptr);
   auto fc1 = alloc_buffer(ctx, c1.host->mm.out.total);
@@ -485,9 +521,9 @@ DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v) {
                            split::kPackB | split::kRunGemm);
   fb.reset();
   // v' = X . envRW, with GEMM 1's fused output moved straight into GEMM 2's fused A operand
-  DevContract& c2 = *op.c2;
+  DevContract& c2 = *op.plans->c2;
   auto fa = alloc_buffer(ctx, c2.host->fa.out.total);
-  launch_copy(ctx, op.x2a, fc1->ptr, fa->ptr);
+  launch_copy(ctx, op.plans->x2a, fc1->ptr, fa->ptr);
   fc1.reset();
   auto fc2 = alloc_buffer(ctx, c2.host->mm.out.total);
   split::launch_split_gemm(ctx, *c2.mm.splitp[S], fa->ptr, nullptr, fc2->ptr,

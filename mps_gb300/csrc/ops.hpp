@@ -47,17 +47,30 @@ double dot(Context* ctx, const DeviceTensor& a, const DeviceTensor& b);
 //      X(l,s1',m',s2,r)  = envLW(l',s1,l,m',s1') . v(l',s1,s2,r)        over (l', s1)
 //      v'(l,s1',s2',r')  = X . envRW(r,m',s2,s2',r')                      over (m', s2, r)
 //    with the constant operands fused and sliced once.
+// The structure-only part of a prepared split-precision H_eff: the two GEMM contraction plans
+// (with their split-GEMM plans, which also hold the packed constant operands) and the composed
+// copy list. Building it is host work (planning, table uploads, tensor maps); the context keeps
+// idle ones by structure and precision so that the next operator of the same structure (the
+// same bond in a later sweep, repeated reference-style calls) skips it. One live operator owns
+// an entry at a time.
+struct HeffPlans {
+  std::shared_ptr<DevContract> c1, c2;
+  DevCopyPlan x2a;                   // fused X of GEMM 1 -> fused A of GEMM 2 (X never built)
+  size_t bytes = 0;                  // device storage held, for the cache budget
+  ~HeffPlans() { x2a.release(); }
+};
+
 struct HeffOp {
   Context* ctx = nullptr;
   int precision = 0;
   DeviceTensor envL, envR, W1, W2;   // precision 0
   DeviceTensor envLW, envRW;         // precision >= 2
   TensorMeta vmeta;
-  std::shared_ptr<DevContract> c1, c2;
-  DevCopyPlan x2a;                   // fused X of GEMM 1 -> fused A of GEMM 2 (X never built)
+  std::shared_ptr<HeffPlans> plans;  // precision >= 2
+  std::string plan_key;
   std::shared_ptr<Buffer> fusedA1, fusedB2;
   double ref_flops = 0;  // algorithmic flops of the reference contraction order
-  ~HeffOp() { x2a.release(); }
+  ~HeffOp();             // hands `plans` back to the context's cache
 };
 
 // Host plans of the W-folded H_eff: the two folding contractions, the two GEMM contractions and

@@ -22,6 +22,7 @@ namespace mpsg {
   } while (0)
 
 struct Context;
+struct HeffPlans;
 namespace split {
 struct SplitPlan;
 }
@@ -111,6 +112,10 @@ struct Context : std::enable_shared_from_this<Context> {
   std::unordered_map<std::string, std::shared_ptr<DevContract>> contract_cache;
   std::unordered_map<std::string, std::shared_ptr<DevReleg>> releg_cache;
   std::unordered_map<std::string, std::shared_ptr<DevGemmPlan>> matmul_cache;
+  // idle prepared-H_eff plans by structure + precision, least recently returned first
+  std::unordered_map<std::string, std::shared_ptr<HeffPlans>> heff_cache;
+  std::vector<std::string> heff_lru;
+  size_t heff_bytes = 0;
   int64_t kernel_launches = 0;    // launches of this library's kernels
   bool debug_sync = false;        // MPSG_DEBUG_SYNC=1: synchronise and check after tensor-core GEMMs
   double gemm_flops = 0;          // algorithmic flops issued through block GEMMs

@@ -124,3 +124,21 @@ def test_split_heff_chi64(S):
     D = gd.heff_problem(64, 0.5, 1911, ncharges=9)
     got = mg.applymps2site(*D, precision=S).to_flat()
     assert relerr(got, want) < 4 * TOL[S]
+
+
+def test_prepared_operator_plan_reuse():
+    """Operators of one structure: two alive at once get separate plans (their packed constant
+    operands must not be shared), and an operator built after one is freed reuses the returned
+    plans. All give the same result, for new environment values too."""
+    v, eL, eR, W1, W2 = gd.heff_problem(64, 0.5, 1911, ncharges=9)
+    want = mg.applymps2site(v, eL, eR, W1, W2, precision=0).to_flat()
+    a = mg.Heff2(v, eL, eR, W1, W2, precision=4)
+    b = mg.Heff2(v, eL, eR, W1, W2, precision=4)
+    ya, yb = a(v).to_flat(), b(v).to_flat()
+    assert relerr(ya, want) < TOL[4] and np.array_equal(ya, yb)
+    del a, b
+    eL2 = mg.copy(eL)
+    mg.rmul(eL2, -0.5)  # new values, same structure
+    c = mg.Heff2(v, eL2, eR, W1, W2, precision=4)  # built from returned plans
+    want2 = mg.applymps2site(v, eL2, eR, W1, W2, precision=0).to_flat()
+    assert relerr(c(v).to_flat(), want2) < TOL[4]
