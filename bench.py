@@ -58,6 +58,10 @@ def parse():
                    help="instead of the H_eff line: mixed-precision 2-site DMRG sweeps of the "
                         "J1 Heisenberg 6 x 24 cylinder at maxdim --sweep-chi (default 1024)")
     p.add_argument("--sweeps", type=int, default=2, help="sweeps of the --cylinder run")
+    p.add_argument("--batched", type=int, default=0, metavar="N",
+                   help="instead of the H_eff line: N independent XXZ chains (L in [32,128], "
+                        "Delta in [0,1.5], maxdim in {128,256,512,1024}, seeded), one sweep "
+                        "each, concurrently and one after the other")
     p.add_argument("--sweep-chi", type=int, default=None, help="maxdim of the sweep (default chi)")
     return p.parse_args()
 
@@ -519,6 +523,34 @@ def run_cylinder(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args):
+    """Many independent chains: one sweep of each of N seeded XXZ chains (mixed configuration),
+    driven concurrently (one context / CUDA stream and one host thread per chain) and one after
+    the other; wall time of each (setup included: random MPS, canonicalisation, environments)."""
+    from mps_gb300 import dmrg as gd
+    specs = gd.chain_ensemble(args.batched)
+    o = gd.SweepOptions(tol=1e-10, lanczostol=1e-7, krylovdim=4, krylovmaxiter=8, **SWEEP_MIXED)
+    import mps_gb300 as mg
+    mg.get_context(0).synchronize()
+    t0 = time.perf_counter()
+    e_conc = gd.run_chains(specs, 1, o, threads=len(specs))
+    t_conc = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    e_seq = gd.run_chains(specs, 1, o, threads=1)
+    t_seq = time.perf_counter() - t0
+    line = {
+        "metric": "independent DMRG chains, one sweep each: wall s", "value": t_conc, "unit": "s",
+        "higher_is_better": False, "n_gpus": 1, "data": "synthetic (seeded Philox)",
+        "config": {"workload": f"{len(specs)} XXZ chains, L in [32,128], Delta in [0,1.5], maxdim "
+                               "in {128,256,512,1024} (Philox seed 1911), one 2-site sweep each",
+                   "mixed": SWEEP_MIXED, "chains": [list(s) for s in specs]},
+        "concurrent_s": t_conc, "one_by_one_s": t_seq, "speedup": t_seq / t_conc,
+        "max_rel_dE_concurrent_vs_one_by_one": max(abs(a - b) / abs(b)
+                                                   for a, b in zip(e_conc, e_seq)),
+    }
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
@@ -527,5 +559,7 @@ if __name__ == "__main__":
         run_gradient(a)
     elif a.cylinder:
         run_cylinder(a)
+    elif a.batched:
+        run_batched(a)
     else:
         run_ours(a)

@@ -218,19 +218,23 @@ constexpr size_t kTileSmem = kViewSmem + sizeof(TileBuf) * kWarps;
 
 size_t copy_aux_bytes() { return sizeof(TaskAux); }
 
-void DevCopyPlan::upload(const std::vector<CopyTask>& tasks, bool identity_) {
+void DevCopyPlan::upload(const std::vector<CopyTask>& tasks, bool identity_, cudaStream_t st) {
   release();
+  stream = st;
   std::vector<int64_t> prefix;
   std::vector<unsigned char> aux;
   build_host(tasks, identity_, prefix, aux);
   if (ntasks == 0) return;
-  MPSG_CUDA(cudaMalloc(&d_tasks, sizeof(CopyTask) * ntasks));
-  MPSG_CUDA(cudaMalloc(&d_prefix, sizeof(int64_t) * (ntasks + 1)));
-  MPSG_CUDA(cudaMalloc(&d_aux, aux.size()));
-  MPSG_CUDA(cudaMemcpy(d_tasks, tasks.data(), sizeof(CopyTask) * ntasks, cudaMemcpyHostToDevice));
-  MPSG_CUDA(cudaMemcpy(d_prefix, prefix.data(), sizeof(int64_t) * (ntasks + 1),
-                       cudaMemcpyHostToDevice));
-  MPSG_CUDA(cudaMemcpy(d_aux, aux.data(), aux.size(), cudaMemcpyHostToDevice));
+  // stream-ordered: no device-wide synchronisation, so contexts on one GPU do not serialise on
+  // plan uploads (pageable sources are staged before the calls return)
+  MPSG_CUDA(cudaMallocAsync((void**)&d_tasks, sizeof(CopyTask) * ntasks, st));
+  MPSG_CUDA(cudaMallocAsync((void**)&d_prefix, sizeof(int64_t) * (ntasks + 1), st));
+  MPSG_CUDA(cudaMallocAsync(&d_aux, aux.size(), st));
+  MPSG_CUDA(cudaMemcpyAsync(d_tasks, tasks.data(), sizeof(CopyTask) * ntasks,
+                            cudaMemcpyHostToDevice, st));
+  MPSG_CUDA(cudaMemcpyAsync(d_prefix, prefix.data(), sizeof(int64_t) * (ntasks + 1),
+                            cudaMemcpyHostToDevice, st));
+  MPSG_CUDA(cudaMemcpyAsync(d_aux, aux.data(), aux.size(), cudaMemcpyHostToDevice, st));
 }
 
 void DevCopyPlan::build_host(const std::vector<CopyTask>& tasks, bool identity_,
@@ -292,9 +296,9 @@ void DevCopyPlan::build_host(const std::vector<CopyTask>& tasks, bool identity_,
 }
 
 void DevCopyPlan::release() {
-  if (d_tasks) cudaFree(d_tasks);
-  if (d_prefix) cudaFree(d_prefix);
-  if (d_aux) cudaFree(d_aux);
+  if (d_tasks) cudaFreeAsync(d_tasks, stream);
+  if (d_prefix) cudaFreeAsync(d_prefix, stream);
+  if (d_aux) cudaFreeAsync(d_aux, stream);
   d_tasks = nullptr;
   d_prefix = nullptr;
   d_aux = nullptr;

@@ -265,17 +265,19 @@ void DevGemmPlan::build_host(const std::vector<GemmTask>& g, double flops_, Gemm
   ntiles = units[kTiled];
 }
 
-void DevGemmPlan::upload(const std::vector<GemmTask>& g, double flops_) {
+void DevGemmPlan::upload(const std::vector<GemmTask>& g, double flops_, cudaStream_t st) {
   release();
+  stream = st;
   GemmTables t;
   build_host(g, flops_, t);
   for (int q = 0; q < 3; ++q) {
     if (count[q] == 0) continue;
     const size_t bt = sizeof(GemmTask) * count[q], bp = sizeof(int64_t) * (count[q] + 1);
-    MPSG_CUDA(cudaMalloc(&d_part[q], bt));
-    MPSG_CUDA(cudaMalloc(&d_part_prefix[q], bp));
-    MPSG_CUDA(cudaMemcpy(d_part[q], t.part[q].data(), bt, cudaMemcpyHostToDevice));
-    MPSG_CUDA(cudaMemcpy(d_part_prefix[q], t.prefix[q].data(), bp, cudaMemcpyHostToDevice));
+    MPSG_CUDA(cudaMallocAsync((void**)&d_part[q], bt, st));
+    MPSG_CUDA(cudaMallocAsync((void**)&d_part_prefix[q], bp, st));
+    MPSG_CUDA(cudaMemcpyAsync(d_part[q], t.part[q].data(), bt, cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(d_part_prefix[q], t.prefix[q].data(), bp, cudaMemcpyHostToDevice,
+                              st));
   }
   d_tasks = d_part[kTiled];
   d_prefix = d_part_prefix[kTiled];
@@ -283,8 +285,8 @@ void DevGemmPlan::upload(const std::vector<GemmTask>& g, double flops_) {
 
 void DevGemmPlan::release() {
   for (int q = 0; q < 3; ++q) {
-    if (d_part[q]) cudaFree(d_part[q]);
-    if (d_part_prefix[q]) cudaFree(d_part_prefix[q]);
+    if (d_part[q]) cudaFreeAsync(d_part[q], stream);
+    if (d_part_prefix[q]) cudaFreeAsync(d_part_prefix[q], stream);
     d_part[q] = nullptr;
     d_part_prefix[q] = nullptr;
     count[q] = 0;

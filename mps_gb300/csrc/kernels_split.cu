@@ -1028,10 +1028,19 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   rowsRA = std::max<int64_t>(rA, 1);
   rowsCB = std::max<int64_t>(rB, 1);
   if (nprob == 0) return;
-  auto up = [](void** d, const void* h, size_t bytes) {
-    MPSG_CUDA(cudaMalloc(d, std::max<size_t>(bytes, 16)));
-    if (bytes) MPSG_CUDA(cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice));
+  // stream-ordered allocation on the context's stream: no device-wide synchronisation, so
+  // contexts sharing the GPU do not serialise on plan builds (pageable sources are staged
+  // before the copy calls return)
+  cudaStream_t st = ctx->stream;
+  stream = st;
+  auto alloc = [st](void** d, size_t bytes) {
+    MPSG_CUDA(cudaMallocAsync(d, std::max<size_t>(bytes, 16), st));
   };
+  auto up = [&](void** d, const void* h, size_t bytes) {
+    alloc(d, bytes);
+    if (bytes) MPSG_CUDA(cudaMemcpyAsync(*d, h, bytes, cudaMemcpyHostToDevice, st));
+  };
+  auto zero = [st](void* d, size_t bytes) { MPSG_CUDA(cudaMemsetAsync(d, 0, bytes, st)); };
   up((void**)&d_probs, probs.data(), sizeof(Problem) * nprob);
   up((void**)&d_tile_prefix, tile_prefix.data(), sizeof(int64_t) * (nprob + 1));
   up((void**)&d_tiles, tl.data(), sizeof(int4) * tl.size());
@@ -1039,29 +1048,28 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   up((void**)&d_packB_prefix, packB_prefix.data(), sizeof(int64_t) * (nprob + 1));
   up((void**)&d_rowA_prefix, rowA_prefix.data(), sizeof(int64_t) * (nprob + 1));
   up((void**)&d_rowB_prefix, rowB_prefix.data(), sizeof(int64_t) * (nprob + 1));
-  MPSG_CUDA(cudaMalloc(&d_RA, sizeof(int32_t) * std::max<int64_t>(rA, 1)));
-  MPSG_CUDA(cudaMalloc(&d_CB, sizeof(int32_t) * std::max<int64_t>(rB, 1)));
-  MPSG_CUDA(cudaMemset(d_RA, 0, sizeof(int32_t) * std::max<int64_t>(rA, 1)));
-  MPSG_CUDA(cudaMemset(d_CB, 0, sizeof(int32_t) * std::max<int64_t>(rB, 1)));
-  MPSG_CUDA(cudaMalloc(&d_EA, sizeof(int16_t) * std::max<int64_t>(eA, 1)));
-  MPSG_CUDA(cudaMalloc(&d_EB, sizeof(int16_t) * std::max<int64_t>(eB, 1)));
-  MPSG_CUDA(cudaMemset(d_EA, 0, sizeof(int16_t) * std::max<int64_t>(eA, 1)));
-  MPSG_CUDA(cudaMemset(d_EB, 0, sizeof(int16_t) * std::max<int64_t>(eB, 1)));
-  MPSG_CUDA(cudaMalloc(&d_packA, std::max<int64_t>(S * rowsA * 64 * 2, 128 * 128)));
-  MPSG_CUDA(cudaMalloc(&d_packB, std::max<int64_t>(S * rowsB * 64 * 2, 128 * 128)));
-  MPSG_CUDA(cudaMalloc(&d_err, sizeof(int)));
-  MPSG_CUDA(cudaMemset(d_err, 0, sizeof(int)));
+  alloc((void**)&d_RA, sizeof(int32_t) * std::max<int64_t>(rA, 1));
+  alloc((void**)&d_CB, sizeof(int32_t) * std::max<int64_t>(rB, 1));
+  zero(d_RA, sizeof(int32_t) * std::max<int64_t>(rA, 1));
+  zero(d_CB, sizeof(int32_t) * std::max<int64_t>(rB, 1));
+  alloc((void**)&d_EA, sizeof(int16_t) * std::max<int64_t>(eA, 1));
+  alloc((void**)&d_EB, sizeof(int16_t) * std::max<int64_t>(eB, 1));
+  zero(d_EA, sizeof(int16_t) * std::max<int64_t>(eA, 1));
+  zero(d_EB, sizeof(int16_t) * std::max<int64_t>(eB, 1));
+  alloc((void**)&d_packA, std::max<int64_t>(S * rowsA * 64 * 2, 128 * 128));
+  alloc((void**)&d_packB, std::max<int64_t>(S * rowsB * 64 * 2, 128 * 128));
+  alloc((void**)&d_err, sizeof(int));
+  zero(d_err, sizeof(int));
   const int box_x = (fast || S > 3) ? 32 : BK;  // K step of the kernel that reads the slices
   make_map(&tmA, d_packA, std::max<int64_t>(rowsA, BM), S, BM, box_x);
   make_map(&tmB, d_packB, std::max<int64_t>(rowsB, bn), S, bn, box_x);
-  (void)ctx;
 }
 
 void SplitPlan::release() {
   void* ptrs[] = {d_probs, d_tile_prefix, d_packA_prefix, d_packB_prefix, d_rowA_prefix,
                   d_rowB_prefix, d_RA, d_CB, d_EA, d_EB, d_packA, d_packB, d_err, d_tiles};
   for (void* p : ptrs)
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, stream);
   d_probs = nullptr;
   d_tiles = nullptr;
   d_tile_prefix = d_packA_prefix = d_packB_prefix = d_rowA_prefix = d_rowB_prefix = nullptr;

@@ -160,7 +160,7 @@ static std::shared_ptr<DevReleg> releg_plan(Context* ctx, const std::string& key
   if (it != ctx->releg_cache.end()) return it->second;
   auto p = std::make_shared<DevReleg>();
   p->host = build();
-  p->cp.upload(p->host.tasks, p->host.identity);
+  p->cp.upload(p->host.tasks, p->host.identity, ctx->stream);
   ctx->releg_cache[key] = p;
   return p;
 }
@@ -239,7 +239,7 @@ DeviceTensor matmul(Context* ctx, const DeviceTensor& a, const DeviceTensor& b, 
   if (it == ctx->matmul_cache.end()) {
     mp = plan_matmul(a.meta, b.meta);
     g = std::make_shared<DevGemmPlan>();
-    g->upload(mp.gemms, mp.flops);
+    g->upload(mp.gemms, mp.flops, ctx->stream);
     ctx->matmul_cache[key] = g;
   } else {
     g = it->second;
@@ -265,10 +265,10 @@ std::shared_ptr<DevContract> get_contract_plan(Context* ctx, const TensorMeta& A
   auto p = std::make_shared<DevContract>();
   p->host = plan_contract(A, idxA, B, idxB);
   if (!p->host->scalar) {
-    p->fa.upload(p->host->fa.tasks, p->host->fa.identity);
-    p->fb.upload(p->host->fb.tasks, p->host->fb.identity);
-    p->mm.upload(p->host->mm.gemms, p->host->mm.flops);
-    p->split.upload(p->host->split.tasks, p->host->split.identity);
+    p->fa.upload(p->host->fa.tasks, p->host->fa.identity, ctx->stream);
+    p->fb.upload(p->host->fb.tasks, p->host->fb.identity, ctx->stream);
+    p->mm.upload(p->host->mm.gemms, p->host->mm.flops, ctx->stream);
+    p->split.upload(p->host->split.tasks, p->host->split.identity, ctx->stream);
   }
   ctx->contract_cache[key] = p;
   return p;
@@ -376,17 +376,17 @@ DeviceTensor mpsupdateright(Context* ctx, const DeviceTensor& env, const DeviceT
 // ------------------------------------------------------------------------------------------
 // prepared effective Hamiltonian
 // ------------------------------------------------------------------------------------------
-static std::shared_ptr<DevContract> private_contract_plan(const TensorMeta& A,
+static std::shared_ptr<DevContract> private_contract_plan(Context* ctx, const TensorMeta& A,
                                                           const std::vector<int>& idxA,
                                                           const TensorMeta& B,
                                                           const std::vector<int>& idxB) {
   auto p = std::make_shared<DevContract>();
   p->host = plan_contract(A, idxA, B, idxB);
   if (p->host->scalar) throw Error(kErrArgument, "unexpected full contraction");
-  p->fa.upload(p->host->fa.tasks, p->host->fa.identity);
-  p->fb.upload(p->host->fb.tasks, p->host->fb.identity);
-  p->mm.upload(p->host->mm.gemms, p->host->mm.flops);
-  p->split.upload(p->host->split.tasks, p->host->split.identity);
+  p->fa.upload(p->host->fa.tasks, p->host->fa.identity, ctx->stream);
+  p->fb.upload(p->host->fb.tasks, p->host->fb.identity, ctx->stream);
+  p->mm.upload(p->host->mm.gemms, p->host->mm.flops, ctx->stream);
+  p->split.upload(p->host->split.tasks, p->host->split.identity, ctx->stream);
   return p;
 }
 
@@ -458,14 +458,14 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
     ctx->heff_bytes -= op->plans->bytes;
   } else {
     auto P = std::make_shared<HeffPlans>();
-    P->c1 = private_contract_plan(op->envLW.meta, kX_A, vmeta, kX_B);
-    P->c2 = private_contract_plan(P->c1->host->split.out, kO_A, op->envRW.meta, kO_B);
+    P->c1 = private_contract_plan(ctx, op->envLW.meta, kX_A, vmeta, kX_B);
+    P->c2 = private_contract_plan(ctx, P->c1->host->split.out, kO_A, op->envRW.meta, kO_B);
     const ContractPlan& h1 = *P->c1->host;
     const ContractPlan& h2 = *P->c2->host;
     std::vector<BlockMap> src_of_x, dst_of_x;
     plan_split_permute_rec(h1.mm.out, h1.rlegs, h1.clegs, h1.perm, &src_of_x);
     plan_symmatrix_rec(h1.split.out, h2.rowsA, h2.colsA, &dst_of_x);
-    P->x2a.upload(compose_through(h1.split.out, src_of_x, dst_of_x), false);
+    P->x2a.upload(compose_through(h1.split.out, src_of_x, dst_of_x), false, ctx->stream);
     for (auto* c : {P->c1.get(), P->c2.get()}) {
       auto& sp = c->mm.splitp[precision];
       sp = std::make_shared<split::SplitPlan>();

@@ -55,7 +55,8 @@ struct DevCopyPlan {
   CopyTask* d_tasks = nullptr;
   int64_t* d_prefix = nullptr;   // ntasks+1 tile prefix
   void* d_aux = nullptr;         // per task: tile shape, axis roles, division constants
-  void upload(const std::vector<CopyTask>& tasks, bool identity_);
+  cudaStream_t stream = nullptr;  // tables are allocated and freed in this stream's order
+  void upload(const std::vector<CopyTask>& tasks, bool identity_, cudaStream_t st);
   // Host half of upload: tile prefix sums and per-task launch data; sets every field except the
   // device pointers (used by callers that place the tables in memory they own).
   void build_host(const std::vector<CopyTask>& tasks, bool identity_,
@@ -84,7 +85,8 @@ struct DevGemmPlan {
   int64_t* d_part_prefix[3] = {nullptr, nullptr, nullptr};
   std::vector<GemmTask> host;
   std::shared_ptr<split::SplitPlan> splitp[8];  // split-precision plans by slice count
-  void upload(const std::vector<GemmTask>& g, double flops_);
+  cudaStream_t stream = nullptr;  // tables are allocated and freed in this stream's order
+  void upload(const std::vector<GemmTask>& g, double flops_, cudaStream_t st);
   // Host half of upload: every field except the device pointers, plus the per-part tables.
   void build_host(const std::vector<GemmTask>& g, double flops_, GemmTables& t);
   void release();

@@ -35,6 +35,7 @@ struct Problem {
 // Device tables, packed-slice scratch and TMA descriptors of one grouped GEMM at S slices.
 struct SplitPlan {
   int S = 0;
+  cudaStream_t stream = nullptr;  // storage is allocated and freed in this stream's order
   bool fast = false;   // one FP32 accumulator, 128 x 256 tiles (S <= 3); else exact chunked mode
   int bn = 64;         // rows of a packed B tile = N of an output tile
   int chunk = 0;       // K columns per exact chunk (whole K in fast mode)

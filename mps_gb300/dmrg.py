@@ -385,3 +385,48 @@ def heff_flops_meta(v, envL, envR, W1, W2):
             total += mg.contract_flops(t, ia, B, ib)
             t = mg.contract(t, ia, B, ib)
     return total
+
+
+# ---------------------------------------------------------------------------------------------
+# many independent chains (the batched workload): one context (CUDA stream) per chain
+# ---------------------------------------------------------------------------------------------
+def chain_ensemble(n: int, seed: int = 1911, lengths=(32, 128), deltas=(0.0, 1.5),
+                   chis=(128, 256, 512, 1024)):
+    """(L, Delta, maxdim) of n independent XXZ chains: L uniform over the even lengths in
+    ``lengths``, Delta uniform in ``deltas``, maxdim drawn from ``chis`` (Philox ``seed``)."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    out = []
+    for _ in range(n):
+        L = 2 * int(rng.integers(lengths[0] // 2, lengths[1] // 2 + 1))
+        out.append((L, float(rng.uniform(*deltas)), int(rng.choice(chis))))
+    return out
+
+
+def run_chains(specs, nsweeps: int, opts: SweepOptions, threads: int | None = None,
+               device: int = 0, seed: int = 7):
+    """2-site DMRG on independent chains (L, Delta, maxdim), each with its own context, so its
+    kernels go to its own CUDA stream; ``threads`` host threads drive them (1 = one after the
+    other). Every chain starts from a random binomial-profile MPS (Philox seed + index),
+    canonicalised and with environments built, then runs ``nsweeps`` sweeps. Returns the last
+    post-truncation energy of each chain."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    results = [None] * len(specs)
+
+    def work(i):
+        L, delta, chi = specs[i]
+        ctx = mg.Context(device)
+        Ws = xxz_u1mpo(L, delta, ctx=ctx)
+        mps = mps_from_host(binomial_mps_host(L, L // 2, chi, seed + i), ctx)
+        center_at(mps, 1, svd=opts.svd)
+        env = initialenv(mps, Ws)
+        o = SweepOptions(**{**opts.__dict__, "maxdim": chi})
+        es = None
+        for _ in range(nsweeps):
+            es = dmrg2sitesweep(mps, Ws, env, o)
+        ctx.synchronize()
+        results[i] = es[-1]
+
+    with ThreadPoolExecutor(max_workers=max(1, threads or len(specs))) as ex:
+        list(ex.map(work, range(len(specs))))
+    return results

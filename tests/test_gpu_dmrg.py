@@ -187,3 +187,16 @@ def test_context_outlives_tensors_in_any_release_order():
     ctx.close()  # the tensor keeps the device context alive
     assert np.array_equal(t.to_flat(), np.full(9, 2.0))
     del t
+
+
+def test_independent_chains_concurrently_equal_one_by_one():
+    """Chains driven concurrently (one context and stream each) give exactly the energies of the
+    same chains run one after the other: the kernels are deterministic and the contexts share
+    nothing but the device."""
+    specs = [(12, 0.3, 24), (16, 1.0, 32), (14, 1.4, 16)]
+    o = gd.SweepOptions(tol=1e-10, lanczostol=1e-8, krylovdim=4, krylovmaxiter=8, precision=4,
+                        energy_precision=7, env_precision=7, svd="gram")
+    one = gd.run_chains(specs, 2, o, threads=1)
+    many = gd.run_chains(specs, 2, o, threads=len(specs))
+    assert one == many
+    assert all(e < 0 for e in one)
