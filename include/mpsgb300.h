@@ -152,6 +152,15 @@ int mpsg_svdtrunc(mpsg_ctx* ctx, const mpsg_tensor* a, int64_t maxdim, double to
 int mpsg_svdtrunc_gram(mpsg_ctx* ctx, const mpsg_tensor* a, int64_t maxdim, double tol,
                        double tieband, int32_t side, mpsg_tensor** u, mpsg_tensor** s,
                        mpsg_tensor** v);
+/* Complex _svd_ / svdtrunc for the complex MPS of time evolution (the reference factorises dense
+ * complex site tensors in src/tdvp.jl:35,61,132,165,195 with LAPACK; here per sector). The matrix is
+ * a_re + i a_im (same charge and spaces); the results are u = u_re + i u_im (isometric columns),
+ * s (real, diagonal) and v = v_re + i v_im holding V^H, so that A = u s v per sector. truncate = 0
+ * keeps every singular value (_svd_); otherwise the rule of mpsg_svdtrunc applies. */
+int mpsg_svd_complex(mpsg_ctx* ctx, const mpsg_tensor* a_re, const mpsg_tensor* a_im,
+                     int32_t truncate, int64_t maxdim, double tol, double tieband,
+                     mpsg_tensor** u_re, mpsg_tensor** u_im, mpsg_tensor** s,
+                     mpsg_tensor** v_re, mpsg_tensor** v_im);
 /* truncatedsizes (src/mpsutils.jl:89-112) on host arrays: nsect sectors, lens[i] descending values
  * each, concatenated in `values`; writes the kept count per sector to ns. */
 int mpsg_truncatedsizes(int32_t nsect, const int64_t* lens, const double* values, int64_t maxdim,

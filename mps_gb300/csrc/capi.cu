@@ -448,6 +448,29 @@ int mpsg_svdtrunc_gram(mpsg_ctx* ctx, const mpsg_tensor* a, int64_t maxdim, doub
   });
 }
 
+int mpsg_svd_complex(mpsg_ctx* ctx, const mpsg_tensor* a_re, const mpsg_tensor* a_im,
+                     int32_t truncate, int64_t maxdim, double tol, double tieband,
+                     mpsg_tensor** u_re, mpsg_tensor** u_im, mpsg_tensor** s,
+                     mpsg_tensor** v_re, mpsg_tensor** v_im) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(a_re, "a_re");
+    need(a_im, "a_im");
+    need(u_re, "u_re");
+    need(u_im, "u_im");
+    need(s, "s");
+    need(v_re, "v_re");
+    need(v_im, "v_im");
+    auto R = mpsg::svd_blocks_complex(&ctx->c, a_re->t, a_im->t, truncate != 0, maxdim, tol,
+                                      tieband);
+    *u_re = wrap(std::move(R.ure));
+    *u_im = wrap(std::move(R.uim));
+    *s = wrap(std::move(R.s));
+    *v_re = wrap(std::move(R.vre));
+    *v_im = wrap(std::move(R.vim));
+  });
+}
+
 int mpsg_truncatedsizes(int32_t nsect, const int64_t* lens, const double* values, int64_t maxdim,
                         double tol, double tieband, int64_t* ns) {
   return guarded([&] {

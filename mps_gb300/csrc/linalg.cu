@@ -117,6 +117,33 @@ __global__ void scale_cols_inv_kernel(double* __restrict__ X, const double* __re
 
 unsigned grid_for(int64_t n) { return (unsigned)std::min<int64_t>((n + 255) / 256, 1184); }
 
+// Complex block assembled from its real and imaginary planes (rows x cols, column-major):
+// dst = A, or A^T when trans, with the imaginary part multiplied by imsign (-1: conjugate).
+__global__ void interleave_kernel(double2* __restrict__ dst, const double* __restrict__ re,
+                                  const double* __restrict__ im, double imsign, int64_t rows,
+                                  int64_t cols, int trans) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = t / rows, i = t - j * rows;
+    const int64_t d = trans ? j + cols * i : t;
+    dst[d] = make_double2(re[t], imsign * im[t]);
+  }
+}
+
+// dst (rows x cols, column-major, split into planes) = op(src)(i, j): src[i + ld j], or
+// src[j + ld i] when trans; conjugated when conj.
+__global__ void cplx_extract_kernel(double* __restrict__ dre, double* __restrict__ dim,
+                                    const double2* __restrict__ src, int64_t rows, int64_t cols,
+                                    int64_t ld, int trans, int conj) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = t / rows, i = t - j * rows;
+    const double2 s = trans ? src[j + ld * i] : src[i + ld * j];
+    dre[t] = s.x;
+    dim[t] = conj ? -s.y : s.y;
+  }
+}
+
 struct BlockSVD {
   int c1, c2;
   int64_t M, N, k;
@@ -418,6 +445,158 @@ SVDResult svd_blocks(Context* ctx, const DeviceTensor& A, bool truncate, int64_t
                                                                B.V->ptr, r, B.N);
     MPSG_CUDA(cudaGetLastError());
     ctx->kernel_launches += 2;
+  }
+  return R;
+}
+
+// Complex per-sector SVD: the blocks are (re + i im), factorised with cuSOLVER's complex
+// QR-iteration SVD on the solver lanes; A = U S V^H per sector, and v holds V^H (the layout of
+// the real path, where v holds V^T). A wide block is factorised through A^H = U' S V'^H, so that
+// U = V' and V^H = U'^H.
+CSVDResult svd_blocks_complex(Context* ctx, const DeviceTensor& Are, const DeviceTensor& Aim,
+                              bool truncate, int64_t maxdim, double tol, double tieband) {
+  if (Are.meta.N() != 2) throw Error(kErrArgument, "svd needs a rank-2 tensor (SymMatrix)");
+  if (!same_meta(Are.meta, Aim.meta))
+    throw Error(kErrSpaceMismatch, "real and imaginary parts differ in charge or spaces");
+  if (Are.diag || Aim.diag) throw Error(kErrArgument, "complex svd of a diagonal tensor");
+  struct CBlock {
+    int c1, c2;
+    int64_t M, N, k;
+    std::shared_ptr<Buffer> work, U, VT, S, wbuf, rwork;
+    int lwork = 0;
+  };
+  const size_t nb = Are.meta.nblocks();
+  SolverLanes& L = lanes(ctx);
+  std::vector<CBlock> blocks(nb);
+  for (size_t b = 0; b < nb; ++b) {
+    CBlock& B = blocks[b];
+    B.c1 = Are.meta.sec.labels(b)[0];
+    B.c2 = Are.meta.sec.labels(b)[1];
+    B.M = Are.meta.sec.sizes(b)[0];
+    B.N = Are.meta.sec.sizes(b)[1];
+    B.k = std::min(B.M, B.N);
+    const int64_t m = std::max(B.M, B.N), n = B.k;
+    B.work = alloc_buffer(ctx, 2 * B.M * B.N);
+    B.U = alloc_buffer(ctx, 2 * m * n);
+    B.VT = alloc_buffer(ctx, 2 * n * n);
+    B.S = alloc_buffer(ctx, n);
+    B.rwork = alloc_buffer(ctx, std::max<int64_t>(n, 1));
+    MPSG_SOLVER(cusolverDnZgesvd_bufferSize(L.sol[0], (int)m, (int)n, &B.lwork));
+    B.wbuf = alloc_buffer(ctx, 2 * std::max(B.lwork, 1));
+  }
+  int* dinfo = nullptr;
+  if (nb) {
+    MPSG_CUDA(cudaMallocAsync((void**)&dinfo, sizeof(int) * nb, ctx->stream));
+    MPSG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * nb, ctx->stream));
+  }
+  std::vector<size_t> order(nb);
+  for (size_t b = 0; b < nb; ++b) order[b] = b;
+  auto cost = [&](size_t b) {
+    const double m = (double)std::max(blocks[b].M, blocks[b].N), n = (double)blocks[b].k;
+    return m * n * n + n * n * n;
+  };
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t x, size_t y) { return cost(x) > cost(y); });
+  MPSG_CUDA(cudaEventRecord(L.fork, ctx->stream));
+  double load[kLanes] = {0, 0, 0, 0};
+  bool used[kLanes] = {false, false, false, false};
+  for (size_t b : order) {
+    int lane = 0;
+    for (int i = 1; i < kLanes; ++i)
+      if (load[i] < load[lane]) lane = i;
+    if (!used[lane]) {
+      MPSG_CUDA(cudaStreamWaitEvent(L.st[lane], L.fork, 0));
+      used[lane] = true;
+    }
+    load[lane] += cost(b);
+    CBlock& B = blocks[b];
+    cudaStream_t st = L.st[lane];
+    const double* re = Are.data() + Are.meta.off[b];
+    const double* im = Aim.data() + Aim.meta.off[b];
+    auto* W = (cuDoubleComplex*)B.work->ptr;
+    auto* U = (cuDoubleComplex*)B.U->ptr;
+    auto* VT = (cuDoubleComplex*)B.VT->ptr;
+    auto* WB = (cuDoubleComplex*)B.wbuf->ptr;
+    const bool tall = B.M >= B.N;
+    // tall: work = A (M x N); wide: work = A^H (N x M)
+    interleave_kernel<<<grid_for(B.M * B.N), 256, 0, st>>>((double2*)W, re, im, tall ? 1.0 : -1.0,
+                                                          B.M, B.N, tall ? 0 : 1);
+    MPSG_CUDA(cudaGetLastError());
+    const int m = (int)std::max(B.M, B.N), n = (int)B.k;
+    MPSG_SOLVER(cusolverDnZgesvd(L.sol[lane], 'S', 'S', m, n, W, m, B.S->ptr, U, m, VT, n, WB,
+                                 B.lwork, B.rwork->ptr, dinfo + b));
+    ctx->kernel_launches += 1;
+  }
+  for (int i = 0; i < kLanes; ++i) {
+    if (!used[i]) continue;
+    MPSG_CUDA(cudaEventRecord(L.join[i], L.st[i]));
+    MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, L.join[i], 0));
+  }
+  std::vector<int> info(nb, 0);
+  std::vector<std::vector<double>> S(nb);
+  if (nb)
+    MPSG_CUDA(cudaMemcpyAsync(info.data(), dinfo, sizeof(int) * nb, cudaMemcpyDeviceToHost,
+                              ctx->stream));
+  for (size_t b = 0; b < nb; ++b) {
+    S[b].resize(blocks[b].k);
+    MPSG_CUDA(cudaMemcpyAsync(S[b].data(), blocks[b].S->ptr, sizeof(double) * blocks[b].k,
+                              cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (dinfo) cudaFreeAsync(dinfo, ctx->stream);
+  for (size_t b = 0; b < nb; ++b)
+    if (info[b] != 0) throw Error(kErrNoConvergence, "complex block SVD did not converge");
+  int64_t total = 0;
+  for (size_t b = 0; b < nb; ++b) total += blocks[b].k;
+  std::vector<int64_t> ns(nb);
+  const bool keep_all = tol <= 0.0 && maxdim >= total;
+  if (truncate && !keep_all) {
+    ns = truncatedsizes(S, maxdim, tol, tieband);
+  } else {
+    for (size_t b = 0; b < nb; ++b) ns[b] = blocks[b].k;
+  }
+  std::vector<std::pair<int, int64_t>> pl, pr;
+  CSVDResult R;
+  for (size_t b = 0; b < nb; ++b) {
+    if (ns[b] <= 0) continue;
+    pl.push_back({blocks[b].c1, ns[b]});
+    pr.push_back({blocks[b].c2, ns[b]});
+    R.singular_values.push_back(std::vector<double>(S[b].begin(), S[b].begin() + ns[b]));
+  }
+  if (pl.empty()) throw Error(kErrTolerance, "no singular value kept");
+  Space Vl = Space::make(pl, Are.meta.space[0].dual);
+  Space Vr = Space::make(pr, Are.meta.space[1].dual);
+  TensorMeta mu = TensorMeta::build(0, {Are.meta.space[0], dual_space(Vl)});
+  TensorMeta ms = TensorMeta::build(Are.meta.charge, {Vl, Vr});
+  TensorMeta mv = TensorMeta::build(0, {dual_space(Vr), Are.meta.space[1]});
+  R.ure = new_tensor(ctx, mu, false);
+  R.uim = new_tensor(ctx, mu, false);
+  R.s = new_tensor(ctx, ms, true);
+  R.s.diag = true;
+  R.vre = new_tensor(ctx, mv, false);
+  R.vim = new_tensor(ctx, mv, false);
+  for (size_t b = 0; b < nb; ++b) {
+    const int64_t r = ns[b];
+    if (r <= 0) continue;
+    const CBlock& B = blocks[b];
+    int su[2] = {B.c1, B.c1}, ss[2] = {B.c1, B.c2}, sv[2] = {B.c2, B.c2};
+    long iu = mu.find(su), is = ms.find(ss), iv = mv.find(sv);
+    if (iu < 0 || is < 0 || iv < 0) throw Error(kErrSpaceMismatch, "svd: output sector missing");
+    const auto* U = (const double2*)B.U->ptr;
+    const auto* VT = (const double2*)B.VT->ptr;
+    double *ure = R.ure.data() + mu.off[iu], *uim = R.uim.data() + mu.off[iu];
+    double *vre = R.vre.data() + mv.off[iv], *vim = R.vim.data() + mv.off[iv];
+    cudaStream_t st = ctx->stream;
+    if (B.M >= B.N) {  // u = U[:, :r] (M x r); v = VT[:r, :] (r x N)
+      cplx_extract_kernel<<<grid_for(B.M * r), 256, 0, st>>>(ure, uim, U, B.M, r, B.M, 0, 0);
+      cplx_extract_kernel<<<grid_for(r * B.N), 256, 0, st>>>(vre, vim, VT, r, B.N, B.N, 0, 0);
+    } else {  // u = (V'^H)^H[:, :r] from VT' (M x M); v = U'^H[:r, :] from U' (N x M)
+      cplx_extract_kernel<<<grid_for(B.M * r), 256, 0, st>>>(ure, uim, VT, B.M, r, B.M, 1, 1);
+      cplx_extract_kernel<<<grid_for(r * B.N), 256, 0, st>>>(vre, vim, U, r, B.N, B.N, 1, 1);
+    }
+    set_diag_kernel<<<1, 256, 0, st>>>(R.s.data() + ms.off[is], B.S->ptr, r);
+    MPSG_CUDA(cudaGetLastError());
+    ctx->kernel_launches += 3;
   }
   return R;
 }

@@ -26,6 +26,15 @@ enum SvdMethod { kSvdExact = 0, kSvdGramLeft = 1, kSvdGramRight = 2 };
 SVDResult svd_blocks(Context* ctx, const DeviceTensor& A, bool truncate, int64_t maxdim,
                      double tol, double tieband, int method = kSvdExact);
 
+// Complex per-sector SVD of (re + i im): A = u s v with u (re, im) isometric, s real diagonal
+// and v = V^H per sector; same truncation rule and output spaces as svd_blocks.
+struct CSVDResult {
+  DeviceTensor ure, uim, s, vre, vim;
+  std::vector<std::vector<double>> singular_values;
+};
+CSVDResult svd_blocks_complex(Context* ctx, const DeviceTensor& Are, const DeviceTensor& Aim,
+                              bool truncate, int64_t maxdim, double tol, double tieband);
+
 struct EigResult {
   double value = 0;
   DeviceTensor vec;

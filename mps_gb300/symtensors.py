@@ -24,7 +24,7 @@ __all__ = [
     "matmul", "contract", "contract_flops", "dot", "norm", "axpy", "axpby", "rmul", "mul",
     "similar", "copy", "fill_", "applymps2site", "applymps2site_flops", "mpsupdateleft",
     "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision", "_svd_",
-    "svdtrunc", "truncatedsizes", "small_eigh", "eigsolve_heff2", "EigInfo", "Heff2",
+    "svdtrunc", "svd_complex", "truncatedsizes", "small_eigh", "eigsolve_heff2", "EigInfo", "Heff2",
 ]
 
 
@@ -609,6 +609,19 @@ def svdtrunc(A: SymTensor, maxdim=None, tol: float = 1e-12, tieband: float = 0.0
              float(tieband), 0 if method == "gram_left" else 1, C.byref(u), C.byref(s),
              C.byref(v))
     return SymTensor(u, A.ctx), SymTensor(s, A.ctx), SymTensor(v, A.ctx)
+
+
+def svd_complex(Are: SymTensor, Aim: SymTensor, maxdim=None, tol: float = 0.0,
+                tieband: float = 0.0, truncate: bool = True):
+    """Per-sector SVD of the complex matrix Are + i Aim: (u_re, u_im, s, v_re, v_im) with
+    A = u s v per sector, u isometric, s real and v = V^H. ``truncate=False`` keeps every value
+    (``_svd_``); otherwise the rule of ``svdtrunc``."""
+    if maxdim is None:
+        maxdim = max(Are.size())
+    out = [C.c_void_p() for _ in range(5)]
+    call("mpsg_svd_complex", Are.ctx.handle, Are.handle, Aim.handle, 1 if truncate else 0,
+         int(maxdim), float(tol), float(tieband), *[C.byref(o) for o in out])
+    return tuple(SymTensor(o, Are.ctx) for o in out)
 
 
 def truncatedsizes(S, maxdim: int = 200, tol: float = 1e-14, tieband: float = 0.0):
