@@ -231,6 +231,16 @@ int mpsg_axpy(mpsg_ctx* ctx, double alpha, const mpsg_tensor* a, mpsg_tensor* b)
 int mpsg_axpby(mpsg_ctx* ctx, double alpha, const mpsg_tensor* a, double beta,
                mpsg_tensor* b);                                                  /* :299-308 */
 int mpsg_dot(mpsg_ctx* ctx, const mpsg_tensor* a, const mpsg_tensor* b, double* out); /* :314 */
+/* n dot products in one call, one synchronisation: out[i] = dot(a[i], b[i]), each pair similar.
+ * For Krylov bases, whose reorthogonalisation takes one dot per basis vector (KrylovKit's
+ * orthogonalizers behind eigsolve / exponentiate, src/tdvp.jl:27 and dmrg.jl:77). */
+int mpsg_dots(mpsg_ctx* ctx, int32_t n, const mpsg_tensor* const* a,
+              const mpsg_tensor* const* b, double* out);
+/* out <- sum_i c[i] * x[i] over n tensors similar to out, in one launch (out may be one of the
+ * x[i]): the multi-term axpy of the same reorthogonalisations (symtensor.jl:288-308 applied
+ * term by term in the reference). */
+int mpsg_lincomb(mpsg_ctx* ctx, int32_t n, const double* c, const mpsg_tensor* const* x,
+                 mpsg_tensor* out);
 int mpsg_norm(mpsg_ctx* ctx, const mpsg_tensor* a, double* out);                 /* :321-323 */
 
 #ifdef __cplusplus

@@ -88,6 +88,8 @@ SIGNATURES = {
     "mpsg_svdtrunc": [P, P, I64, F64, F64, PP, PP, PP],
     "mpsg_svdtrunc_gram": [P, P, I64, F64, F64, I32, PP, PP, PP],
     "mpsg_svd_complex": [P, P, P, I32, I64, F64, F64, PP, PP, PP, PP, PP],
+    "mpsg_dots": [P, I32, PP, PP, PF64],
+    "mpsg_lincomb": [P, I32, PF64, PP, P],
     "mpsg_truncatedsizes": [I32, PI64, PF64, I64, F64, F64, PI64],
     "mpsg_small_eigh": [I32, PF64, PF64, PF64],
     "mpsg_eigsolve_heff2": [P, P, P, P, P, P, I32, I32, F64, I32, PF64, PP, PF64, PI32, PI32,

@@ -760,6 +760,48 @@ int mpsg_axpby(mpsg_ctx* ctx, double alpha, const mpsg_tensor* a, double beta, m
   });
 }
 
+int mpsg_dots(mpsg_ctx* ctx, int32_t n, const mpsg_tensor* const* a,
+              const mpsg_tensor* const* b, double* out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    if (n < 0) throw mpsg::Error(mpsg::kErrArgument, "negative count");
+    if (n == 0) return;
+    need(a, "a");
+    need(b, "b");
+    need(out, "out");
+    std::vector<mpsg::VecPair> pairs((size_t)n);
+    for (int32_t i = 0; i < n; ++i) {
+      need(a[i], "a[i]");
+      need(b[i], "b[i]");
+      mpsg::require_similar(a[i]->t, b[i]->t, "The two SymTensors have to be similar to dot!");
+      pairs[i] = {a[i]->t.data(), b[i]->t.data(), a[i]->t.meta.total};
+    }
+    mpsg::dots_host(&ctx->c, pairs, out);
+  });
+}
+
+int mpsg_lincomb(mpsg_ctx* ctx, int32_t n, const double* c, const mpsg_tensor* const* x,
+                 mpsg_tensor* out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(out, "out");
+    if (n < 0) throw mpsg::Error(mpsg::kErrArgument, "negative count");
+    std::vector<const double*> xs((size_t)n);
+    std::vector<double> cs((size_t)n);
+    if (n) {
+      need(c, "c");
+      need(x, "x");
+    }
+    for (int32_t i = 0; i < n; ++i) {
+      need(x[i], "x[i]");
+      mpsg::require_similar(x[i]->t, out->t, "lincomb: the tensors are not similar!");
+      xs[i] = x[i]->t.data();
+      cs[i] = c[i];
+    }
+    mpsg::launch_lincomb(&ctx->c, out->t.meta.total, xs, cs, out->t.data());
+  });
+}
+
 int mpsg_dot(mpsg_ctx* ctx, const mpsg_tensor* a, const mpsg_tensor* b, double* out) {
   return guarded([&] {
     need(ctx, "ctx");

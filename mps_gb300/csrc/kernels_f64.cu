@@ -233,6 +233,43 @@ __global__ void __launch_bounds__(256) sum_partials_kernel(int np, const double*
   if (threadIdx.x == 0) *out = r;
 }
 
+// Batched dot products: blockIdx.y selects the pair; every pair gets the same fixed grid of
+// partial sums and one CTA per pair adds them in a fixed order (deterministic).
+__global__ void __launch_bounds__(256) dots_partial_kernel(const VecPair* __restrict__ pairs,
+                                                           double* __restrict__ partial) {
+  __shared__ double sh[8];
+  const VecPair p = pairs[blockIdx.y];
+  double v = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < p.n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    v = fma(p.x[i], p.y[i], v);
+  double r = block_sum(v, sh);
+  if (threadIdx.x == 0) partial[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = r;
+}
+
+__global__ void __launch_bounds__(256) dots_sum_kernel(int np, const double* __restrict__ p,
+                                                       double* __restrict__ out) {
+  __shared__ double sh[8];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) v += p[(int64_t)blockIdx.x * np + i];
+  double r = block_sum(v, sh);
+  if (threadIdx.x == 0) out[blockIdx.x] = r;
+}
+
+// y[e] = sum_i c[i] x_i[e]; one thread reads every operand of its element before writing it, so
+// y may be one of the operands
+__global__ void __launch_bounds__(256) lincomb_kernel(int64_t n, int m,
+                                                      const double* const* __restrict__ xs,
+                                                      const double* __restrict__ c,
+                                                      double* __restrict__ y) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int i = 0; i < m; ++i) s = fma(c[i], xs[i][e], s);
+    y[e] = s;
+  }
+}
+
 int vec_grid(Context* ctx, int64_t n) {
   int64_t g = (n + 255) / 256;
   return (int)std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * 4));
@@ -340,6 +377,50 @@ void launch_scale(Context* ctx, int64_t n, double a, const double* x, double* y)
   scale_kernel<<<vec_grid(ctx, n), 256, 0, ctx->stream>>>(n, a, x, y);
   MPSG_CUDA(cudaGetLastError());
   ctx->kernel_launches++;
+}
+
+void dots_host(Context* ctx, const std::vector<VecPair>& pairs, double* out) {
+  const int np = (int)pairs.size();
+  if (np == 0) return;
+  int64_t nmax = 1;
+  for (const VecPair& p : pairs) nmax = std::max(nmax, p.n);
+  const int g = std::min(vec_grid(ctx, nmax), 64);
+  cudaStream_t st = ctx->stream;
+  VecPair* d_pairs = nullptr;
+  double* d_part = nullptr;
+  MPSG_CUDA(cudaMallocAsync((void**)&d_pairs, sizeof(VecPair) * np, st));
+  MPSG_CUDA(cudaMallocAsync((void**)&d_part, sizeof(double) * ((int64_t)np * g + np), st));
+  MPSG_CUDA(cudaMemcpyAsync(d_pairs, pairs.data(), sizeof(VecPair) * np, cudaMemcpyHostToDevice,
+                            st));
+  double* d_out = d_part + (int64_t)np * g;
+  dots_partial_kernel<<<dim3((unsigned)g, (unsigned)np), 256, 0, st>>>(d_pairs, d_part);
+  dots_sum_kernel<<<(unsigned)np, 256, 0, st>>>(g, d_part, d_out);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches += 2;
+  MPSG_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * np, cudaMemcpyDeviceToHost, st));
+  MPSG_CUDA(cudaFreeAsync(d_pairs, st));
+  MPSG_CUDA(cudaFreeAsync(d_part, st));
+  MPSG_CUDA(cudaStreamSynchronize(st));
+}
+
+void launch_lincomb(Context* ctx, int64_t n, const std::vector<const double*>& xs,
+                    const std::vector<double>& c, double* y) {
+  const int m = (int)xs.size();
+  if (n == 0) return;
+  cudaStream_t st = ctx->stream;
+  const double** d_xs = nullptr;
+  double* d_c = nullptr;
+  MPSG_CUDA(cudaMallocAsync((void**)&d_xs, sizeof(double*) * std::max(m, 1), st));
+  MPSG_CUDA(cudaMallocAsync((void**)&d_c, sizeof(double) * std::max(m, 1), st));
+  if (m) {
+    MPSG_CUDA(cudaMemcpyAsync(d_xs, xs.data(), sizeof(double*) * m, cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(d_c, c.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+  }
+  lincomb_kernel<<<vec_grid(ctx, n), 256, 0, st>>>(n, m, d_xs, d_c, y);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches++;
+  MPSG_CUDA(cudaFreeAsync(d_xs, st));
+  MPSG_CUDA(cudaFreeAsync(d_c, st));
 }
 
 void launch_dot(Context* ctx, int64_t n, const double* x, const double* y, double* d_out) {

@@ -167,5 +167,15 @@ void launch_axpby(Context* ctx, int64_t n, double a, const double* x, double b, 
 void launch_scale(Context* ctx, int64_t n, double a, const double* x, double* y);
 // sum_i x_i*y_i into *out (device), deterministic two-pass reduction
 void launch_dot(Context* ctx, int64_t n, const double* x, const double* y, double* d_out);
+// Many dot products in one pair of launches; writes the host array out and synchronises.
+struct VecPair {
+  const double* x;
+  const double* y;
+  int64_t n;
+};
+void dots_host(Context* ctx, const std::vector<VecPair>& pairs, double* out);
+// y = sum_i c[i] xs[i] (elementwise, n elements; y may alias an operand)
+void launch_lincomb(Context* ctx, int64_t n, const std::vector<const double*>& xs,
+                    const std::vector<double>& c, double* y);
 
 }  // namespace mpsg

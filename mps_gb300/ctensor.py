@@ -31,7 +31,7 @@ class Ops:
     svd_complex(re, im, truncate, maxdim, tol, tieband) -> (ure, uim, s, vre, vim)."""
 
     def __init__(self, contract, dual, lincomb, dot, symmatrix, splitleg, matmul, space,
-                 svd_complex, download, fill, from_blocks, dual_space, fuselegs):
+                 svd_complex, download, fill, from_blocks, dual_space, fuselegs, dots=None):
         self.contract = contract
         self.dual = dual
         self.lincomb = lincomb
@@ -46,6 +46,8 @@ class Ops:
         self.from_blocks = from_blocks  # from_blocks(charge, spaces, {sector: block})
         self.dual_space = dual_space
         self.fuselegs = fuselegs        # fuselegs(A, l, n)
+        # dots([(a, b), ...]) -> [dot(a, b), ...] (one synchronisation when batched)
+        self.dots = dots if dots is not None else (lambda pairs: [dot(a, b) for a, b in pairs])
 
 
 def gpu_ops(precision: int = 0, ctx=None) -> Ops:
@@ -54,13 +56,11 @@ def gpu_ops(precision: int = 0, ctx=None) -> Ops:
     from . import symtensors as mg
 
     def lincomb(terms):
-        c0, T0 = terms[0]
-        out = mg.copy(T0)
-        if c0 != 1.0:
-            mg.rmul(out, c0)
-        for c, T in terms[1:]:
-            mg.axpy(c, T, out)
-        return out
+        out = mg.similar(terms[0][1])
+        return mg.lincomb([c for c, _ in terms], [T for _, T in terms], out)
+
+    def dots(pairs):
+        return mg.dots([a for a, _ in pairs], [b for _, b in pairs])
 
     def svdc(re, im, truncate, maxdim, tol, tieband):
         return mg.svd_complex(re, im, maxdim=maxdim, tol=tol, tieband=tieband,
@@ -70,7 +70,7 @@ def gpu_ops(precision: int = 0, ctx=None) -> Ops:
                lincomb, mg.dot, mg.SymMatrix, mg.splitleg,
                lambda A, B: mg.matmul(A, B, precision=0), lambda A: A.space, svdc,
                lambda A: A.to_flat(), lambda x, c, sp: mg.fill(x, c, sp, ctx),
-               lambda c, sp, b: mg.from_blocks(c, sp, b, ctx), mg.dual, mg.fuselegs)
+               lambda c, sp, b: mg.from_blocks(c, sp, b, ctx), mg.dual, mg.fuselegs, dots)
 
 
 class CTensor:
@@ -151,21 +151,37 @@ def clincomb(ops: Ops, terms) -> CTensor:
 
 def cdot(ops: Ops, A, B) -> complex:
     """<A|B> = sum conj(A) B."""
-    A, B = creal(A), creal(B)
-    re = ops.dot(A.re, B.re)
-    im = 0.0
-    if A.im is not None and B.im is not None:
-        re += A.sign * B.sign * ops.dot(A.im, B.im)
-    if B.im is not None:
-        im += B.sign * ops.dot(A.re, B.im)
-    if A.im is not None:
-        im -= A.sign * ops.dot(A.im, B.re)
-    return complex(re, im)
+    return cdots(ops, [A], B)[0]
+
+
+def cdots(ops: Ops, As, B):
+    """[<A|B> for A in As] with every real dot product in one batched call."""
+    B = creal(B)
+    pairs, plan = [], []
+    for A in As:
+        A = creal(A)
+        idx = []
+        for (x, y, coef, part) in ((A.re, B.re, 1.0, 0), (A.im, B.im, A.sign * B.sign, 0),
+                                   (A.re, B.im, B.sign, 1), (A.im, B.re, -A.sign, 1)):
+            if x is None or y is None:
+                continue
+            idx.append((len(pairs), coef, part))
+            pairs.append((x, y))
+        plan.append(idx)
+    vals = ops.dots(pairs) if pairs else []
+    out = []
+    for idx in plan:
+        z = [0.0, 0.0]
+        for k, coef, part in idx:
+            z[part] += coef * vals[k]
+        out.append(complex(z[0], z[1]))
+    return out
 
 
 def cnorm(ops: Ops, A) -> float:
     A = creal(A)
-    n2 = ops.dot(A.re, A.re) + (0.0 if A.im is None else ops.dot(A.im, A.im))
+    pairs = [(A.re, A.re)] + ([] if A.im is None else [(A.im, A.im)])
+    n2 = sum(ops.dots(pairs))
     return float(np.sqrt(max(n2, 0.0)))
 
 
@@ -254,7 +270,8 @@ def _expT(alphas, betas, tau):
 def exponentiate(ops: Ops, f, t, x, krylovdim: int = 30, tol: float = 1e-12,
                  maxiter: int = 100):
     """exp(t f) x for a Hermitian map f on complex tensors, t complex: Lanczos with full
-    reorthogonalisation (twice); the Krylov dimension is the first m whose a-posteriori error
+    reorthogonalisation (classical Gram-Schmidt, twice, with batched dot products); the Krylov
+    dimension is the first m whose a-posteriori error
     beta_m |e_m^T exp(tau T_m) e_1| |x| is within tol for the remaining time tau; when the full
     basis cannot reach that, the step is halved until it can and the integration restarts from
     the new vector. Returns (y, ExpInfo)."""
@@ -273,13 +290,13 @@ def exponentiate(ops: Ops, f, t, x, krylovdim: int = 30, tol: float = 1e-12,
         for j in range(krylovdim):
             w = f(V[j])
             numops += 1
-            a = cdot(ops, V[j], w).real
-            terms = [(1.0, w), (-a, V[j])]
-            if j > 0:
-                terms.append((-betas[j - 1], V[j - 1]))
-            w = clincomb(ops, terms)
-            for _ in range(2):
-                coef = [cdot(ops, u, w) for u in V]
+            # classical Gram-Schmidt against the whole basis, twice; the first pass's coefficient
+            # on V[j] is the Lanczos alpha (the others vanish in exact arithmetic)
+            a = 0.0
+            for rep in range(2):
+                coef = cdots(ops, V, w)
+                if rep == 0:
+                    a = coef[j].real
                 w = clincomb(ops, [(1.0, w)] + [(-cu, u) for cu, u in zip(coef, V)])
             b = cnorm(ops, w)
             alphas.append(a)

@@ -24,7 +24,8 @@ __all__ = [
     "matmul", "contract", "contract_flops", "dot", "norm", "axpy", "axpby", "rmul", "mul",
     "similar", "copy", "fill_", "applymps2site", "applymps2site_flops", "mpsupdateleft",
     "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision", "_svd_",
-    "svdtrunc", "svd_complex", "truncatedsizes", "small_eigh", "eigsolve_heff2", "EigInfo", "Heff2",
+    "svdtrunc", "svd_complex", "dots", "lincomb", "truncatedsizes", "small_eigh",
+    "eigsolve_heff2", "EigInfo", "Heff2",
 ]
 
 
@@ -676,6 +677,29 @@ def eigsolve_heff2(x0, envL, envR, W1, W2, krylovdim=5, maxiter=8, tol=1e-7, pre
 # ---------------------------------------------------------------------------------------------
 # vector operations (src/symtensor.jl:266-323)
 # ---------------------------------------------------------------------------------------------
+def dots(As, Bs):
+    """[dot(a, b) for a, b in zip(As, Bs)] in one library call (one synchronisation)."""
+    n = len(As)
+    if n != len(Bs):
+        raise MPSGError(_lib.ERR_ARGUMENT, "dots: length mismatch")
+    if n == 0:
+        return []
+    out = (C.c_double * n)()
+    ha = (C.c_void_p * n)(*[a.handle for a in As])
+    hb = (C.c_void_p * n)(*[b.handle for b in Bs])
+    call("mpsg_dots", As[0].ctx.handle, n, ha, hb, out)
+    return list(out)
+
+
+def lincomb(coeffs, Xs, out):
+    """out <- sum_i coeffs[i] * Xs[i] in one launch (out may be one of the Xs); returns out."""
+    n = len(Xs)
+    c = (C.c_double * max(n, 1))(*[float(x) for x in coeffs])
+    hx = (C.c_void_p * max(n, 1))(*[x.handle for x in Xs])
+    call("mpsg_lincomb", out.ctx.handle, n, c, hx, out.handle)
+    return out
+
+
 def dot(A, B) -> float:
     out = C.c_double()
     call("mpsg_dot", A.ctx.handle, A.handle, B.handle, C.byref(out))

@@ -13,8 +13,9 @@ package, not vendored and unpinned; the call sites are src/tdvp.jl:27,40,52,68,7
 basis with full reorthogonalisation; the exponential of the small tridiagonal matrix through
 its eigen-decomposition; the a-posteriori error beta_m |e_m^T exp(tau T) e_1| decides the
 Krylov dimension; a step that the full basis cannot take within tol is cut in halves. The
-library implements the same scheme, so results agree to rounding; parity against a Julia run is
-unpinned (Julia is absent).
+library implements the same scheme (its reorthogonalisation is classical Gram-Schmidt twice with
+batched dot products, this one modified Gram-Schmidt twice: both are full reorthogonalisation),
+so results agree to rounding; parity against a Julia run is unpinned (Julia is absent).
 
 Turning point of a sweep: the reference evolves the last site (1-site) or the last pair (2-site)
 once, by dt, between the left-to-right and the right-to-left half-sweeps (src/tdvp.jl:45-48,

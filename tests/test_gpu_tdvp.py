@@ -131,3 +131,23 @@ def test_gpu_tdvp_conservation_and_backend_agreement_on_a_truncated_chain():
         g = td.expectation(ops_g, As_g, {i: sz_g, j: sz_g})
         o = td.expectation(ops_o, As_o, {i: sz_o, j: sz_o})
         assert abs(g - o) < 1e-11
+
+
+def test_batched_dots_and_lincomb():
+    rng = np.random.default_rng(3)
+    V = U1Space((0, 5), (1, 7), (2, 3))
+    W = U1Space((0, 4), (1, 2), isdual=True)
+    ts = [rand_tensor(1, (V, W), rng) for _ in range(5)]
+    gs = [to_device(t) for t in ts]
+    got = mg.dots(gs[:4], gs[1:])
+    want = [float(np.vdot(st.flatten(a), st.flatten(b))) for a, b in zip(ts[:4], ts[1:])]
+    np.testing.assert_allclose(got, want, rtol=1e-14)
+    assert got == [mg.dot(a, b) for a, b in zip(gs[:4], gs[1:])]
+    c = [0.5, -2.0, 3.25]
+    out = mg.lincomb(c, gs[:3], mg.similar(gs[0]))
+    ref = sum(ci * st.flatten(t) for ci, t in zip(c, ts[:3]))
+    np.testing.assert_allclose(out.to_flat(), ref, rtol=1e-14, atol=1e-14)
+    mg.lincomb([1.0, -1.0], [gs[3], gs[4]], gs[3])  # out aliases an operand
+    np.testing.assert_allclose(gs[3].to_flat(), st.flatten(ts[3]) - st.flatten(ts[4]), atol=1e-14)
+    with pytest.raises(mg.SpaceMismatch):
+        mg.lincomb([1.0], [to_device(rand_tensor(0, (V, W), rng))], gs[0])
