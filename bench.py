@@ -401,6 +401,21 @@ def run_ours(args):
             "executed_frac": achieved * pairs / peak if achieved else None,
             "traffic": profile_traffic(f"gemm_p{S}_chi{args.chi}")}
     share = {k: round(v_[0] / args.steps / step_ms, 4) for k, v_ in kinds.items() if v_[1]}
+    # HBM rooflines of the memory-bound kernels of one application: algorithmic bytes (copies:
+    # 8 read + 8 written per element moved; packing: 8 + 8 read + 2 S written per element) over
+    # their CUDA-event time, against the measured copy bandwidth
+    hbm = peaks["hbm_gbs"] if peaks else 6800.0
+    mem_roof = {}
+    if S:
+        copy_b, pack_b = op.traffic()
+        for name, nbytes, ks in (("permute", copy_b, ("copy",)),
+                                 ("pack", pack_b, ("pack", "pack_slices"))):
+            ms_k = sum(kinds[k][0] for k in ks) / args.steps
+            if ms_k > 0 and nbytes > 0:
+                gbs = nbytes / (ms_k / 1e3) / 1e9
+                mem_roof[name] = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                                  "frac": gbs / hbm, "bytes_per_step": nbytes,
+                                  "ms_per_step": ms_k}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -421,6 +436,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "kernel_share_of_step": share,
         "roofline": roof,
+        "memory_rooflines": mem_roof,
         "clocks": clocks,
     }
     if rank == 0 and not args.no_sweep and ws == 1:

@@ -216,6 +216,10 @@ int mpsg_heff2_create(mpsg_ctx* ctx, const mpsg_tensor* v_like, const mpsg_tenso
 int mpsg_heff2_apply(mpsg_ctx* ctx, mpsg_heff* op, const mpsg_tensor* v, mpsg_tensor** out);
 /* Algorithmic flops of one application in the reference contraction order. */
 int mpsg_heff2_flops(const mpsg_heff* op, double* flops);
+/* Algorithmic bytes per application of a prepared split-precision operator: block-permute
+ * copies (8 read + 8 written per element moved) and operand packing (exponent pass 8 read, slice
+ * pass 8 read + 2 S written per element); 0 for precision 0. For HBM rooflines of those kernels. */
+int mpsg_heff2_traffic(const mpsg_heff* op, double* copy_bytes, double* pack_bytes);
 int mpsg_heff2_free(mpsg_heff* op);
 /* Host self-check of the tensor-core H_eff plans for these structures (any tensors, also
  * structure-only ones): every copy and GEMM window in bounds, every output element written

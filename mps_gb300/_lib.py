@@ -96,6 +96,7 @@ SIGNATURES = {
                             PI32],
     "mpsg_heff2_create": [P, P, P, P, P, P, I32, PP],
     "mpsg_heff2_apply": [P, P, P, PP],
+    "mpsg_heff2_traffic": [P, PF64, PF64],
     "mpsg_heff2_flops": [P, PF64],
     "mpsg_heff2_free": [P],
     "mpsg_plan_heff2_check": [P, P, P, P, P],

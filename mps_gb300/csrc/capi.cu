@@ -570,6 +570,14 @@ int mpsg_heff2_flops(const mpsg_heff* op, double* flops) {
   });
 }
 
+int mpsg_heff2_traffic(const mpsg_heff* op, double* copy_bytes, double* pack_bytes) {
+  return guarded([&] {
+    need(op, "op");
+    if (copy_bytes) *copy_bytes = op->op->copy_bytes;
+    if (pack_bytes) *pack_bytes = op->op->pack_bytes;
+  });
+}
+
 int mpsg_heff2_free(mpsg_heff* op) {
   return guarded([&] { delete op; });
 }

@@ -477,6 +477,9 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
   // constant operands: fuse once, slice once
   DevContract& c1 = *op->plans->c1;
   DevContract& c2 = *op->plans->c2;
+  op->copy_bytes = 16.0 * (double)(c1.fb.elems + op->plans->x2a.elems + c2.split.elems);
+  op->pack_bytes = (16.0 + 2.0 * precision) *
+                   (double)(c1.host->fb.out.total + c2.host->fa.out.total);
   op->fusedA1 = alloc_buffer(ctx, c1.host->fa.out.total);
   launch_copy(ctx, c1.fa, op->envLW.data(), op->fusedA1->ptr);
   op->fusedB2 = alloc_buffer(ctx, c2.host->fb.out.total);

@@ -70,6 +70,9 @@ struct HeffOp {
   std::string plan_key;
   std::shared_ptr<Buffer> fusedA1, fusedB2;
   double ref_flops = 0;  // algorithmic flops of the reference contraction order
+  // algorithmic bytes per application (precision >= 2): block-permute copies (8 read + 8 written
+  // per element) and operand packing (exponent pass 8 read, slice pass 8 read + 2 S written)
+  double copy_bytes = 0, pack_bytes = 0;
   ~HeffOp();             // hands `plans` back to the context's cache
 };
 

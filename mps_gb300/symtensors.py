@@ -544,6 +544,13 @@ class Heff2:
         call("mpsg_heff2_flops", self._h, C.byref(f))
         return f.value
 
+    def traffic(self):
+        """(copy bytes, packing bytes) per application: the algorithmic HBM traffic of the
+        block-permute copies and of the operand packing (split-precision operators)."""
+        c, p = C.c_double(), C.c_double()
+        call("mpsg_heff2_traffic", self._h, C.byref(c), C.byref(p))
+        return c.value, p.value
+
     def __del__(self):
         try:
             if self._h:
