@@ -483,6 +483,16 @@ def run_gradient(args):
     grads = [g(A) for A in mps.As]
     ctx.synchronize()
     t_grad = time.perf_counter() - t0
+    # the same gradients keeping only every ceil(sqrt(L))-th environment (recomputed per segment)
+    import math
+    t0 = time.perf_counter()
+    Ec, gc = gr.energy_gradients_checkpointed(mps.As, Ws)
+    dEd_c = gr.xxz_delta_derivative(gc, Ws, lx)
+    ctx.synchronize()
+    t_ckpt = time.perf_counter() - t0
+    ckpt_rel = max(float(np.linalg.norm(gc(A).to_flat() - gA.to_flat())
+                         / max(np.linalg.norm(gA.to_flat()), 1e-300))
+                   for A, gA in zip(mps.As, grads))
     h = 1e-5
     ep = gr.energy_gradients(mps.As, gd.xxz_u1mpo(lx, delta + h, ctx=ctx))[0]
     em = gr.energy_gradients(mps.As, gd.xxz_u1mpo(lx, delta - h, ctx=ctx))[0]
@@ -498,6 +508,9 @@ def run_gradient(args):
                    "dtype": "f64"},
         "energy": E, "dE_dDelta": dEd, "dE_dDelta_fd": fd, "fd_abs_diff": abs(dEd - fd),
         "center_stationarity_relerr": stat, "dmrg_s": t_dmrg, "last_sweep_energy": es[-1],
+        "checkpointed": {"s": t_ckpt, "every": math.ceil(math.sqrt(lx)),
+                         "dE_dDelta": dEd_c, "max_rel_diff_dA": ckpt_rel,
+                         "energy_abs_diff": abs(Ec - E)},
     }
     print(json.dumps(line), flush=True)
 

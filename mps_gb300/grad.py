@@ -145,13 +145,75 @@ def xxz_delta_derivative(g, Ws, lx):
     return total
 
 
+def _left_update(contract, dual, L, A, W):
+    """One left environment update (src/apply.jl:49-58) with the given contract / dual."""
+    t = contract(L, (-1, 3, 4), A, (-1, 2, 1))
+    t = contract(t, (1, -1, -2, 4), W, (-2, 2, 3, -1))
+    return contract(t, (1, -1, 2, -2), dual(A), (-2, -1, 3))
+
+
+def checkpointed_gradients(be: Backend, As, Ws, Lb, Rb, every: int | None = None):
+    """<psi|O|psi> and the cotangent map of every site and MPO tensor, keeping only every
+    ``every``-th left environment (default ceil(sqrt(L))) instead of all of them and every
+    intermediate: the backward sweep recomputes one segment at a time from its checkpoint on a
+    fresh tape and propagates the environment cotangent to the previous checkpoint. Memory is
+    O(L / every + every) environments instead of O(3 L); the extra cost is one more forward
+    sweep. Results equal ``mpo_expectation`` + ``Tape.backward`` (same contractions)."""
+    import math
+    lx = len(As)
+    k = every if every else max(1, math.ceil(math.sqrt(lx)))
+    ckpt = {0: Lb}
+    L = Lb
+    for x in range(lx):
+        L = _left_update(be.contract, be.dual, L, As[x], Ws[x])
+        if (x + 1) % k == 0 and x + 1 < lx:
+            ckpt[x + 1] = L
+    E = be.contract(L, (-1, -2, -3), Rb, (-1, -2, -3))
+    dL = _vjp_one(be, (-1, -2, -3), Rb, (-1, -2, -3), 1.0)
+    del L
+    grads = {}
+
+    def acc(x, g):
+        if g is None:
+            return
+        k_ = id(x)
+        grads[k_] = g if k_ not in grads else be.axpy(1.0, g, be.scaled(grads[k_], 1.0))
+
+    end = lx
+    for c in sorted(ckpt, reverse=True):
+        tape = Tape(be)
+        L = ckpt.pop(c)
+        L0 = L
+        for x in range(c, end):
+            L = _left_update(tape.contract, tape.dual, L, As[x], Ws[x])
+        g = tape.backward(L, dL)
+        for x in range(c, end):
+            if id(As[x]) not in {id(a) for a in As[x + 1:end]}:  # once per object per segment
+                acc(As[x], g(As[x]))
+        for W in {id(w): w for w in Ws[c:end]}.values():
+            acc(W, g(W))
+        dL = g(L0)
+        end = c
+    return float(E), lambda t: grads.get(id(t))
+
+
+def energy_gradients_checkpointed(As, Ws, every: int | None = None):
+    """``energy_gradients`` with checkpointed environments on the GPU library."""
+    from . import symtensors as mg
+    from .symtensors import dual as dsp
+    ctx = As[0].ctx
+    lVa, rVa = As[0].space[0], dsp(As[-1].space[2])
+    lVw, rVw = Ws[0].space[0], dsp(Ws[-1].space[2])
+    Lb = mg.fill(1.0, 0, (dsp(lVa), dsp(lVw), lVa), ctx)
+    Rb = mg.fill(1.0, 0, (rVa, rVw, dsp(rVa)), ctx)
+    return checkpointed_gradients(gpu_backend(), As, Ws, Lb, Rb, every)
+
+
 def mpo_expectation(tape: Tape, As, Ws, Lb, Rb):
     """<psi|O|psi> for the MPS tensors As (legs (Vl, d, dual(Vr))) and the MPO Ws by left
     environment updates (src/apply.jl:49-58) from the boundary Lb, closed with Rb. Every
     environment is kept on the tape."""
     L = Lb
     for A, W in zip(As, Ws):
-        t = tape.contract(L, (-1, 3, 4), A, (-1, 2, 1))
-        t = tape.contract(t, (1, -1, -2, 4), W, (-2, 2, 3, -1))
-        L = tape.contract(t, (1, -1, 2, -2), tape.dual(A), (-2, -1, 3))
+        L = _left_update(tape.contract, tape.dual, L, A, W)
     return tape.contract(L, (-1, -2, -3), Rb, (-1, -2, -3))

@@ -61,3 +61,8 @@ def test_gpu_energy_gradient_delta_and_site_tensors():
     # a converged state is stationary: dE/dA_l = 2 E A_l at the normalised center (l = 1)
     gA = g(mps.As[0])
     assert relerr(gA.to_flat(), 2 * E * mps.As[0].to_flat()) < 1e-6
+    # the checkpointed backward sweep (environments recomputed per segment) gives the same
+    E2, g2 = gr.energy_gradients_checkpointed(mps.As, Ws, every=4)
+    assert abs(E2 - E) < 1e-12 * abs(E)
+    for X in list(mps.As) + list({id(w): w for w in Ws}.values()):
+        assert relerr(g2(X).to_flat(), g(X).to_flat()) < 1e-12
