@@ -530,7 +530,7 @@ def run_cylinder(args):
     Ws = lt.device_mpo(n, lt.cylinder_heisenberg_terms(width, length), ctx=ctx)
     mps = gd.mps_from_host(gd.binomial_mps_host(n, n // 2, chi, 13), ctx)
     t0 = time.perf_counter()
-    gd.center_at(mps, 1, svd="gram")
+    gd.center_at(mps, 1, svd="gram", normalize=True)  # 144 random sites: keep the norm at 1
     env = gd.initialenv(mps, Ws)
     ctx.synchronize()
     t_init = time.perf_counter() - t0

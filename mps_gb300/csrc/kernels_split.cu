@@ -955,6 +955,17 @@ static void make_map(CUtensorMap* map, void* base, int64_t rows_total, int S, in
 
 int chunk_for(int S) { return exact_chunk(S); }
 
+}  // namespace split
+
+size_t DevGemmPlan::device_bytes() const {
+  size_t b = 0;
+  for (const auto& sp : splitp)
+    if (sp) b += (size_t)sp->S * (size_t)(sp->rowsA + sp->rowsB) * 128;
+  return b;
+}
+
+namespace split {
+
 void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   release();
   S = S_;

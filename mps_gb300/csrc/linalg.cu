@@ -393,9 +393,35 @@ SVDResult svd_blocks(Context* ctx, const DeviceTensor& A, bool truncate, int64_t
   if (dinfo) cudaFreeAsync(dinfo, ctx->stream);
   for (size_t b = 0; b < nb; ++b) {
     if (info[b] == 0) continue;
-    if (method != kSvdExact)
-      throw Error(kErrNoConvergence, "symmetric eigensolver of a Gram block did not converge");
-    run_jacobi(ctx, A.data() + A.meta.off[b], blocks[b]);
+    if (method != kSvdExact) {
+      // the Gram eigensolver failed on this block: factorise it exactly instead (QR-iteration
+      // SVD, then Jacobi), which also leaves u and v orthonormal with u s v = A
+      BlockSVD E;
+      E.c1 = blocks[b].c1;
+      E.c2 = blocks[b].c2;
+      E.M = blocks[b].M;
+      E.N = blocks[b].N;
+      E.k = blocks[b].k;
+      prepare_exact(ctx, L.sol[0], E);
+      int* d1 = nullptr;
+      MPSG_CUDA(cudaMallocAsync((void**)&d1, sizeof(int), ctx->stream));
+      MPSG_CUDA(cudaMemsetAsync(d1, 0, sizeof(int), ctx->stream));
+      MPSG_CUDA(cudaEventRecord(L.fork, ctx->stream));
+      MPSG_CUDA(cudaStreamWaitEvent(L.st[0], L.fork, 0));
+      run_exact(ctx, L.st[0], L.sol[0], A.data() + A.meta.off[b], E, d1);
+      MPSG_CUDA(cudaEventRecord(L.join[0], L.st[0]));
+      MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, L.join[0], 0));
+      int i1 = 0;
+      MPSG_CUDA(cudaMemcpyAsync(&i1, d1, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+      cudaFreeAsync(d1, ctx->stream);
+      if (i1 != 0) run_jacobi(ctx, A.data() + A.meta.off[b], E);
+      blocks[b].U = E.U;
+      blocks[b].S = E.S;
+      blocks[b].V = E.V;
+    } else {
+      run_jacobi(ctx, A.data() + A.meta.off[b], blocks[b]);
+    }
     MPSG_CUDA(cudaMemcpy(S[b].data(), blocks[b].S->ptr, sizeof(double) * blocks[b].k,
                          cudaMemcpyDeviceToHost));
   }

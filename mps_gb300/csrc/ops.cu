@@ -226,6 +226,9 @@ static void run_gemm(Context* ctx, DevGemmPlan& g, const double* A, const double
   if (!sp) {
     sp = std::make_shared<split::SplitPlan>();
     sp->build(ctx, g.host, precision);
+    // the new scratch counts against the plan caches' budgets (the caller holds `g`)
+    ctx->contract_cache.trim();
+    ctx->matmul_cache.trim();
   }
   split::launch_split_gemm(ctx, *sp, A, B, C);
 }
@@ -234,15 +237,12 @@ DeviceTensor matmul(Context* ctx, const DeviceTensor& a, const DeviceTensor& b, 
   std::string key = "G|" + meta_key(a.meta) + "*" + meta_key(b.meta);
   std::shared_ptr<DevGemmPlan> g;
   std::shared_ptr<TensorMeta> outmeta;
-  auto it = ctx->matmul_cache.find(key);
-  MatmulPlan mp;
-  if (it == ctx->matmul_cache.end()) {
-    mp = plan_matmul(a.meta, b.meta);
+  g = ctx->matmul_cache.get(key);
+  if (!g) {
+    MatmulPlan mp = plan_matmul(a.meta, b.meta);
     g = std::make_shared<DevGemmPlan>();
     g->upload(mp.gemms, mp.flops, ctx->stream);
-    ctx->matmul_cache[key] = g;
-  } else {
-    g = it->second;
+    ctx->matmul_cache.put(key, g);
   }
   DeviceTensor t;
   t.ctx = ctx;
@@ -260,8 +260,7 @@ std::shared_ptr<DevContract> get_contract_plan(Context* ctx, const TensorMeta& A
                                                const TensorMeta& B,
                                                const std::vector<int>& idxB) {
   std::string key = "C|" + meta_key(A) + vkey(idxA) + "|" + meta_key(B) + vkey(idxB);
-  auto it = ctx->contract_cache.find(key);
-  if (it != ctx->contract_cache.end()) return it->second;
+  if (auto hit = ctx->contract_cache.get(key)) return hit;
   auto p = std::make_shared<DevContract>();
   p->host = plan_contract(A, idxA, B, idxB);
   if (!p->host->scalar) {
@@ -270,7 +269,7 @@ std::shared_ptr<DevContract> get_contract_plan(Context* ctx, const TensorMeta& A
     p->mm.upload(p->host->mm.gemms, p->host->mm.flops, ctx->stream);
     p->split.upload(p->host->split.tasks, p->host->split.identity, ctx->stream);
   }
-  ctx->contract_cache[key] = p;
+  ctx->contract_cache.put(key, p);
   return p;
 }
 

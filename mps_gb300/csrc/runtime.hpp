@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <list>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -86,6 +87,7 @@ struct DevGemmPlan {
   std::vector<GemmTask> host;
   std::shared_ptr<split::SplitPlan> splitp[8];  // split-precision plans by slice count
   cudaStream_t stream = nullptr;  // tables are allocated and freed in this stream's order
+  size_t device_bytes() const;    // packed-slice scratch of the split plans (the bulk)
   void upload(const std::vector<GemmTask>& g, double flops_, cudaStream_t st);
   // Host half of upload: every field except the device pointers, plus the per-part tables.
   void build_host(const std::vector<GemmTask>& g, double flops_, GemmTables& t);
@@ -96,7 +98,46 @@ struct DevContract {
   std::shared_ptr<ContractPlan> host;
   DevCopyPlan fa, fb, split;
   DevGemmPlan mm;
+  size_t device_bytes() const { return mm.device_bytes(); }
   ~DevContract();
+};
+
+// Plans by structure key, least recently used first, trimmed to a device-byte budget (split
+// plans carry packed operand scratch as large as their operands, and a sweep meets a new
+// structure at every bond). Entries are shared: evicting one that a caller still holds only
+// drops the cache's reference.
+template <class T>
+struct PlanCache {
+  size_t budget = size_t(16) << 30;
+  std::list<std::string> order;
+  std::unordered_map<std::string, std::pair<std::shared_ptr<T>, std::list<std::string>::iterator>>
+      map;
+  std::shared_ptr<T> get(const std::string& k) {
+    auto it = map.find(k);
+    if (it == map.end()) return nullptr;
+    order.splice(order.end(), order, it->second.second);
+    return it->second.first;
+  }
+  void put(const std::string& k, std::shared_ptr<T> v) {
+    order.push_back(k);
+    map[k] = {std::move(v), std::prev(order.end())};
+    trim();
+  }
+  // evict least recently used entries (never the most recent one) while over budget
+  void trim() {
+    size_t total = 0;
+    for (const auto& e : map) total += e.second.first->device_bytes();
+    while (total > budget && order.size() > 1) {
+      auto it = map.find(order.front());
+      total -= it->second.first->device_bytes();
+      map.erase(it);
+      order.pop_front();
+    }
+  }
+  void clear() {
+    map.clear();
+    order.clear();
+  }
 };
 
 struct DevReleg {
@@ -111,9 +152,9 @@ struct Context : std::enable_shared_from_this<Context> {
   cudaStream_t stream = nullptr;
   double* d_partials = nullptr;   // reduction partials (one per CTA of a reduction launch)
   double* h_pinned = nullptr;     // small pinned host scratch for scalar results
-  std::unordered_map<std::string, std::shared_ptr<DevContract>> contract_cache;
+  PlanCache<DevContract> contract_cache;
   std::unordered_map<std::string, std::shared_ptr<DevReleg>> releg_cache;
-  std::unordered_map<std::string, std::shared_ptr<DevGemmPlan>> matmul_cache;
+  PlanCache<DevGemmPlan> matmul_cache;
   // idle prepared-H_eff plans by structure + precision, least recently returned first
   std::unordered_map<std::string, std::shared_ptr<HeffPlans>> heff_cache;
   std::vector<std::string> heff_lru;

@@ -227,34 +227,42 @@ def _factor(M, keep, svd):
     return mg.svdtrunc(M, maxdim=max(M.size()), tol=0.0, method="gram_" + keep)
 
 
-def _pushleft(mps: MPState, l: int, svd="exact"):
+def _pushleft(mps: MPState, l: int, svd="exact", normalize=False):
     """``_pushleft!`` (src/symmps.jl:167-174), 1-based ``l``."""
     A = mps.As[l - 1]
     u, s, v = _factor(mg.fuselegs(A, 2, 2), "right", svd)
+    if normalize:
+        mg.rmul(s, 1.0 / mg.norm(s))
     mps.As[l - 1] = mg.splitleg(v, 2, A.space[1:3])
     mps.As[l - 2] = mg.contract(mps.As[l - 2], (1, 2, -1), mg.matmul(u, s, precision=0), (-1, 3),
                                 precision=0)
 
 
-def _pushright(mps: MPState, l: int, svd="exact"):
+def _pushright(mps: MPState, l: int, svd="exact", normalize=False):
     """``_pushright!`` (src/symmps.jl:176-183)."""
     A = mps.As[l - 1]
     u, s, v = _factor(mg.fuselegs(A, 1, 2), "left", svd)
+    if normalize:
+        mg.rmul(s, 1.0 / mg.norm(s))
     mps.As[l - 1] = mg.splitleg(u, 1, A.space[0:2])
     mps.As[l] = mg.contract(mg.matmul(s, v, precision=0), (1, -1), mps.As[l], (-1, 2, 3),
                             precision=0)
 
 
-def center_at(mps: MPState, center: int, svd: str = "exact") -> MPState:
+def center_at(mps: MPState, center: int, svd: str = "exact",
+              normalize: bool = False) -> MPState:
     """``center_at!`` (src/symmps.jl:185-200). ``svd="gram"`` canonicalises with the
-    density-matrix factorisation (same bond spaces, orthonormal site tensors)."""
+    density-matrix factorisation (same bond spaces, orthonormal site tensors). ``normalize``
+    rescales the singular values passed on at every step to unit norm: the state keeps its
+    direction while its norm, which for a long random MPS grows or shrinks geometrically (and
+    whose Gram matrices square it), stays 1."""
     x1, xL = 1, len(mps)
     if mps.center > 0:
         x1 = xL = mps.center
     for p in range(x1, center):
-        _pushright(mps, p, svd)
+        _pushright(mps, p, svd, normalize)
     for p in range(xL, center, -1):
-        _pushleft(mps, p, svd)
+        _pushleft(mps, p, svd, normalize)
     mps.center = center
     return mps
 
