@@ -68,6 +68,8 @@ def parse():
                         "Delta derivative of a two-point function by central differences")
     p.add_argument("--tdvp-lx", type=int, default=32)
     p.add_argument("--tdvp-steps", type=int, default=10)
+    p.add_argument("--tdvp-precision", type=int, default=0,
+                   help="block-GEMM arithmetic of the TDVP contractions (0 = FP64, S = slices)")
     return p.parse_args()
 
 
@@ -600,7 +602,7 @@ def run_tdvp(args):
     lx, chi, delta, dt, h = args.tdvp_lx, args.sweep_chi or 64, 0.5, 0.05, 1e-5
     steps = args.tdvp_steps
     ctx = mg.get_context(0)
-    ops = ct.gpu_ops(0, ctx)
+    ops = ct.gpu_ops(args.tdvp_precision, ctx)
     host = gd.binomial_mps_host(lx, lx // 2, chi, 17)
     i = lx // 2
     sz = td.site_operator(ops, mg.VectorSpace(gd.SITE), {0: -0.5, 1: 0.5})
@@ -638,7 +640,9 @@ def run_tdvp(args):
         "data": "synthetic (seeded Philox N(0,1) initial MPS)",
         "config": {"workload": f"XXZ chain L={lx}, Delta={delta}, binomial bond profile ~{chi}, "
                                f"{steps} sweeps of dt={dt} (each sweep evolves by 2 dt), "
-                               "Krylov tol 1e-12, dim <= 30", "dtype": "complex f64"},
+                               "Krylov tol 1e-12, dim <= 30",
+                   "dtype": "complex f64" + (f" via {args.tdvp_precision} bf16 slices"
+                                             if args.tdvp_precision else "")},
         "t": 2 * dt * steps, "C_t": r0["C"], "dC_dDelta_fd": (rp["C"] - rm["C"]) / (2 * h),
         "norm_drift": r0["norm_drift"], "energy_drift": r0["energy_drift"],
         "matvecs_per_sweep": r0["matvecs"] / steps, "unconverged_exponentials": r0["unconverged"],
