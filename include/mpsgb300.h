@@ -105,6 +105,17 @@ int mpsg_matmul(mpsg_ctx* ctx, const mpsg_tensor* a, const mpsg_tensor* b, int32
  * *scalar and *out is set to NULL. */
 int mpsg_contract(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa, const mpsg_tensor* b,
                   const int32_t* idxb, int32_t precision, mpsg_tensor** out, double* scalar);
+/* contract for complex operands held as real and imaginary parts (a = ar + i sa ai, b = br +
+ * i sb bi; ai or bi may be NULL for a real operand; sa, sb = +-1 fold a conjugation in): up to
+ * four real contractions on one plan, combined in place, so c = cr + i ci (ci NULL when both
+ * operands are real). A full contraction returns the complex number in scalar_re, scalar_im with
+ * cr = ci = NULL. For the complex MPS of time evolution (src/tdvp.jl, whose @tensor contractions
+ * this replaces). */
+int mpsg_contract_complex(mpsg_ctx* ctx, const mpsg_tensor* ar, const mpsg_tensor* ai,
+                          double sa, const int32_t* idxa, const mpsg_tensor* br,
+                          const mpsg_tensor* bi, double sb, const int32_t* idxb,
+                          int32_t precision, mpsg_tensor** cr, mpsg_tensor** ci,
+                          double* scalar_re, double* scalar_im);
 /* The same FP64 contraction into a caller-provided result, allocating no device memory (no
  * counterpart in the reference). For hosts that cannot let a library allocate during a call,
  * e.g. one that handed the GPU's memory to its own arena up front. `out` must already exist

@@ -332,6 +332,56 @@ int mpsg_contract(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa, cons
   });
 }
 
+int mpsg_contract_complex(mpsg_ctx* ctx, const mpsg_tensor* ar, const mpsg_tensor* ai,
+                          double sa, const int32_t* idxa, const mpsg_tensor* br,
+                          const mpsg_tensor* bi, double sb, const int32_t* idxb,
+                          int32_t precision, mpsg_tensor** cr, mpsg_tensor** ci,
+                          double* scalar_re, double* scalar_im) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(ar, "ar");
+    need(br, "br");
+    need(idxa, "idxa");
+    need(idxb, "idxb");
+    need(cr, "cr");
+    need(ci, "ci");
+    if (ai) mpsg::require_similar(ar->t, ai->t, "real and imaginary parts differ in structure");
+    if (bi) mpsg::require_similar(br->t, bi->t, "real and imaginary parts differ in structure");
+    mpsg::Context* c = &ctx->c;
+    const auto ia = ivec(idxa, ar->t.meta.N());
+    const auto ib = ivec(idxb, br->t.meta.N());
+    double srr = 0, sri = 0, sir = 0, sii = 0;
+    mpsg::DeviceTensor rr = mpsg::contract(c, ar->t, ia, br->t, ib, precision, &srr);
+    mpsg::DeviceTensor ri, ir, ii;
+    if (bi) ri = mpsg::contract(c, ar->t, ia, bi->t, ib, precision, &sri);
+    if (ai) ir = mpsg::contract(c, ai->t, ia, br->t, ib, precision, &sir);
+    if (ai && bi) ii = mpsg::contract(c, ai->t, ia, bi->t, ib, precision, &sii);
+    if (!rr.buf && rr.meta.space.empty()) {  // every leg contracted: a complex number
+      *cr = nullptr;
+      *ci = nullptr;
+      if (scalar_re) *scalar_re = srr - sa * sb * sii;
+      if (scalar_im) *scalar_im = sb * sri + sa * sir;
+      return;
+    }
+    const int64_t n = rr.meta.total;
+    // re = rr - sa sb ii, im = sb ri + sa ir, both formed in place in one launch each
+    if (ai && bi) mpsg::launch_lincomb(c, n, {rr.data(), ii.data()}, {1.0, -sa * sb}, rr.data());
+    *cr = wrap(std::move(rr));
+    if (ri.buf && ir.buf) {
+      mpsg::launch_lincomb(c, n, {ri.data(), ir.data()}, {sb, sa}, ri.data());
+      *ci = wrap(std::move(ri));
+    } else if (ri.buf) {
+      if (sb != 1.0) mpsg::launch_lincomb(c, n, {ri.data()}, {sb}, ri.data());
+      *ci = wrap(std::move(ri));
+    } else if (ir.buf) {
+      if (sa != 1.0) mpsg::launch_lincomb(c, n, {ir.data()}, {sa}, ir.data());
+      *ci = wrap(std::move(ir));
+    } else {
+      *ci = nullptr;
+    }
+  });
+}
+
 int mpsg_contract_flops(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa,
                         const mpsg_tensor* b, const int32_t* idxb, double* flops) {
   return guarded([&] {

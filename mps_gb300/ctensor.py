@@ -31,7 +31,8 @@ class Ops:
     svd_complex(re, im, truncate, maxdim, tol, tieband) -> (ure, uim, s, vre, vim)."""
 
     def __init__(self, contract, dual, lincomb, dot, symmatrix, splitleg, matmul, space,
-                 svd_complex, download, fill, from_blocks, dual_space, fuselegs, dots=None):
+                 svd_complex, download, fill, from_blocks, dual_space, fuselegs, dots=None,
+                 ccontract=None):
         self.contract = contract
         self.dual = dual
         self.lincomb = lincomb
@@ -48,6 +49,9 @@ class Ops:
         self.fuselegs = fuselegs        # fuselegs(A, l, n)
         # dots([(a, b), ...]) -> [dot(a, b), ...] (one synchronisation when batched)
         self.dots = dots if dots is not None else (lambda pairs: [dot(a, b) for a, b in pairs])
+        # optional one-call complex contraction: ccontract(ar, ai, sa, ia, br, bi, sb, ib)
+        # -> (cr, ci) or a complex number
+        self.ccontract = ccontract
 
 
 def gpu_ops(precision: int = 0, ctx=None) -> Ops:
@@ -62,6 +66,9 @@ def gpu_ops(precision: int = 0, ctx=None) -> Ops:
     def dots(pairs):
         return mg.dots([a for a, _ in pairs], [b for _, b in pairs])
 
+    def ccon(ar, ai, sa, ia, br, bi, sb, ib):
+        return mg.contract_complex(ar, ai, sa, ia, br, bi, sb, ib, precision=precision)
+
     def svdc(re, im, truncate, maxdim, tol, tieband):
         return mg.svd_complex(re, im, maxdim=maxdim, tol=tol, tieband=tieband,
                               truncate=truncate)
@@ -70,7 +77,8 @@ def gpu_ops(precision: int = 0, ctx=None) -> Ops:
                lincomb, mg.dot, mg.SymMatrix, mg.splitleg,
                lambda A, B: mg.matmul(A, B, precision=0), lambda A: A.space, svdc,
                lambda A: A.to_flat(), lambda x, c, sp: mg.fill(x, c, sp, ctx),
-               lambda c, sp, b: mg.from_blocks(c, sp, b, ctx), mg.dual, mg.fuselegs, dots)
+               lambda c, sp, b: mg.from_blocks(c, sp, b, ctx), mg.dual, mg.fuselegs, dots,
+               ccon)
 
 
 class CTensor:
@@ -113,6 +121,9 @@ def ccontract(ops: Ops, A, ia, B, ib):
     """contract for complex operands (either may be real); a full contraction returns a
     Python complex."""
     A, B = creal(A), creal(B)
+    if ops.ccontract is not None:
+        r = ops.ccontract(A.re, A.im, A.sign, ia, B.re, B.im, B.sign, ib)
+        return r if isinstance(r, complex) else CTensor(r[0], r[1])
     rr = ops.contract(A.re, ia, B.re, ib)
     ri = None if B.im is None else ops.contract(A.re, ia, B.im, ib)
     ir = None if A.im is None else ops.contract(A.im, ia, B.re, ib)

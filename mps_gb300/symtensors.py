@@ -21,7 +21,8 @@ from ._lib import call, i32arr, i64arr, SpaceMismatch, MPSGError
 __all__ = [
     "VectorSpace", "U1Space", "Context", "get_context", "SymTensor", "dual", "zeros", "fill",
     "from_flat", "from_blocks", "meta", "permutelegs", "fuselegs", "splitleg", "SymMatrix",
-    "matmul", "contract", "contract_flops", "dot", "norm", "axpy", "axpby", "rmul", "mul",
+    "matmul", "contract", "contract_complex", "contract_flops", "dot", "norm", "axpy", "axpby",
+    "rmul", "mul",
     "similar", "copy", "fill_", "applymps2site", "applymps2site_flops", "mpsupdateleft",
     "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision", "_svd_",
     "svdtrunc", "svd_complex", "dots", "lincomb", "truncatedsizes", "small_eigh",
@@ -498,6 +499,22 @@ def contract(A: SymTensor, idxA, B: SymTensor, idxB, precision=None):
     if not h.value:
         return s.value
     return SymTensor(h, A.ctx)
+
+
+def contract_complex(Ar, Ai, sa, idxA, Br, Bi, sb, idxB, precision=None):
+    """contract of (Ar + i sa Ai) with (Br + i sb Bi) in one library call (Ai / Bi may be None):
+    returns (Cr, Ci) (Ci None for two real operands), or a Python complex when every leg is
+    contracted."""
+    if len(idxA) != Ar.rank or len(idxB) != Br.rank:
+        raise MPSGError(_lib.ERR_ARGUMENT, "index tuple length differs from tensor rank")
+    cr, ci = C.c_void_p(), C.c_void_p()
+    sr, si = C.c_double(), C.c_double()
+    call("mpsg_contract_complex", Ar.ctx.handle, Ar.handle, Ai.handle if Ai is not None else None,
+         float(sa), i32arr(idxA), Br.handle, Bi.handle if Bi is not None else None, float(sb),
+         i32arr(idxB), _prec(precision), C.byref(cr), C.byref(ci), C.byref(sr), C.byref(si))
+    if not cr.value:
+        return complex(sr.value, si.value)
+    return SymTensor(cr, Ar.ctx), (SymTensor(ci, Ar.ctx) if ci.value else None)
 
 
 def contract_flops(A: SymTensor, idxA, B: SymTensor, idxB) -> float:

@@ -151,3 +151,32 @@ def test_batched_dots_and_lincomb():
     np.testing.assert_allclose(gs[3].to_flat(), st.flatten(ts[3]) - st.flatten(ts[4]), atol=1e-14)
     with pytest.raises(mg.SpaceMismatch):
         mg.lincomb([1.0], [to_device(rand_tensor(0, (V, W), rng))], gs[0])
+
+
+@pytest.mark.parametrize("sa,sb,real_b", [(1.0, 1.0, False), (-1.0, 1.0, False),
+                                          (1.0, -1.0, False), (-1.0, 1.0, True)])
+def test_contract_complex_matches_complex_oracle(sa, sb, real_b):
+    rng = np.random.default_rng(17)
+    V1, V2 = U1Space((0, 3), (1, 4), (2, 2)), U1Space((0, 2), (1, 5))
+    V3 = U1Space((-1, 2), (0, 3), (1, 2))
+    ar, ai = rand_tensor(0, (V1, V2, V3), rng), rand_tensor(0, (V1, V2, V3), rng)
+    V4 = U1Space((0, 3), (1, 2))
+    br, bi = rand_tensor(0, (dual_space(V3), dual_space(V2), V4), rng), \
+        rand_tensor(0, (dual_space(V3), dual_space(V2), V4), rng)
+    cplx = lambda r, i, s: st.SymTensor(r.charge, r.space,
+                                        {k: r.blocks[k] + 1j * s * i.blocks[k] for k in r.blocks},
+                                        check=False)
+    A = cplx(ar, ai, sa)
+    B = st.SymTensor(br.charge, br.space, {k: br.blocks[k] + 0j for k in br.blocks},
+                     check=False) if real_b else cplx(br, bi, sb)
+    want = st.contract(A, (1, -2, -1), B, (-1, -2, 2))
+    cr, ci = mg.contract_complex(to_device(ar), to_device(ai), sa, (1, -2, -1), to_device(br),
+                                 None if real_b else to_device(bi), sb, (-1, -2, 2))
+    got = cr.to_flat() + 1j * ci.to_flat()
+    ref = st.flatten(want)
+    assert np.linalg.norm(got - ref) < 1e-13 * np.linalg.norm(ref)
+    # a full contraction with the conjugated dual gives the complex number |A|^2
+    z = mg.contract_complex(to_device(ar), to_device(ai), sa, (-1, -2, -3),
+                            mg.dual(to_device(ar)), mg.dual(to_device(ai)), -sa, (-1, -2, -3))
+    zz = sum(np.sum(A.blocks[k] * np.conj(A.blocks[k])) for k in A.blocks)
+    assert abs(z - zz) < 1e-12 * abs(zz)
