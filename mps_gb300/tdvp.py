@@ -196,14 +196,30 @@ def tdvp2sitesweep(ops: Ops, dt: float, As, Ws, env, maxdim: int = 200, tol: flo
 # ---------------------------------------------------------------------------------------------
 # measurements (src/symmps.jl:265-371, generalised to complex states)
 # ---------------------------------------------------------------------------------------------
-def site_operator(ops: Ops, dspace, diag_or_blocks):
-    """A charge-0 site operator with legs (d, dual(d)) (the SymMatrix ops of src/symmps.jl:
-    265-343): ``diag_or_blocks`` maps each site charge to its 1x1 (or dxd) block."""
+def site_operator(ops: Ops, dspace, diag_or_matrix, charge: int = 0):
+    """A site operator with legs (d, dual(d)) and the given charge (the SymMatrix ops of
+    src/symmps.jl:265-343): either a dict {site charge: diagonal value} (charge 0), or a dense
+    d x d matrix <out|op|in> in the charge-ordered site basis, of which the blocks with
+    c_out - c_in = charge are kept (e.g. S+ with charge +1, S- with charge -1)."""
     blocks = {}
-    for c, _ in dspace.sectors:
-        b = diag_or_blocks[c]
-        blocks[(c, c)] = [[b]] if not hasattr(b, "__len__") else b
-    return ops.from_blocks(0, (dspace, ops.dual_space(dspace)), blocks)
+    if isinstance(diag_or_matrix, dict):
+        if charge != 0:
+            raise ValueError("a diagonal operator has charge 0")
+        for c, _ in dspace.sectors:
+            b = diag_or_matrix[c]
+            blocks[(c, c)] = [[b]] if not hasattr(b, "__len__") else b
+    else:
+        import numpy as np
+        m = np.asarray(diag_or_matrix, dtype=float)
+        start, p = {}, 0
+        for c, n in dspace.sectors:
+            start[c] = (p, n)
+            p += n
+        for co, (po, no) in start.items():
+            for ci, (pi, ni) in start.items():
+                if co - ci == charge:
+                    blocks[(co, ci)] = m[po:po + no, pi:pi + ni]
+    return ops.from_blocks(charge, (dspace, ops.dual_space(dspace)), blocks)
 
 
 def _transfer(ops: Ops, L, A, op=None):

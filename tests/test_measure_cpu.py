@@ -93,3 +93,22 @@ def test_schmidt_values_and_entropy():
         np.testing.assert_allclose(got, s, rtol=1e-10, atol=1e-13)
         pr = s ** 2
         assert ent[l - 1] == pytest.approx(-np.sum(pr * np.log(pr)), abs=1e-10)
+
+
+def test_charged_two_point_function():
+    """<S+_i S-_j> (operator charges +1 and -1, src/symmps.jl:312-343 allows charges summing to
+    zero) against the dense state vector, for a real and a complex state."""
+    ops = oracle_ops()
+    d = U1Space((0, 1), (1, 1))
+    sp = td.site_operator(ops, d, np.array([[0.0, 0.0], [1.0, 0.0]]), charge=1)
+    sm = td.site_operator(ops, d, np.array([[0.0, 1.0], [0.0, 0.0]]), charge=-1)
+    for As, psi in states(ops):
+        got = ms.measure_pairs(As, sp, sm, ops=ops)
+        idx = np.arange(2 ** LX)
+        for (i, j), v in got.items():
+            bi, bj = 1 << (LX - i), 1 << (LX - j)
+            # S-_j then S+_i: j up -> down, then i down -> up
+            src = idx[((idx & bj) != 0) & ((idx & bi) == 0)]
+            dst = src - bj + bi
+            want = np.vdot(psi[dst], psi[src])
+            assert abs(v - want) < 1e-12, (i, j)
