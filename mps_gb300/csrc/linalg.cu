@@ -7,6 +7,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <exception>
+#include <functional>
+#include <thread>
 
 #include "linalg.hpp"
 
@@ -117,6 +120,51 @@ __global__ void scale_cols_inv_kernel(double* __restrict__ X, const double* __re
 
 unsigned grid_for(int64_t n) { return (unsigned)std::min<int64_t>((n + 255) / 256, 1184); }
 
+// Runs work(lane, b) for every block, largest cost first, each block on the least loaded of the
+// solver lanes; the lanes are forked from and joined back into the context stream. Each lane's
+// list is issued by its own host thread: cuSOLVER's eigen- and SVD solvers block the calling
+// thread on large blocks, which would otherwise serialise the lanes.
+void run_on_lanes(Context* ctx, SolverLanes& L, size_t nb, const std::function<double(size_t)>& cost,
+                  const std::function<void(int, size_t)>& work) {
+  std::vector<size_t> order(nb);
+  for (size_t b = 0; b < nb; ++b) order[b] = b;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t x, size_t y) { return cost(x) > cost(y); });
+  std::vector<size_t> list[kLanes];
+  double load[kLanes] = {0, 0, 0, 0};
+  for (size_t b : order) {
+    int lane = 0;
+    for (int i = 1; i < kLanes; ++i)
+      if (load[i] < load[lane]) lane = i;
+    load[lane] += cost(b);
+    list[lane].push_back(b);
+  }
+  MPSG_CUDA(cudaEventRecord(L.fork, ctx->stream));
+  for (int i = 0; i < kLanes; ++i)
+    if (!list[i].empty()) MPSG_CUDA(cudaStreamWaitEvent(L.st[i], L.fork, 0));
+  std::exception_ptr failure[kLanes];
+  auto run_lane = [&](int i) {
+    try {
+      MPSG_CUDA(cudaSetDevice(ctx->device));  // the current device is per host thread
+      for (size_t b : list[i]) work(i, b);
+    } catch (...) {
+      failure[i] = std::current_exception();
+    }
+  };
+  std::vector<std::thread> threads;
+  for (int i = 1; i < kLanes; ++i)
+    if (!list[i].empty()) threads.emplace_back(run_lane, i);
+  run_lane(0);
+  for (auto& t : threads) t.join();
+  for (int i = 0; i < kLanes; ++i) {
+    if (list[i].empty()) continue;
+    MPSG_CUDA(cudaEventRecord(L.join[i], L.st[i]));
+    MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, L.join[i], 0));
+  }
+  for (int i = 0; i < kLanes; ++i)
+    if (failure[i]) std::rethrow_exception(failure[i]);
+}
+
 // Complex block assembled from its real and imaginary planes (rows x cols, column-major):
 // dst = A, or A^T when trans, with the imaginary part multiplied by imsign (-1: conjugate).
 __global__ void interleave_kernel(double2* __restrict__ dst, const double* __restrict__ re,
@@ -191,7 +239,6 @@ void run_exact(Context* ctx, cudaStream_t st, cusolverDnHandle_t h, const double
     transpose_prefix_kernel<<<g2, dim3(32, 8), 0, st>>>(B.U->ptr, B.aux->ptr, M, M);
   }
   MPSG_CUDA(cudaGetLastError());
-  ctx->kernel_launches += 1;
   (void)k;
 }
 
@@ -270,7 +317,6 @@ void run_gram(Context* ctx, cudaStream_t st, cusolverDnHandle_t h, cublasHandle_
   const int64_t rows = left ? N : M;
   scale_cols_inv_kernel<<<grid_for(rows * k), 256, 0, st>>>(Y, B.S->ptr, rows, k);
   MPSG_CUDA(cudaGetLastError());
-  ctx->kernel_launches += 2;
 }
 
 }  // namespace
@@ -348,38 +394,18 @@ SVDResult svd_blocks(Context* ctx, const DeviceTensor& A, bool truncate, int64_t
     MPSG_CUDA(cudaMallocAsync((void**)&dinfo, sizeof(int) * nb, ctx->stream));
     MPSG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * nb, ctx->stream));
   }
-  // largest blocks first, each to the least loaded lane
-  std::vector<size_t> order(nb);
-  for (size_t b = 0; b < nb; ++b) order[b] = b;
   auto cost = [&](size_t b) {
     const double m = (double)std::max(blocks[b].M, blocks[b].N);
     const double n = (double)blocks[b].k;
     return m * n * n + n * n * n;
   };
-  std::stable_sort(order.begin(), order.end(),
-                   [&](size_t x, size_t y) { return cost(x) > cost(y); });
-  MPSG_CUDA(cudaEventRecord(L.fork, ctx->stream));
-  double load[kLanes] = {0, 0, 0, 0};
-  bool used[kLanes] = {false, false, false, false};
-  for (size_t b : order) {
-    int lane = 0;
-    for (int i = 1; i < kLanes; ++i)
-      if (load[i] < load[lane]) lane = i;
-    if (!used[lane]) {
-      MPSG_CUDA(cudaStreamWaitEvent(L.st[lane], L.fork, 0));
-      used[lane] = true;
-    }
-    load[lane] += cost(b);
+  run_on_lanes(ctx, L, nb, cost, [&](int lane, size_t b) {
     const double* Ab = A.data() + A.meta.off[b];
     if (method == kSvdExact) run_exact(ctx, L.st[lane], L.sol[lane], Ab, blocks[b], dinfo + b);
     else run_gram(ctx, L.st[lane], L.sol[lane], L.blas[lane], Ab, blocks[b],
                   method == kSvdGramLeft, dinfo + b);
-  }
-  for (int i = 0; i < kLanes; ++i) {
-    if (!used[i]) continue;
-    MPSG_CUDA(cudaEventRecord(L.join[i], L.st[i]));
-    MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, L.join[i], 0));
-  }
+  });
+  ctx->kernel_launches += (int64_t)nb * (method == kSvdExact ? 1 : 2);
   std::vector<int> info(nb, 0);
   if (nb)
     MPSG_CUDA(cudaMemcpyAsync(info.data(), dinfo, sizeof(int) * nb, cudaMemcpyDeviceToHost,
@@ -409,6 +435,7 @@ SVDResult svd_blocks(Context* ctx, const DeviceTensor& A, bool truncate, int64_t
       MPSG_CUDA(cudaEventRecord(L.fork, ctx->stream));
       MPSG_CUDA(cudaStreamWaitEvent(L.st[0], L.fork, 0));
       run_exact(ctx, L.st[0], L.sol[0], A.data() + A.meta.off[b], E, d1);
+      ctx->kernel_launches += 1;
       MPSG_CUDA(cudaEventRecord(L.join[0], L.st[0]));
       MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, L.join[0], 0));
       int i1 = 0;
@@ -515,26 +542,11 @@ CSVDResult svd_blocks_complex(Context* ctx, const DeviceTensor& Are, const Devic
     MPSG_CUDA(cudaMallocAsync((void**)&dinfo, sizeof(int) * nb, ctx->stream));
     MPSG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * nb, ctx->stream));
   }
-  std::vector<size_t> order(nb);
-  for (size_t b = 0; b < nb; ++b) order[b] = b;
   auto cost = [&](size_t b) {
     const double m = (double)std::max(blocks[b].M, blocks[b].N), n = (double)blocks[b].k;
     return m * n * n + n * n * n;
   };
-  std::stable_sort(order.begin(), order.end(),
-                   [&](size_t x, size_t y) { return cost(x) > cost(y); });
-  MPSG_CUDA(cudaEventRecord(L.fork, ctx->stream));
-  double load[kLanes] = {0, 0, 0, 0};
-  bool used[kLanes] = {false, false, false, false};
-  for (size_t b : order) {
-    int lane = 0;
-    for (int i = 1; i < kLanes; ++i)
-      if (load[i] < load[lane]) lane = i;
-    if (!used[lane]) {
-      MPSG_CUDA(cudaStreamWaitEvent(L.st[lane], L.fork, 0));
-      used[lane] = true;
-    }
-    load[lane] += cost(b);
+  run_on_lanes(ctx, L, nb, cost, [&](int lane, size_t b) {
     CBlock& B = blocks[b];
     cudaStream_t st = L.st[lane];
     const double* re = Are.data() + Are.meta.off[b];
@@ -551,13 +563,8 @@ CSVDResult svd_blocks_complex(Context* ctx, const DeviceTensor& Are, const Devic
     const int m = (int)std::max(B.M, B.N), n = (int)B.k;
     MPSG_SOLVER(cusolverDnZgesvd(L.sol[lane], 'S', 'S', m, n, W, m, B.S->ptr, U, m, VT, n, WB,
                                  B.lwork, B.rwork->ptr, dinfo + b));
-    ctx->kernel_launches += 1;
-  }
-  for (int i = 0; i < kLanes; ++i) {
-    if (!used[i]) continue;
-    MPSG_CUDA(cudaEventRecord(L.join[i], L.st[i]));
-    MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, L.join[i], 0));
-  }
+  });
+  ctx->kernel_launches += (int64_t)nb;
   std::vector<int> info(nb, 0);
   std::vector<std::vector<double>> S(nb);
   if (nb)
