@@ -63,6 +63,8 @@ def parse():
                         "Delta in [0,1.5], maxdim in {128,256,512,1024}, seeded), one sweep "
                         "each, concurrently and one after the other")
     p.add_argument("--sweep-chi", type=int, default=None, help="maxdim of the sweep (default chi)")
+    p.add_argument("--sweep-phases", action="store_true",
+                   help="also report the sweep's eigensolve / truncation / environment times")
     p.add_argument("--tdvp", action="store_true",
                    help="instead: 1-site TDVP of an XXZ chain (complex symmetric MPS) and the "
                         "Delta derivative of a two-point function by central differences")
@@ -218,7 +220,7 @@ SWEEP_MIXED = dict(precision=4, energy_precision=7, env_precision=7, svd="gram")
 SWEEP_FP64 = dict(precision=0, energy_precision=0, env_precision=0, svd="exact")
 
 
-def sweep_bench(ctx, chi, lx=32, seed=7):
+def sweep_bench(ctx, chi, lx=32, seed=7, phases=False):
     """One 2-site DMRG sweep (src/dmrg.jl:58-179) of the L=lx Heisenberg chain (J=1, OBC, Sz=0)
     at maxdim=chi from a random MPS whose bonds hold about chi states (binomial charge profile),
     canonicalised at site 1 with environments built (untimed). The sweep runs twice from copies
@@ -246,6 +248,14 @@ def sweep_bench(ctx, chi, lx=32, seed=7):
     t64, e64, n64 = out["fp64"]
     tmx, emx, nmx = out["mixed"]
     de = [abs(a - b) for a, b in zip(emx, e64)]
+    breakdown = {}
+    if phases:  # the same sweeps again, synchronised after every phase (not the timed numbers)
+        for name, cfg in (("fp64", SWEEP_FP64), ("mixed", SWEEP_MIXED)):
+            mps = gd.MPState([mg.copy(A) for A in m0.As], center=1)
+            env = [None if e is None else mg.copy(e) for e in env0]
+            pt = gd.PhaseTimer(ctx)
+            gd.dmrg2sitesweep(mps, Ws, env, timing=pt, **kw, **cfg)
+            breakdown[name] = {k: round(v, 3) for k, v in pt.s.items()}
     return {
         "workload": f"one 2-site DMRG sweep, Heisenberg chain L={lx} (J=1, OBC, Sz=0), "
                     f"maxdim={chi}, cutoff 1e-10, Krylov dim 4, maxiter 8, tol 1e-7; initial "
@@ -257,6 +267,7 @@ def sweep_bench(ctx, chi, lx=32, seed=7):
         "dE_final": abs(emx[-1] - e64[-1]), "dE_max_over_sweep": max(de),
         "dE_rel_final": abs(emx[-1] - e64[-1]) / abs(e64[-1]),
         "matvecs_fp64": n64, "matvecs_mixed": nmx, "energies_per_sweep": len(e64),
+        **({"phases_s": breakdown} if phases else {}),
     }
 
 
@@ -442,7 +453,7 @@ def run_ours(args):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_sweep and ws == 1:
-        line["sweep"] = sweep_bench(ctx, args.sweep_chi or args.chi)
+        line["sweep"] = sweep_bench(ctx, args.sweep_chi or args.chi, phases=args.sweep_phases)
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
         os.environ.setdefault("OPENBLAS_NUM_THREADS", str(os.cpu_count() or 1))
         vv, n, tm, cores = cpu_heff_rate(args.chi, flops)

@@ -310,12 +310,16 @@ class SweepOptions:
         self.env_precision = env_precision
 
 
-def _truncate_and_energy(v, AA, env, Ws, l, o: SweepOptions, keep="left"):
+def _truncate_and_energy(v, AA, env, Ws, l, o: SweepOptions, keep="left", tick=None):
     """svdtrunc + normalisation + post-truncation energy (dmrg.jl:88-93); ``keep`` names the
     factor that becomes the new (orthonormal) site tensor."""
+    import time
+    t = time.perf_counter()
     method = "exact" if o.svd == "exact" else "gram_" + keep
     u, s, vt = mg.svdtrunc(mg.SymMatrix(v, [1, 2], [3, 4]), maxdim=o.maxdim, tol=o.tol,
                            tieband=o.tieband, method=method)
+    if tick:
+        t = tick("svdtrunc", t)
     ns = mg.norm(s)
     truncerr = 1.0 - ns
     mg.rmul(s, 1.0 / ns)
@@ -323,6 +327,8 @@ def _truncate_and_energy(v, AA, env, Ws, l, o: SweepOptions, keep="left"):
     AA = mg.splitleg(mg.splitleg(usv, 2, AA.space[2:4]), 1, AA.space[0:2])
     e = mg.dot(AA, mg.applymps2site(AA, env[l - 1], env[l + 2], Ws[l - 1], Ws[l],
                                     precision=o.energy_precision))
+    if tick:
+        tick("energy", t)
     return u, s, vt, AA, e, truncerr
 
 
@@ -335,43 +341,76 @@ def _eig(AA, env, Ws, l, o: SweepOptions, stats):
     return v
 
 
-def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stats=None, **kw):
+class PhaseTimer:
+    """Wall time per sweep phase (eigensolve, svdtrunc, energy, environment update), each phase
+    closed by a device synchronisation; pass one as ``timing=`` to dmrg2sitesweep."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.s = {}
+
+    def __call__(self, name, t0):
+        import time
+        self.ctx.synchronize()
+        t1 = time.perf_counter()
+        self.s[name] = self.s.get(name, 0.0) + (t1 - t0)
+        return t1
+
+
+def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stats=None,
+                   timing: PhaseTimer | None = None, **kw):
     """``dmrg2sitesweep!`` (src/dmrg.jl:58-179): one left-to-right-to-left sweep on the GPU.
     Returns the reference's energy list (3L-5 post-truncation energies; the right-to-left loop
-    pushes each energy twice, dmrg.jl:132,156)."""
+    pushes each energy twice, dmrg.jl:132,156). ``timing`` (a PhaseTimer) accumulates the wall
+    time of the eigensolves, truncations (svdtrunc), post-truncation energies and environment
+    updates."""
+    import time
     o = opts or SweepOptions(**kw)
+    tick = (lambda name, t0: timing(name, t0)) if timing else (lambda name, t0: t0)
+    now = time.perf_counter
     lx = len(mps)
     if mps.center != 1:
         raise mg.SpaceMismatch(2, "The center of MPS has to be 1 for dmrg L->R->L")
     energies = []
     A = mps.As[0]
+    t = now()
     for l in range(1, lx - 1):
         AA = mg.contract(A, (1, 2, -1), mps.As[l], (-1, 3, 4), precision=0)
         v = _eig(AA, env, Ws, l, o, stats)
-        u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o)
+        t = tick("eigsolve", t)
+        u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o, tick=timing)
         energies.append(e)
+        t = now()
         mps.As[l - 1] = mg.splitleg(u, 1, A.space[0:2])
         env[l] = mg.mpsupdateleft(env[l - 1], mps.As[l - 1], Ws[l - 1], precision=o.env_precision)
         A = mg.splitleg(mg.matmul(s, vt, precision=0), 2, AA.space[2:4])
+        t = tick("environment", t)
     l = lx - 1
     AA = mg.contract(A, (1, 2, -1), mps.As[l], (-1, 3, 4), precision=0)
     v = _eig(AA, env, Ws, l, o, stats)
+    t = tick("eigsolve", t)
     e = None
     for l in range(lx - 1, 1, -1):
-        u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o, keep="right")
+        u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o, keep="right",
+                                                  tick=timing)
         energies.append(e)
+        t = now()
         mps.As[l] = mg.splitleg(vt, 2, AA.space[2:4])
         env[l + 1] = mg.mpsupdateright(env[l + 2], mps.As[l], Ws[l], precision=o.env_precision)
         A = mg.splitleg(mg.matmul(u, s, precision=0), 1, AA.space[0:2])
+        t = tick("environment", t)
         AA = mg.contract(mps.As[l - 2], (1, 2, -1), A, (-1, 3, 4), precision=0)
         v = _eig(AA, env, Ws, l - 1, o, stats)
+        t = tick("eigsolve", t)
         energies.append(e)
     l = 1
-    u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o, keep="right")
+    u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o, keep="right", tick=timing)
+    t = now()
     energies.append(e)
     mps.As[1] = mg.splitleg(vt, 2, AA.space[2:4])
     env[2] = mg.mpsupdateright(env[3], mps.As[1], Ws[1], precision=o.env_precision)
     mps.As[0] = mg.splitleg(mg.matmul(u, s, precision=0), 1, AA.space[0:2])
+    tick("environment", t)
     return energies
 
 
