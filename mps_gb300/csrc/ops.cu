@@ -273,6 +273,26 @@ std::shared_ptr<DevContract> get_contract_plan(Context* ctx, const TensorMeta& A
   return p;
 }
 
+std::shared_ptr<Buffer> contract_gemm(Context* ctx, DevContract& p, const DeviceTensor& a,
+                                      const DeviceTensor& b, int precision) {
+  std::shared_ptr<Buffer> fa, fb;
+  const double* pa = a.data();
+  const double* pb = b.data();
+  if (!p.fa.identity) {
+    fa = alloc_buffer(ctx, p.host->fa.out.total);
+    launch_copy(ctx, p.fa, a.data(), fa->ptr);
+    pa = fa->ptr;
+  }
+  if (!p.fb.identity) {
+    fb = alloc_buffer(ctx, p.host->fb.out.total);
+    launch_copy(ctx, p.fb, b.data(), fb->ptr);
+    pb = fb->ptr;
+  }
+  auto fc = alloc_buffer(ctx, p.host->mm.out.total);
+  run_gemm(ctx, p.mm, pa, pb, fc->ptr, precision);
+  return fc;
+}
+
 DeviceTensor contract(Context* ctx, const DeviceTensor& a, const std::vector<int>& idxA,
                       const DeviceTensor& b, const std::vector<int>& idxB, int precision,
                       double* scalar) {
@@ -299,24 +319,10 @@ DeviceTensor contract(Context* ctx, const DeviceTensor& a, const std::vector<int
     if (scalar) *scalar = s;
     return DeviceTensor();
   }
-  std::shared_ptr<Buffer> fa, fb, fc;
-  const double* pa = a.data();
-  const double* pb = b.data();
-  if (!p->fa.identity) {
-    fa = alloc_buffer(ctx, p->host->fa.out.total);
-    launch_copy(ctx, p->fa, a.data(), fa->ptr);
-    pa = fa->ptr;
-  }
-  if (!p->fb.identity) {
-    fb = alloc_buffer(ctx, p->host->fb.out.total);
-    launch_copy(ctx, p->fb, b.data(), fb->ptr);
-    pb = fb->ptr;
-  }
+  std::shared_ptr<Buffer> fc = contract_gemm(ctx, *p, a, b, precision);
   DeviceTensor t;
   t.ctx = ctx;
   t.meta = p->host->split.out;
-  fc = alloc_buffer(ctx, p->host->mm.out.total);
-  run_gemm(ctx, p->mm, pa, pb, fc->ptr, precision);
   if (p->split.identity) {
     t.buf = fc;
   } else {
@@ -408,6 +414,16 @@ FoldedHeffPlans plan_heff_folded(const TensorMeta& v, const TensorMeta& envL,
   plan_split_permute_rec(c1.mm.out, c1.rlegs, c1.clegs, c1.perm, &src_of_x);
   plan_symmatrix_rec(c1.split.out, c2.rowsA, c2.colsA, &dst_of_x);
   F.x2a = compose_through(c1.split.out, src_of_x, dst_of_x);
+  for (int side = 0; side < 2; ++side) {  // fold output -> fused GEMM operand
+    const ContractPlan& f = side ? *F.rw : *F.lw;
+    std::vector<BlockMap> src, dst;
+    plan_split_permute_rec(f.mm.out, f.rlegs, f.clegs, f.perm, &src);
+    if (side)
+      plan_symmatrix_rec(f.split.out, c2.rowsB, c2.colsB, &dst);
+    else
+      plan_symmatrix_rec(f.split.out, c1.rowsA, c1.colsA, &dst);
+    (side ? F.rw2b : F.lw2a) = compose_through(f.split.out, src, dst);
+  }
   return F;
 }
 
@@ -423,6 +439,10 @@ void check_heff_folded(const TensorMeta& v, const TensorMeta& envL, const Tensor
   }
   check_composition(F.c1->split.tasks, F.c1->mm.out.total, F.c1->split.out.total,
                     F.c2->fa.tasks, F.c2->fa.out.total, F.x2a);
+  check_composition(F.lw->split.tasks, F.lw->mm.out.total, F.lw->split.out.total,
+                    F.c1->fa.tasks, F.c1->fa.out.total, F.lw2a);
+  check_composition(F.rw->split.tasks, F.rw->mm.out.total, F.rw->split.out.total,
+                    F.c2->fb.tasks, F.c2->fb.out.total, F.rw2b);
   if (!same_meta(F.c2->split.out, v)) throw Error(kErrSpaceMismatch, "folded H_eff changes v's structure");
 }
 
@@ -443,8 +463,12 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
   }
   if (precision < 2 || precision > split::kMaxSlices)
     throw Error(kErrUnsupported, "precision must be 0 (FP64) or 2..7 bf16 slices");
-  op->envLW = contract(ctx, envL, kLW_A, W1, kLW_B, 0, nullptr);
-  op->envRW = contract(ctx, W2, kRW_A, envR, kRW_B, 0, nullptr);
+  // the W folds (FP64): their fused GEMM outputs go straight into GEMM 1's A and GEMM 2's B
+  // operands through composed copies, so envLW and envRW are never materialised
+  auto plw = get_contract_plan(ctx, envL.meta, kLW_A, W1.meta, kLW_B);
+  auto prw = get_contract_plan(ctx, W2.meta, kRW_A, envR.meta, kRW_B);
+  const TensorMeta& lwmeta = plw->host->split.out;
+  const TensorMeta& rwmeta = prw->host->split.out;
   op->plan_key = "H" + std::to_string(precision) + "|" + meta_key(vmeta) + "|" +
                  meta_key(envL.meta) + "|" + meta_key(envR.meta) + "|" + meta_key(W1.meta) +
                  "|" + meta_key(W2.meta);
@@ -457,14 +481,25 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
     ctx->heff_bytes -= op->plans->bytes;
   } else {
     auto P = std::make_shared<HeffPlans>();
-    P->c1 = private_contract_plan(ctx, op->envLW.meta, kX_A, vmeta, kX_B);
-    P->c2 = private_contract_plan(ctx, P->c1->host->split.out, kO_A, op->envRW.meta, kO_B);
+    P->c1 = private_contract_plan(ctx, lwmeta, kX_A, vmeta, kX_B);
+    P->c2 = private_contract_plan(ctx, P->c1->host->split.out, kO_A, rwmeta, kO_B);
     const ContractPlan& h1 = *P->c1->host;
     const ContractPlan& h2 = *P->c2->host;
     std::vector<BlockMap> src_of_x, dst_of_x;
     plan_split_permute_rec(h1.mm.out, h1.rlegs, h1.clegs, h1.perm, &src_of_x);
     plan_symmatrix_rec(h1.split.out, h2.rowsA, h2.colsA, &dst_of_x);
     P->x2a.upload(compose_through(h1.split.out, src_of_x, dst_of_x), false, ctx->stream);
+    for (int side = 0; side < 2; ++side) {
+      const ContractPlan& f = side ? *prw->host : *plw->host;
+      std::vector<BlockMap> src, dst;
+      plan_split_permute_rec(f.mm.out, f.rlegs, f.clegs, f.perm, &src);
+      if (side)
+        plan_symmatrix_rec(f.split.out, h2.rowsB, h2.colsB, &dst);
+      else
+        plan_symmatrix_rec(f.split.out, h1.rowsA, h1.colsA, &dst);
+      (side ? P->rw2b : P->lw2a).upload(compose_through(f.split.out, src, dst), false,
+                                        ctx->stream);
+    }
     for (auto* c : {P->c1.get(), P->c2.get()}) {
       auto& sp = c->mm.splitp[precision];
       sp = std::make_shared<split::SplitPlan>();
@@ -479,14 +514,24 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
   op->copy_bytes = 16.0 * (double)(c1.fb.elems + op->plans->x2a.elems + c2.split.elems);
   op->pack_bytes = (16.0 + 2.0 * precision) *
                    (double)(c1.host->fb.out.total + c2.host->fa.out.total);
-  op->fusedA1 = alloc_buffer(ctx, c1.host->fa.out.total);
-  launch_copy(ctx, c1.fa, op->envLW.data(), op->fusedA1->ptr);
-  op->fusedB2 = alloc_buffer(ctx, c2.host->fb.out.total);
-  launch_copy(ctx, c2.fb, op->envRW.data(), op->fusedB2->ptr);
+  {
+    auto clw = contract_gemm(ctx, *plw, envL, W1, 0);
+    op->fusedA1 = alloc_buffer(ctx, c1.host->fa.out.total);
+    launch_copy(ctx, op->plans->lw2a, clw->ptr, op->fusedA1->ptr);
+  }
+  {
+    auto crw = contract_gemm(ctx, *prw, W2, envR, 0);
+    op->fusedB2 = alloc_buffer(ctx, c2.host->fb.out.total);
+    launch_copy(ctx, op->plans->rw2b, crw->ptr, op->fusedB2->ptr);
+  }
   split::launch_split_gemm(ctx, *c1.mm.splitp[precision], op->fusedA1->ptr, nullptr, nullptr,
                            split::kPackA);
   split::launch_split_gemm(ctx, *c2.mm.splitp[precision], nullptr, op->fusedB2->ptr, nullptr,
                            split::kPackB);
+  // the packed slices are all the GEMMs read: the FP64 operands go back to the pool (the frees
+  // are ordered after the packing on the stream)
+  op->fusedA1.reset();
+  op->fusedB2.reset();
   return op;
 }
 

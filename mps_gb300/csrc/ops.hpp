@@ -19,6 +19,10 @@ DeviceTensor symmatrix(Context* ctx, const DeviceTensor& a, const std::vector<in
                        const std::vector<int>& cols);
 DeviceTensor matmul(Context* ctx, const DeviceTensor& a, const DeviceTensor& b, int precision);
 
+// The GEMM part of a contraction (operand fusion + block products): the result in the plan's
+// fused output layout, before the final split / permutation.
+std::shared_ptr<Buffer> contract_gemm(Context* ctx, DevContract& p, const DeviceTensor& a,
+                                      const DeviceTensor& b, int precision);
 std::shared_ptr<DevContract> get_contract_plan(Context* ctx, const TensorMeta& A,
                                                const std::vector<int>& idxA,
                                                const TensorMeta& B,
@@ -56,15 +60,20 @@ double dot(Context* ctx, const DeviceTensor& a, const DeviceTensor& b);
 struct HeffPlans {
   std::shared_ptr<DevContract> c1, c2;
   DevCopyPlan x2a;                   // fused X of GEMM 1 -> fused A of GEMM 2 (X never built)
+  DevCopyPlan lw2a, rw2b;            // fold outputs -> GEMM 1's A / GEMM 2's B (composed)
   size_t bytes = 0;                  // device storage held, for the cache budget
-  ~HeffPlans() { x2a.release(); }
+  ~HeffPlans() {
+    x2a.release();
+    lw2a.release();
+    rw2b.release();
+  }
 };
 
 struct HeffOp {
   Context* ctx = nullptr;
   int precision = 0;
   DeviceTensor envL, envR, W1, W2;   // precision 0
-  DeviceTensor envLW, envRW;         // precision >= 2
+
   TensorMeta vmeta;
   std::shared_ptr<HeffPlans> plans;  // precision >= 2
   std::string plan_key;
@@ -81,6 +90,9 @@ struct HeffOp {
 struct FoldedHeffPlans {
   std::shared_ptr<ContractPlan> lw, rw, c1, c2;
   std::vector<CopyTask> x2a;
+  // the folds' fused GEMM outputs moved straight into GEMM 1's A / GEMM 2's B operands
+  // (envLW and envRW are never materialised)
+  std::vector<CopyTask> lw2a, rw2b;
 };
 FoldedHeffPlans plan_heff_folded(const TensorMeta& v, const TensorMeta& envL,
                                  const TensorMeta& envR, const TensorMeta& W1,
