@@ -136,6 +136,18 @@ int mpsg_contract_flops(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa
 int mpsg_applymps2site(mpsg_ctx* ctx, const mpsg_tensor* v, const mpsg_tensor* envl,
                        const mpsg_tensor* envr, const mpsg_tensor* w1, const mpsg_tensor* w2,
                        int32_t precision, mpsg_tensor** out);              /* :93-105 */
+/* _applymps2site from host arrays to a host array (no reference counterpart: the reference's
+ * data lives on the host). hv, henvl, henvr, hw1, hw2 hold the flat data of v, envl, envr, w1,
+ * w2 (each tensor's element count), which are overwritten with it; the result's flat data is
+ * written to hout (v's element count) and, if out is not NULL, returned as a device tensor too.
+ * The uploads run on a copy stream while the operator is prepared: each W fold starts once its
+ * two inputs have arrived. Pinned host memory makes the copies asynchronous. Returns when hout
+ * is complete. */
+int mpsg_applymps2site_host(mpsg_ctx* ctx, mpsg_tensor* v, mpsg_tensor* envl, mpsg_tensor* envr,
+                            mpsg_tensor* w1, mpsg_tensor* w2, const double* hv,
+                            const double* henvl, const double* henvr, const double* hw1,
+                            const double* hw2, int32_t precision, double* hout,
+                            mpsg_tensor** out);
 int mpsg_applymps2site_flops(mpsg_ctx* ctx, const mpsg_tensor* v, const mpsg_tensor* envl,
                              const mpsg_tensor* envr, const mpsg_tensor* w1,
                              const mpsg_tensor* w2, double* flops);

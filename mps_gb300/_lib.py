@@ -82,6 +82,7 @@ SIGNATURES = {
     "mpsg_contract_noalloc": [P, P, PI32, P, PI32, P],
     "mpsg_contract_complex": [P, P, P, F64, PI32, P, P, F64, PI32, I32, PP, PP, PF64, PF64],
     "mpsg_applymps2site": [P, P, P, P, P, P, I32, PP],
+    "mpsg_applymps2site_host": [P, P, P, P, P, P, P, P, P, P, P, I32, P, PP],
     "mpsg_applymps2site_flops": [P, P, P, P, P, P, PF64],
     "mpsg_mpsupdateleft": [P, P, P, P, I32, PP],
     "mpsg_mpsupdateright": [P, P, P, P, I32, PP],

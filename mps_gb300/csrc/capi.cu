@@ -410,6 +410,29 @@ int mpsg_applymps2site(mpsg_ctx* ctx, const mpsg_tensor* v, const mpsg_tensor* e
   });
 }
 
+int mpsg_applymps2site_host(mpsg_ctx* ctx, mpsg_tensor* v, mpsg_tensor* envl, mpsg_tensor* envr,
+                            mpsg_tensor* w1, mpsg_tensor* w2, const double* hv,
+                            const double* henvl, const double* henvr, const double* hw1,
+                            const double* hw2, int32_t precision, double* hout,
+                            mpsg_tensor** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(v, "v");
+    need(envl, "envl");
+    need(envr, "envr");
+    need(w1, "w1");
+    need(w2, "w2");
+    need(hout, "hout");
+    const double* hin[5] = {hv, henvl, henvr, hw1, hw2};
+    const mpsg_tensor* ts[5] = {v, envl, envr, w1, w2};
+    for (int i = 0; i < 5; ++i)
+      if (ts[i]->t.meta.total) need(hin[i], "host input");
+    auto r = mpsg::applymps2site_host(&ctx->c, v->t, envl->t, envr->t, w1->t, w2->t, hin,
+                                      precision, hout);
+    if (out) *out = wrap(std::move(r));
+  });
+}
+
 int mpsg_applymps2site_flops(mpsg_ctx* ctx, const mpsg_tensor* v, const mpsg_tensor* envl,
                              const mpsg_tensor* envr, const mpsg_tensor* w1,
                              const mpsg_tensor* w2, double* flops) {

@@ -91,6 +91,10 @@ Context::~Context() {
       cudaEventDestroy(ev.b);
     }
   for (auto e : event_pool) cudaEventDestroy(e);
+  if (copy_stream) cudaStreamSynchronize(copy_stream);
+  for (auto e : copy_ev)
+    if (e) cudaEventDestroy(e);
+  if (copy_stream) cudaStreamDestroy(copy_stream);
   if (solver && solver_destroy) solver_destroy(solver);
   if (d_partials) cudaFree(d_partials);
   if (h_pinned) cudaFreeHost(h_pinned);
@@ -355,6 +359,46 @@ DeviceTensor applymps2site(Context* ctx, const DeviceTensor& v, const DeviceTens
   return contract(ctx, t3, kH4A, envR, kH4B, precision, nullptr);
 }
 
+DeviceTensor applymps2site_host(Context* ctx, const DeviceTensor& v, const DeviceTensor& envL,
+                                const DeviceTensor& envR, const DeviceTensor& W1,
+                                const DeviceTensor& W2, const double* const host_in[5],
+                                int precision, double* host_out) {
+  if (!ctx->copy_stream) {
+    MPSG_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    for (auto& e : ctx->copy_ev) MPSG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  cudaStream_t cs = ctx->copy_stream;
+  // the uploads overwrite the inputs: after everything already queued on the context stream
+  MPSG_CUDA(cudaEventRecord(ctx->copy_ev[3], ctx->stream));
+  MPSG_CUDA(cudaStreamWaitEvent(cs, ctx->copy_ev[3], 0));
+  const DeviceTensor* dst[5] = {&W1, &envL, &W2, &envR, &v};
+  const int src_of[5] = {3, 1, 4, 2, 0};  // host_in order: v, envL, envR, W1, W2
+  for (int i = 0; i < 5; ++i) {
+    const DeviceTensor& t = *dst[i];
+    if (t.meta.total)
+      MPSG_CUDA(cudaMemcpyAsync(t.data(), host_in[src_of[i]], sizeof(double) * t.meta.total,
+                                cudaMemcpyHostToDevice, cs));
+    if (i == 1) MPSG_CUDA(cudaEventRecord(ctx->copy_ev[0], cs));  // W1, envL: left fold
+    if (i == 3) MPSG_CUDA(cudaEventRecord(ctx->copy_ev[1], cs));  // W2, envR: right fold
+  }
+  MPSG_CUDA(cudaEventRecord(ctx->copy_ev[2], cs));  // v
+  DeviceTensor out;
+  if (precision != 0) {
+    auto op = heff_create(ctx, v.meta, envL, envR, W1, W2, precision, ctx->copy_ev[0],
+                          ctx->copy_ev[1]);
+    MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[2], 0));
+    out = heff_apply(*op, v);
+  } else {
+    MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[2], 0));
+    out = applymps2site(ctx, v, envL, envR, W1, W2, 0);
+  }
+  if (out.meta.total)
+    MPSG_CUDA(cudaMemcpyAsync(host_out, out.data(), sizeof(double) * out.meta.total,
+                              cudaMemcpyDeviceToHost, ctx->stream));
+  MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return out;
+}
+
 double applymps2site_flops(Context* ctx, const TensorMeta& v, const TensorMeta& envL,
                            const TensorMeta& envR, const TensorMeta& W1, const TensorMeta& W2) {
   auto p1 = get_contract_plan(ctx, envL, kH1A, v, kH1B);
@@ -448,7 +492,8 @@ void check_heff_folded(const TensorMeta& v, const TensorMeta& envL, const Tensor
 
 std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const DeviceTensor& envL,
                                     const DeviceTensor& envR, const DeviceTensor& W1,
-                                    const DeviceTensor& W2, int precision) {
+                                    const DeviceTensor& W2, int precision, cudaEvent_t wait_left,
+                                    cudaEvent_t wait_right) {
   auto op = std::make_shared<HeffOp>();
   op->ctx = ctx;
   op->precision = precision;
@@ -514,11 +559,13 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
   op->copy_bytes = 16.0 * (double)(c1.fb.elems + op->plans->x2a.elems + c2.split.elems);
   op->pack_bytes = (16.0 + 2.0 * precision) *
                    (double)(c1.host->fb.out.total + c2.host->fa.out.total);
+  if (wait_left) MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, wait_left, 0));
   {
     auto clw = contract_gemm(ctx, *plw, envL, W1, 0);
     op->fusedA1 = alloc_buffer(ctx, c1.host->fa.out.total);
     launch_copy(ctx, op->plans->lw2a, clw->ptr, op->fusedA1->ptr);
   }
+  if (wait_right) MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, wait_right, 0));
   {
     auto crw = contract_gemm(ctx, *prw, W2, envR, 0);
     op->fusedB2 = alloc_buffer(ctx, c2.host->fb.out.total);

@@ -100,9 +100,19 @@ FoldedHeffPlans plan_heff_folded(const TensorMeta& v, const TensorMeta& envL,
 // Host self-check of those plans (bounds, coverage, composition == two steps).
 void check_heff_folded(const TensorMeta& v, const TensorMeta& envL, const TensorMeta& envR,
                        const TensorMeta& W1, const TensorMeta& W2);
+// wait_left / wait_right: events the left / right W fold waits for (inputs still arriving)
 std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const DeviceTensor& envL,
                                     const DeviceTensor& envR, const DeviceTensor& W1,
-                                    const DeviceTensor& W2, int precision);
+                                    const DeviceTensor& W2, int precision,
+                                    cudaEvent_t wait_left = nullptr,
+                                    cudaEvent_t wait_right = nullptr);
+// _applymps2site from host arrays (v, envL, envR, W1, W2 in host_in, into the given device
+// tensors) to a host array: the uploads run on a copy stream, each W fold starts as soon as its
+// two inputs have arrived, and the result is downloaded before returning.
+DeviceTensor applymps2site_host(Context* ctx, const DeviceTensor& v, const DeviceTensor& envL,
+                                const DeviceTensor& envR, const DeviceTensor& W1,
+                                const DeviceTensor& W2, const double* const host_in[5],
+                                int precision, double* host_out);
 DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v);
 
 }  // namespace mpsg

@@ -159,6 +159,8 @@ struct Context : std::enable_shared_from_this<Context> {
   std::unordered_map<std::string, std::shared_ptr<HeffPlans>> heff_cache;
   std::vector<std::string> heff_lru;
   size_t heff_bytes = 0;
+  cudaStream_t copy_stream = nullptr;   // host<->device transfers overlapped with compute
+  cudaEvent_t copy_ev[4] = {};          // ... and the events that order them
   int64_t kernel_launches = 0;    // launches of this library's kernels
   bool debug_sync = false;        // MPSG_DEBUG_SYNC=1: synchronise and check after tensor-core GEMMs
   double gemm_flops = 0;          // algorithmic flops issued through block GEMMs

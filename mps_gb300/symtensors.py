@@ -23,7 +23,8 @@ __all__ = [
     "from_flat", "from_blocks", "meta", "permutelegs", "fuselegs", "splitleg", "SymMatrix",
     "matmul", "contract", "contract_complex", "contract_flops", "dot", "norm", "axpy", "axpby",
     "rmul", "mul",
-    "similar", "copy", "fill_", "applymps2site", "applymps2site_flops", "mpsupdateleft",
+    "similar", "copy", "fill_", "applymps2site", "applymps2site_host", "applymps2site_flops",
+    "mpsupdateleft",
     "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision", "_svd_",
     "svdtrunc", "svd_complex", "dots", "lincomb", "truncatedsizes", "small_eigh",
     "eigsolve_heff2", "EigInfo", "Heff2",
@@ -575,6 +576,33 @@ class Heff2:
                 self._h = None
         except Exception:
             pass
+
+
+def _host_ptr(x, n):
+    """Address of a float64 host buffer of n elements (a torch tensor or a numpy array)."""
+    if hasattr(x, "data_ptr"):
+        if x.numel() != n or x.element_size() != 8 or not x.is_contiguous():
+            raise MPSGError(_lib.ERR_ARGUMENT, "host buffer: wrong size, type or layout")
+        return x.data_ptr()
+    a = np.asarray(x)
+    if a.dtype != np.float64 or a.size != n or not a.flags.c_contiguous:
+        raise MPSGError(_lib.ERR_ARGUMENT, "host buffer: wrong size, type or layout")
+    return a.ctypes.data
+
+
+def applymps2site_host(v, envL, envR, W1, W2, host_in, host_out, precision=None,
+                       keep=False):
+    """``_applymps2site`` from host buffers to a host buffer in one call: ``host_in`` holds the
+    flat data of (v, envL, envR, W1, W2), copied into those device tensors while the operator
+    is prepared; the result's flat data lands in ``host_out``. Returns the device result when
+    ``keep``. Pinned buffers (e.g. torch ``pin_memory()``) make the copies asynchronous."""
+    ts = (v, envL, envR, W1, W2)
+    ptrs = [_host_ptr(h, t.numel()) for h, t in zip(host_in, ts)]
+    optr = _host_ptr(host_out, v.numel())
+    out = C.c_void_p()
+    call("mpsg_applymps2site_host", v.ctx.handle, *[t.handle for t in ts], *ptrs,
+         _prec(precision), optr, C.byref(out) if keep else None)
+    return SymTensor(out, v.ctx) if keep else None
 
 
 def applymps2site_flops(v, envL, envR, W1, W2) -> float:

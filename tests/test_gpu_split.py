@@ -142,3 +142,26 @@ def test_prepared_operator_plan_reuse():
     c = mg.Heff2(v, eL2, eR, W1, W2, precision=4)  # built from returned plans
     want2 = mg.applymps2site(v, eL2, eR, W1, W2, precision=0).to_flat()
     assert relerr(c(v).to_flat(), want2) < TOL[4]
+
+
+@pytest.mark.parametrize("S", [0, 4, 7])
+def test_applymps2site_from_host_buffers(S):
+    """The host-buffer entry point (uploads overlapped with the operator preparation) gives the
+    result of the device call, and overwrites the device inputs with the host data."""
+    (sv, sl, sr), flats = gd.heff_inputs_host(64, 0.5, 1911, 9)
+    conv = lambda sp: tuple(st.VectorSpace(V.sectors, V.isdual) for V in sp)
+    O = [st.from_flat(0, conv(s), f) for s, f in zip((sv, sl, sr), flats)]
+    W = om.xxz_u1mpo(3, 0.5)[1]
+    want = st.flatten(om.applymps2site(O[0], O[1], O[2], W, W))
+    D = gd.heff_problem(64, 0.5, 1911, ncharges=9)
+    host_in = [np.ascontiguousarray(t.to_flat()) for t in D]
+    dev = [mg.zeros(t.charge, t.space) for t in D]
+    out = np.zeros(D[0].numel())
+    r = mg.applymps2site_host(*dev, host_in, out, precision=S, keep=True)
+    tol = 1e-12 if S == 0 else 4 * TOL[S]
+    assert relerr(out, want) < tol
+    np.testing.assert_array_equal(out, r.to_flat())
+    for d, h in zip(dev, host_in):
+        np.testing.assert_array_equal(d.to_flat(), h)
+    with pytest.raises(mg.MPSGError):
+        mg.applymps2site_host(*dev, host_in, np.zeros(3), precision=S)
