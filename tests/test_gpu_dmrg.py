@@ -200,3 +200,23 @@ def test_independent_chains_concurrently_equal_one_by_one():
     many = gd.run_chains(specs, 2, o, threads=len(specs))
     assert one == many
     assert all(e < 0 for e in one)
+
+
+def test_sweep_with_offloaded_environments_is_bit_identical():
+    """A sweep whose environments live in a 3-entry device window (the rest in host memory)
+    gives exactly the energies of the all-resident sweep."""
+    from mps_gb300.envstore import OffloadedEnvs
+    lx, chi = 16, 32
+    _, md, _, Wd, _, ed = heisenberg_setup(lx, chi, seed=3)
+    res = []
+    for window in (None, 3):
+        mps = gd.MPState([mg.copy(A) for A in md.As], center=1)
+        env = [None if e is None else mg.copy(e) for e in ed]
+        if window:
+            env = OffloadedEnvs(env, window=window)
+        es = gd.dmrg2sitesweep(mps, Wd, env, maxdim=chi, tol=1e-10, krylovdim=4,
+                               krylovmaxiter=8)
+        res.append(es)
+        if window:
+            assert env.downloads > 0 and env.uploads > 0
+    assert res[0] == res[1]
