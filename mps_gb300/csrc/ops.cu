@@ -23,8 +23,12 @@ std::shared_ptr<Buffer> alloc_buffer(Context* ctx, int64_t n) {
   return b;
 }
 
+std::atomic<int> g_live_contexts{0};
+
 void context_init(Context* ctx, int device) {
   ctx->device = device;
+  ++g_live_contexts;
+  ctx->counted = true;
   MPSG_CUDA(cudaSetDevice(device));
   MPSG_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
   MPSG_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
@@ -79,6 +83,7 @@ void collect_kernel_times(Context* ctx) {
 }
 
 Context::~Context() {
+  if (counted) --g_live_contexts;
   heff_cache.clear();
   heff_lru.clear();
   contract_cache.clear();
@@ -584,7 +589,8 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
 
 HeffOp::~HeffOp() {
   if (!plans || plan_key.empty() || !ctx) return;
-  constexpr size_t kBudget = size_t(8) << 30;  // idle plans kept per context (device bytes)
+  // idle plans kept (device bytes): a share of 8 GiB per process
+  const size_t kBudget = cache_share(size_t(8) << 30);
   if (ctx->heff_cache.count(plan_key)) return;  // an idle copy exists already: drop this one
   ctx->heff_cache[plan_key] = plans;
   ctx->heff_lru.push_back(plan_key);

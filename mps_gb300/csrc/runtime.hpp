@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <list>
 #include <memory>
 #include <mutex>
@@ -102,13 +103,21 @@ struct DevContract {
   ~DevContract();
 };
 
+// Live contexts of the process: the plan-cache budgets below are shares of a per-process total,
+// so many concurrent contexts (independent chains) together stay within the device memory.
+extern std::atomic<int> g_live_contexts;
+inline size_t cache_share(size_t total) {
+  const int n = g_live_contexts.load();
+  return total / (size_t)(n > 1 ? n : 1);
+}
+
 // Plans by structure key, least recently used first, trimmed to a device-byte budget (split
 // plans carry packed operand scratch as large as their operands, and a sweep meets a new
 // structure at every bond). Entries are shared: evicting one that a caller still holds only
 // drops the cache's reference.
 template <class T>
 struct PlanCache {
-  size_t budget = size_t(16) << 30;
+  size_t total_budget = size_t(16) << 30;  // per process, shared by the live contexts
   std::list<std::string> order;
   std::unordered_map<std::string, std::pair<std::shared_ptr<T>, std::list<std::string>::iterator>>
       map;
@@ -127,6 +136,7 @@ struct PlanCache {
   void trim() {
     size_t total = 0;
     for (const auto& e : map) total += e.second.first->device_bytes();
+    const size_t budget = cache_share(total_budget);
     while (total > budget && order.size() > 1) {
       auto it = map.find(order.front());
       total -= it->second.first->device_bytes();
@@ -161,6 +171,7 @@ struct Context : std::enable_shared_from_this<Context> {
   size_t heff_bytes = 0;
   cudaStream_t copy_stream = nullptr;   // host<->device transfers overlapped with compute
   cudaEvent_t copy_ev[4] = {};          // ... and the events that order them
+  bool counted = false;           // included in g_live_contexts
   int64_t kernel_launches = 0;    // launches of this library's kernels
   bool debug_sync = false;        // MPSG_DEBUG_SYNC=1: synchronise and check after tensor-core GEMMs
   double gemm_flops = 0;          // algorithmic flops issued through block GEMMs

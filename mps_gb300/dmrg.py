@@ -465,7 +465,7 @@ def run_chains(specs, nsweeps: int, opts: SweepOptions, threads: int | None = No
         ctx = mg.Context(device)
         Ws = xxz_u1mpo(L, delta, ctx=ctx)
         mps = mps_from_host(binomial_mps_host(L, L // 2, chi, seed + i), ctx)
-        center_at(mps, 1, svd=opts.svd)
+        center_at(mps, 1, svd=opts.svd, normalize=True)  # long random chains: keep the norm 1
         env = initialenv(mps, Ws)
         o = SweepOptions(**{**opts.__dict__, "maxdim": chi})
         es = None
