@@ -189,8 +189,10 @@ __host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
 }
 
 // (hi + lo) * 2^E as FP64 using integer instructions only (hi, lo normal or zero FP32 values
-// with |lo| <= |hi|).  Bits below 2^-62 of |hi| are truncated.
+// with |lo| <= |hi|; a non-finite hi is returned as is).  Bits below 2^-62 of |hi| are
+// truncated.
 __device__ __forceinline__ double ds_to_f64(float hi, float lo, int E) {
+  if ((__float_as_uint(hi) & 0x7f800000u) == 0x7f800000u) return (double)hi;  // NaN / Inf
   if (hi == 0.f) {
     hi = lo;
     lo = 0.f;
@@ -277,6 +279,7 @@ __device__ __forceinline__ int exp_bound(unsigned long long absbits) {
 }
 
 constexpr int kNoExponent = (int)0x80808080;  // byte pattern of the reset: "row entirely zero"
+constexpr unsigned long long kNonFinite = 0x7ff0000000000000ull;  // |bits| of Inf; NaN above
 
 // One CTA per (problem, block of operand rows, K chunk): chunk exponents e(r,c), and the row
 // reference R(r) = max_c e(r,c) by atomicMax (R is reset to kNoExponent before the pass).
@@ -311,9 +314,10 @@ __global__ void __launch_bounds__(256) pack_exponents_kernel(
       unsigned long long m = 0;
       if (r0 + r < rows)
         for (int64_t k = k0 + kg; k < k1; k += 8) {
-          const unsigned long long b =
+          unsigned long long b =
               (unsigned long long)__double_as_longlong(X[off + (r0 + r) + k * ks]) &
               0x7fffffffffffffffull;
+          if (b >= kNonFinite) b = 0;  // NaN / Inf: packed as NaN slices, not a scale
           m = b > m ? b : m;
         }
       red[kg][r] = m;
@@ -335,8 +339,9 @@ __global__ void __launch_bounds__(256) pack_exponents_kernel(
         if (r >= rows) break;
         unsigned long long m = 0;
         for (int64_t k = k0 + lane; k < k1; k += 32) {
-          const unsigned long long b =
+          unsigned long long b =
               (unsigned long long)__double_as_longlong(X[off + r * rs + k]) & 0x7fffffffffffffffull;
+          if (b >= kNonFinite) b = 0;
           m = b > m ? b : m;
         }
 #pragma unroll
@@ -421,18 +426,19 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
           if constexpr (!kWide) {
             const uint32_t m32 = (((uint32_t)hw << 11) | (lw >> 21)) | 0x80000000u;
             const int s = sbase - eb;  // >= 32 - beta*S > 0 for every element of the row chunk
-            if (eb != 0 && s <= 32 && r < rows) {
+            if (eb != 0 && eb != 0x7ff && s <= 32 && r < rows) {
               F = (int)(((m32 >> (s - 1)) + 1u) >> 1);  // round half up
               if (hw < 0) F = -F;
             }
           } else {
             const uint64_t m53 = ((uint64_t)(((uint32_t)hw & 0xfffffu) | 0x100000u) << 32) | lw;
             const int s = sbase + 21 - eb;  // >= 53 - beta*S >= 4 for up to 7 slices
-            if (eb != 0 && s <= 54 && r < rows) {
+            if (eb != 0 && eb != 0x7ff && s <= 54 && r < rows) {
               F = (long long)(((m53 >> (s - 1)) + 1ull) >> 1);  // round half up
               if (hw < 0) F = -F;
             }
           }
+          const bool nonfinite = eb == 0x7ff && r < rows;  // propagates as NaN through the MMA
 #pragma unroll
           for (int q = 0; q < S; ++q) {
             const int shq = kBeta * (S - 1 - q);
@@ -443,7 +449,8 @@ __global__ void __launch_bounds__(256) pack_slices_kernel(
               tq = (int)t;
             }
             const float v = (float)tq * scale[q];  // exact: |tq| <= 2^beta
-            const uint16_t h = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+            const uint16_t h =
+                nonfinite ? (uint16_t)0x7fc0u : __bfloat16_as_ushort(__float2bfloat16_rn(v));
             if (j & 1) packed[q][j >> 1] |= (uint32_t)h << 16;
             else packed[q][j >> 1] = (uint32_t)h;
           }
@@ -724,6 +731,7 @@ __device__ __forceinline__ double f32_to_f64_scaled(float v, int E) {
   const uint32_t u = __float_as_uint(v);
   const int ef = (int)((u >> 23) & 0xff);
   if (ef == 0) return 0.0;  // zero (FP32 denormals are far below the accuracy of this path)
+  if (ef == 0xff) return (double)v;  // NaN / Inf stay non-finite
   const long long be = (long long)ef - 127 + 1023 + E;
   const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
   if (be <= 0) return 0.0;
