@@ -40,7 +40,7 @@ UNIT = "GFLOP/s"
 DEFAULT_SLICES = 4
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=20)
@@ -74,7 +74,7 @@ def parse():
     p.add_argument("--tdvp-steps", type=int, default=10)
     p.add_argument("--tdvp-precision", type=int, default=0,
                    help="block-GEMM arithmetic of the TDVP contractions (0 = FP64, S = slices)")
-    return p.parse_args()
+    return p.parse_args(argv)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -83,6 +83,22 @@ def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def replica_rate(t_local, flops, ws, device=None):
+    """Whole-job rate of ``ws`` independent replicas, one per rank, each timing the same step.
+
+    The job's step time is the slowest rank's (all-reduce MAX over the default process group; any
+    backend) and one job step does ``ws`` times the flops of one replica. Returns (step time in s,
+    GFLOP/s)."""
+    t = float(t_local)
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([t], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    return t, ws * flops / t / 1e9
 
 
 class ClockSampler:
@@ -329,17 +345,11 @@ def run_ours(args):
         ms = timed_steps(op, args.steps)
     launches = ctx.counters()[0] - launches0
     clocks = cs.summary()
-    t_local = sum(ms) / len(ms) / 1e3
-    t = t_local
-    if ws > 1:
-        tt = torch.tensor([t_local], device=f"cuda:{local}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
-    value = ws * flops / t / 1e9
+    t, value = replica_rate(sum(ms) / len(ms) / 1e3, flops, ws, f"cuda:{local}")
 
     # the plain FP64 drop-in on the same inputs
     ms64 = timed_steps(op64, max(3, min(args.steps, 10))) if S != 0 else ms
-    t64 = sum(ms64) / len(ms64) / 1e3
+    t64, value64 = replica_rate(sum(ms64) / len(ms64) / 1e3, flops, ws, f"cuda:{local}")
 
     # accuracy of this step against the FP64 drop-in
     y = op(v).to_flat()
@@ -368,7 +378,7 @@ def run_ours(args):
         if i >= args.warmup:
             e2e_t.append(t1 - t0)
     e2e_err = float(np.linalg.norm(host_out.numpy() - y64) / np.linalg.norm(y64))
-    e2e_value = ws * flops / statistics.mean(e2e_t) / 1e9
+    _, e2e_value = replica_rate(statistics.mean(e2e_t), flops, ws, f"cuda:{local}")
 
     peaks = measured_peaks()
     step_ms = sum(ms) / len(ms)
@@ -438,7 +448,7 @@ def run_ours(args):
                    "op_build_ms": op_build_ms,
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "flushed before every timed step (512 MiB write)"},
-        "fp64": {"value": ws * flops / t64 / 1e9, "unit": UNIT, "ms_per_step": t64 * 1e3,
+        "fp64": {"value": value64, "unit": UNIT, "ms_per_step": t64 * 1e3,
                  "speedup_mixed_vs_fp64": t64 / t},
         "rel_err_vs_fp64": rel_err,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
