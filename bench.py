@@ -65,6 +65,10 @@ def parse(argv=None):
     p.add_argument("--batched-concurrent-only", action="store_true",
                    help="--batched without the one-after-the-other comparison run")
     p.add_argument("--sweep-chi", type=int, default=None, help="maxdim of the sweep (default chi)")
+    p.add_argument("--sweep-offload", type=int, default=0, metavar="W",
+                   help="also run the mixed sweep with environments in a W-entry device window "
+                        "(the rest in host memory; asynchronous copies with prefetch, and "
+                        "blocking copies)")
     p.add_argument("--sweep-phases", action="store_true",
                    help="also report the sweep's eigensolve / truncation / environment times")
     p.add_argument("--tdvp", action="store_true",
@@ -238,7 +242,7 @@ SWEEP_MIXED = dict(precision=4, energy_precision=7, env_precision=7, svd="gram")
 SWEEP_FP64 = dict(precision=0, energy_precision=0, env_precision=0, svd="exact")
 
 
-def sweep_bench(ctx, chi, lx=32, seed=7, phases=False):
+def sweep_bench(ctx, chi, lx=32, seed=7, phases=False, offload=0):
     """One 2-site DMRG sweep (src/dmrg.jl:58-179) of the L=lx Heisenberg chain (J=1, OBC, Sz=0)
     at maxdim=chi from a random MPS whose bonds hold about chi states (binomial charge profile),
     canonicalised at site 1 with environments built (untimed). The sweep runs twice from copies
@@ -274,6 +278,25 @@ def sweep_bench(ctx, chi, lx=32, seed=7, phases=False):
             pt = gd.PhaseTimer(ctx)
             gd.dmrg2sitesweep(mps, Ws, env, timing=pt, **kw, **cfg)
             breakdown[name] = {k: round(v, 3) for k, v in pt.s.items()}
+    moved = {}
+    if offload:  # the mixed sweep with environments kept off the device
+        from mps_gb300.envstore import OffloadedEnvs
+        for mode in ("async", "blocking"):
+            mps = gd.MPState([mg.copy(A) for A in m0.As], center=1)
+            env = [None if e is None else mg.copy(e) for e in env0]
+            load = (lambda c, s, f: mg.from_flat(c, s, f, ctx)) if mode == "blocking" else None
+            st = OffloadedEnvs(env, window=offload, ctx=ctx, load=load)
+            del env
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            es = gd.dmrg2sitesweep(mps, Ws, st, **kw, **SWEEP_MIXED)
+            ctx.synchronize()
+            moved[mode] = {
+                "sweep_s": time.perf_counter() - t0, "bit_identical": es == emx,
+                "downloads": st.downloads, "uploads": st.uploads,
+                "prefetches": st.prefetches, "prefetch_hits": st.prefetch_hits,
+                "clean_evictions": st.clean_evictions,
+                "GB_down": st.transfer.bytes_down / 1e9, "GB_up": st.transfer.bytes_up / 1e9}
     return {
         "workload": f"one 2-site DMRG sweep, Heisenberg chain L={lx} (J=1, OBC, Sz=0), "
                     f"maxdim={chi}, cutoff 1e-10, Krylov dim 4, maxiter 8, tol 1e-7; initial "
@@ -286,6 +309,8 @@ def sweep_bench(ctx, chi, lx=32, seed=7, phases=False):
         "dE_rel_final": abs(emx[-1] - e64[-1]) / abs(e64[-1]),
         "matvecs_fp64": n64, "matvecs_mixed": nmx, "energies_per_sweep": len(e64),
         **({"phases_s": breakdown} if phases else {}),
+        **({"offloaded_envs": {"window": offload, "resident_mixed_s": tmx, **moved}}
+           if offload else {}),
     }
 
 
@@ -462,7 +487,8 @@ def run_ours(args):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_sweep and ws == 1:
-        line["sweep"] = sweep_bench(ctx, args.sweep_chi or args.chi, phases=args.sweep_phases)
+        line["sweep"] = sweep_bench(ctx, args.sweep_chi or args.chi, phases=args.sweep_phases,
+                                    offload=args.sweep_offload)
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
         os.environ.setdefault("OPENBLAS_NUM_THREADS", str(os.cpu_count() or 1))
         vv, n, tm, cores = cpu_heff_rate(args.chi, flops)

@@ -84,6 +84,29 @@ int mpsg_tensor_download(const mpsg_tensor* t, double* host, int64_t nelem);
 /* Raw device pointer of the flat buffer (for callers that keep data resident). */
 int mpsg_tensor_device_ptr(const mpsg_tensor* t, double** dptr);
 int mpsg_tensor_copy(mpsg_ctx* ctx, const mpsg_tensor* t, mpsg_tensor** out);
+/* ---- asynchronous host copies (src/dmrg_envio.jl:5-261 keeps environments in files and
+ * moves them with @async tasks; here they move between HBM and pinned host memory on the
+ * context's copy stream while the context stream computes) -------------------------------- */
+typedef struct mpsg_copy mpsg_copy;
+/* Page-locked host memory for nelem doubles (the copies below overlap compute only from it). */
+int mpsg_host_alloc(int64_t nelem, double** host);
+int mpsg_host_free(double* host);
+/* Starts t -> host (download) or host -> t (upload) after the work queued so far on the
+ * context stream; t must belong to ctx and nelem must equal its size. The copy holds t's device
+ * memory until it completes, so t may be freed at once. host must stay valid until the copy
+ * completes. Context-stream work that reads an uploaded t must come after mpsg_copy_wait. */
+int mpsg_tensor_download_async(mpsg_ctx* ctx, const mpsg_tensor* t, double* host, int64_t nelem,
+                               mpsg_copy** copy);
+int mpsg_tensor_upload_async(mpsg_ctx* ctx, mpsg_tensor* t, const double* host, int64_t nelem,
+                             mpsg_copy** copy);
+/* Orders the context stream after the copy without waiting on the host. */
+int mpsg_copy_wait(mpsg_ctx* ctx, mpsg_copy* copy);
+/* *done = 1 once the copy has completed, else 0. */
+int mpsg_copy_query(mpsg_copy* copy, int32_t* done);
+/* Waits on the host until the copy has completed. */
+int mpsg_copy_synchronize(mpsg_copy* copy);
+/* Releases the handle (waiting on the host first if the copy is still running). */
+int mpsg_copy_free(mpsg_copy* copy);
 /* dual(A): negated charge, flipped leg flags, same blocks (symtensor.jl:201-212). */
 int mpsg_dual(mpsg_ctx* ctx, const mpsg_tensor* a, mpsg_tensor** out);
 

@@ -70,6 +70,14 @@ SIGNATURES = {
     "mpsg_tensor_upload": [P, PF64, I64],
     "mpsg_tensor_download": [P, PF64, I64],
     "mpsg_tensor_device_ptr": [P, PP],
+    "mpsg_host_alloc": [I64, PP],
+    "mpsg_host_free": [P],
+    "mpsg_tensor_download_async": [P, P, P, I64, PP],
+    "mpsg_tensor_upload_async": [P, P, P, I64, PP],
+    "mpsg_copy_wait": [P, P],
+    "mpsg_copy_query": [P, PI32],
+    "mpsg_copy_synchronize": [P],
+    "mpsg_copy_free": [P],
     "mpsg_tensor_copy": [P, P, PP],
     "mpsg_dual": [P, P, PP],
     "mpsg_permutelegs": [P, P, PI32, PP],

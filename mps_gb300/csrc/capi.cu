@@ -228,6 +228,88 @@ int mpsg_tensor_download(const mpsg_tensor* t, double* host, int64_t n) {
   });
 }
 
+struct mpsg_copy {
+  std::unique_ptr<mpsg::AsyncCopy> c;
+};
+
+int mpsg_host_alloc(int64_t n, double** host) {
+  return guarded([&] {
+    need(host, "host");
+    if (n < 0) throw mpsg::Error(mpsg::kErrArgument, "host_alloc: negative size");
+    *host = nullptr;
+    MPSG_CUDA(cudaMallocHost((void**)host, sizeof(double) * (size_t)std::max<int64_t>(n, 1)));
+  });
+}
+
+int mpsg_host_free(double* host) {
+  return guarded([&] {
+    if (host) MPSG_CUDA(cudaFreeHost(host));
+  });
+}
+
+static void check_async_args(mpsg_ctx* ctx, const mpsg_tensor* t, const void* host, int64_t n,
+                             mpsg_copy** copy) {
+  need(ctx, "ctx");
+  need(t, "t");
+  need(copy, "copy");
+  if (t->t.ctx != &ctx->c)
+    throw mpsg::Error(mpsg::kErrArgument, "async copy: tensor belongs to another context");
+  if (n != t->t.meta.total) throw mpsg::Error(mpsg::kErrArgument, "async copy: size mismatch");
+  if (n) need(host, "host");
+}
+
+int mpsg_tensor_download_async(mpsg_ctx* ctx, const mpsg_tensor* t, double* host, int64_t n,
+                               mpsg_copy** copy) {
+  return guarded([&] {
+    check_async_args(ctx, t, host, n, copy);
+    auto c = mpsg::copy_async(&ctx->c, t->t, host, /*to_host=*/true);
+    *copy = new mpsg_copy{std::move(c)};
+  });
+}
+
+int mpsg_tensor_upload_async(mpsg_ctx* ctx, mpsg_tensor* t, const double* host, int64_t n,
+                             mpsg_copy** copy) {
+  return guarded([&] {
+    check_async_args(ctx, t, host, n, copy);
+    auto c = mpsg::copy_async(&ctx->c, t->t, const_cast<double*>(host), /*to_host=*/false);
+    *copy = new mpsg_copy{std::move(c)};
+  });
+}
+
+int mpsg_copy_wait(mpsg_ctx* ctx, mpsg_copy* copy) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(copy, "copy");
+    MPSG_CUDA(cudaStreamWaitEvent(ctx->c.stream, copy->c->done, 0));
+  });
+}
+
+int mpsg_copy_query(mpsg_copy* copy, int32_t* done) {
+  return guarded([&] {
+    need(copy, "copy");
+    need(done, "done");
+    cudaError_t e = cudaEventQuery(copy->c->done);
+    if (e == cudaErrorNotReady) {
+      (void)cudaGetLastError();  // not an error: the copy is still running
+      *done = 0;
+      return;
+    }
+    MPSG_CUDA(e);
+    *done = 1;
+  });
+}
+
+int mpsg_copy_synchronize(mpsg_copy* copy) {
+  return guarded([&] {
+    need(copy, "copy");
+    MPSG_CUDA(cudaEventSynchronize(copy->c->done));
+  });
+}
+
+int mpsg_copy_free(mpsg_copy* copy) {
+  return guarded([&] { delete copy; });
+}
+
 int mpsg_tensor_device_ptr(const mpsg_tensor* t, double** p) {
   return guarded([&] {
     need(t, "t");

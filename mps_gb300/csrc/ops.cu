@@ -364,14 +364,46 @@ DeviceTensor applymps2site(Context* ctx, const DeviceTensor& v, const DeviceTens
   return contract(ctx, t3, kH4A, envR, kH4B, precision, nullptr);
 }
 
+void ensure_copy_stream(Context* ctx) {
+  if (ctx->copy_stream) return;
+  MPSG_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  for (auto& e : ctx->copy_ev) MPSG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+}
+
+AsyncCopy::~AsyncCopy() {
+  if (done) {
+    cudaEventSynchronize(done);
+    cudaEventDestroy(done);
+  }
+}
+
+std::unique_ptr<AsyncCopy> copy_async(Context* ctx, const DeviceTensor& t, double* host,
+                                      bool to_host) {
+  ensure_copy_stream(ctx);
+  auto c = std::make_unique<AsyncCopy>();
+  c->owner = ctx->shared_from_this();
+  c->buf = t.buf;
+  MPSG_CUDA(cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming));
+  // after the kernels that wrote t (download), or t's allocation and every queued reader of its
+  // old contents (upload)
+  MPSG_CUDA(cudaEventRecord(ctx->copy_ev[3], ctx->stream));
+  MPSG_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[3], 0));
+  const size_t bytes = sizeof(double) * (size_t)t.meta.total;
+  if (bytes) {
+    if (to_host)
+      MPSG_CUDA(cudaMemcpyAsync(host, t.data(), bytes, cudaMemcpyDeviceToHost, ctx->copy_stream));
+    else
+      MPSG_CUDA(cudaMemcpyAsync(t.data(), host, bytes, cudaMemcpyHostToDevice, ctx->copy_stream));
+  }
+  MPSG_CUDA(cudaEventRecord(c->done, ctx->copy_stream));
+  return c;
+}
+
 DeviceTensor applymps2site_host(Context* ctx, const DeviceTensor& v, const DeviceTensor& envL,
                                 const DeviceTensor& envR, const DeviceTensor& W1,
                                 const DeviceTensor& W2, const double* const host_in[5],
                                 int precision, double* host_out) {
-  if (!ctx->copy_stream) {
-    MPSG_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
-    for (auto& e : ctx->copy_ev) MPSG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  }
+  ensure_copy_stream(ctx);
   cudaStream_t cs = ctx->copy_stream;
   // the uploads overwrite the inputs: after everything already queued on the context stream
   MPSG_CUDA(cudaEventRecord(ctx->copy_ev[3], ctx->stream));

@@ -115,4 +115,17 @@ DeviceTensor applymps2site_host(Context* ctx, const DeviceTensor& v, const Devic
                                 int precision, double* host_out);
 DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v);
 
+// One host<->device copy on the context's copy stream, started after the work queued so far on
+// the context stream. It holds the tensor's device buffer, so the tensor may be released at once;
+// destroying an unfinished copy waits for it on the host.
+struct AsyncCopy {
+  std::shared_ptr<Context> owner;
+  std::shared_ptr<Buffer> buf;
+  cudaEvent_t done = nullptr;
+  ~AsyncCopy();
+};
+void ensure_copy_stream(Context* ctx);
+std::unique_ptr<AsyncCopy> copy_async(Context* ctx, const DeviceTensor& t, double* host,
+                                      bool to_host);
+
 }  // namespace mpsg

@@ -332,6 +332,14 @@ def _truncate_and_energy(v, AA, env, Ws, l, o: SweepOptions, keep="left", tick=N
     return u, s, vt, AA, e, truncerr
 
 
+def _prefetch(env, i):
+    """Hint to an environment store that keeps entries off the device (``OffloadedEnvs``):
+    entry ``i`` is read soon. Plain lists ignore it."""
+    f = getattr(env, "prefetch", None)
+    if f is not None and 0 <= i < len(env):
+        f(i)
+
+
 def _eig(AA, env, Ws, l, o: SweepOptions, stats):
     e, v, info = mg.eigsolve_heff2(AA, env[l - 1], env[l + 2], Ws[l - 1], Ws[l],
                                    krylovdim=o.krylovdim, maxiter=o.krylovmaxiter,
@@ -375,6 +383,7 @@ def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stat
     A = mps.As[0]
     t = now()
     for l in range(1, lx - 1):
+        _prefetch(env, l + 3)  # the right environment of the next bond
         AA = mg.contract(A, (1, 2, -1), mps.As[l], (-1, 3, 4), precision=0)
         v = _eig(AA, env, Ws, l, o, stats)
         t = tick("eigsolve", t)
@@ -391,6 +400,7 @@ def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stat
     t = tick("eigsolve", t)
     e = None
     for l in range(lx - 1, 1, -1):
+        _prefetch(env, l - 2)  # the left environment of the next bond
         u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o, keep="right",
                                                   tick=timing)
         energies.append(e)

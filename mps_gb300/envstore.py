@@ -1,41 +1,142 @@
 """Environment residency for long sweeps (the role of src/dmrg_envio.jl:5-261, which keeps every
-environment in a file and loads it when the sweep reaches it).
+environment in a file and moves it with ``@async`` tasks when the sweep reaches it).
 
 ``OffloadedEnvs`` stands in for the environment list of ``dmrg2sitesweep`` (which only indexes
-it): at most ``window`` environments stay on the device, least recently used ones move to host
-memory (downloaded before their device memory is released) and come back when the sweep reads
-them again. A sweep touches each environment a few times per bond, so with a window of a few
-bonds the traffic is about one environment down and one up per bond, small next to the
-contractions that produce them. The stored values are exact copies: a sweep gives bit-identical
-results with any window.
+it): at most ``window`` environments stay on the device and the least recently used ones move
+to host memory. By default the copies run on the context's copy stream, between HBM and
+page-locked host buffers, while the context stream computes:
+
+* an evicted environment is downloaded asynchronously; its device memory is released when the
+  copy has finished, and the host buffer is reused only after every copy that uses it is done;
+* a host copy is uploaded asynchronously and the context stream is ordered after the upload
+  (no host wait), either when the sweep reads the entry or earlier, through ``prefetch(i)``,
+  which the sweep calls about one bond ahead so that the copy overlaps the eigensolve;
+* a host copy stays valid until the entry is written again, so evicting an environment that
+  was only read costs no copy at all.
+
+The stored values are exact copies: a sweep gives bit-identical results with any window.
 """
 from __future__ import annotations
+
+
+class SyncTransfer:
+    """Blocking copies through NumPy arrays: ``to_flat()`` down, ``load(charge, space, flat)``
+    up. Works with any tensor type that has ``charge``, ``space`` and ``to_flat()``."""
+
+    def __init__(self, load):
+        self.load = load
+        self.bytes_down = self.bytes_up = 0
+
+    def download(self, t):
+        flat = t.to_flat()
+        self.bytes_down += flat.nbytes
+        return (t.charge, t.space, flat), None
+
+    def upload(self, entry):
+        charge, space, flat = entry
+        self.bytes_up += flat.nbytes
+        return self.load(charge, space, flat), None
+
+    def ready(self, copy):
+        return True
+
+    def order(self, copy):
+        pass
+
+    def release(self, entry):
+        pass
+
+
+class PinnedPool:
+    """Reusable page-locked host buffers (``HostBuffer``): a request takes the smallest free
+    buffer of at least ``n`` and at most ``2 n`` doubles, else a new one; at most ``keep``
+    free buffers are held."""
+
+    def __init__(self, alloc=None, keep: int = 8):
+        if alloc is None:
+            from .symtensors import HostBuffer as alloc
+        self._alloc = alloc
+        self._free = []
+        self.keep = keep
+        self.allocated = 0
+
+    def take(self, n: int):
+        best = None
+        for b in self._free:
+            if n <= b.n <= 2 * max(n, 1) and (best is None or b.n < best.n):
+                best = b
+        if best is not None:
+            self._free.remove(best)
+            return best
+        self.allocated += 1
+        return self._alloc(n)
+
+    def give(self, b):
+        self._free.append(b)
+        if len(self._free) > self.keep:
+            self._free.pop(0)
+
+
+class AsyncTransfer:
+    """Copies on the context's copy stream between device tensors and pinned host buffers
+    (``download_async`` / ``upload_async``)."""
+
+    def __init__(self, ctx=None, pool=None):
+        self.ctx = ctx
+        self.pool = pool if pool is not None else PinnedPool()
+        self.bytes_down = self.bytes_up = 0
+
+    def download(self, t):
+        from . import symtensors as mg
+        if self.ctx is None:
+            self.ctx = t.ctx
+        n = t.numel()
+        buf = self.pool.take(n)
+        self.bytes_down += 8 * n
+        return (t.charge, t.space, buf), mg.download_async(t, buf)
+
+    def upload(self, entry):
+        from . import symtensors as mg
+        charge, space, buf = entry
+        t = mg.zeros(charge, space, self.ctx)
+        self.bytes_up += 8 * t.numel()
+        return t, mg.upload_async(t, buf)
+
+    def ready(self, copy):
+        return copy.query()
+
+    def order(self, copy):
+        copy.wait()
+
+    def release(self, entry):
+        self.pool.give(entry[2])
 
 
 class OffloadedEnvs:
     """List-like store of environments with a device-resident window of ``window`` entries.
 
-    ``load(charge, space, flat)`` rebuilds a device tensor from its host copy (default: the
-    library's ``from_flat`` on ``ctx``); stored tensors need ``charge``, ``space`` and
-    ``to_flat()``."""
+    ``transfer`` moves the data (default: ``AsyncTransfer`` on ``ctx``; ``load`` given instead
+    selects blocking ``SyncTransfer`` copies with that loader)."""
 
-    def __init__(self, envs, window: int = 6, ctx=None, load=None):
+    def __init__(self, envs, window: int = 6, ctx=None, load=None, transfer=None):
         if window < 1:
             raise ValueError("window must be at least 1")
-        if load is None:
-            from . import symtensors as mg
-
-            def load(charge, space, flat):
-                return mg.from_flat(charge, space, flat, ctx)
-
-        self._load = load
+        if transfer is None:
+            transfer = SyncTransfer(load) if load is not None else AsyncTransfer(ctx)
+        self.transfer = transfer
         self.window = window
         self._n = len(envs)
-        self._dev = {}
-        self._host = {}
-        self._order = []  # device-resident indices, least recently used first
+        self._dev = {}       # index -> device tensor
+        self._host = {}      # index -> host entry (valid copy of the entry's current value)
+        self._busy = {}      # index -> copies in flight that use the host entry's buffer
+        self._pending = {}   # index -> upload not yet ordered before the context stream
+        self._retired = []   # (copies, host entry) of overwritten entries, released when done
+        self._order = []     # device-resident indices, least recently used first
         self.uploads = 0
         self.downloads = 0
+        self.prefetches = 0
+        self.prefetch_hits = 0
+        self.clean_evictions = 0
         for i, e in enumerate(envs):
             if e is not None:
                 self[i] = e
@@ -55,31 +156,85 @@ class OffloadedEnvs:
             self._order.remove(i)
         self._order.append(i)
 
+    def _reap(self):
+        ready = self.transfer.ready
+        for i in list(self._busy):
+            left = [c for c in self._busy[i] if not ready(c)]
+            if left:
+                self._busy[i] = left
+            else:
+                del self._busy[i]
+        keep = []
+        for copies, entry in self._retired:
+            copies = [c for c in copies if not ready(c)]
+            if copies:
+                keep.append((copies, entry))
+            else:
+                self.transfer.release(entry)
+        self._retired = keep
+
     def _evict(self):
         while len(self._dev) > self.window:
-            j = self._order.pop(0)
+            # prefetched entries the sweep has not read yet go last
+            cand = [j for j in self._order if j not in self._pending] or self._order
+            j = cand[0]
+            self._order.remove(j)
+            self._pending.pop(j, None)
             t = self._dev.pop(j)
-            self._host[j] = (t.charge, t.space, t.to_flat())
+            if j in self._host:
+                self.clean_evictions += 1
+                continue
+            entry, c = self.transfer.download(t)
+            self._host[j] = entry
+            if c is not None:
+                self._busy.setdefault(j, []).append(c)
             self.downloads += 1
+
+    def _fetch(self, i, order_now):
+        t, c = self.transfer.upload(self._host[i])
+        self.uploads += 1
+        if c is not None:
+            self._busy.setdefault(i, []).append(c)
+            if order_now:
+                self.transfer.order(c)
+            else:
+                self._pending[i] = c
+        self._dev[i] = t
+        self._touch(i)
+        self._evict()
+        return t
 
     def __getitem__(self, i):
         i = self._index(i)
+        self._reap()
         if i in self._dev:
+            c = self._pending.pop(i, None)
+            if c is not None:
+                self.transfer.order(c)
+                self.prefetch_hits += 1
             self._touch(i)
             return self._dev[i]
         if i in self._host:
-            charge, space, flat = self._host.pop(i)
-            t = self._load(charge, space, flat)
-            self.uploads += 1
-            self._dev[i] = t
-            self._touch(i)
-            self._evict()
-            return t
+            return self._fetch(i, order_now=True)
         return None
+
+    def prefetch(self, i) -> bool:
+        """Starts the upload of entry ``i`` if it lives only on the host; the context stream is
+        ordered after it when the entry is read."""
+        i = self._index(i)
+        if i in self._dev or i not in self._host:
+            return False
+        self._reap()
+        self._fetch(i, order_now=False)
+        self.prefetches += 1
+        return True
 
     def __setitem__(self, i, t):
         i = self._index(i)
-        self._host.pop(i, None)
+        self._reap()
+        if i in self._host:
+            self._retired.append((self._busy.pop(i, []), self._host.pop(i)))
+        self._pending.pop(i, None)
         if t is None:
             self._dev.pop(i, None)
             if i in self._order:
@@ -92,3 +247,8 @@ class OffloadedEnvs:
     def resident(self):
         """Indices held on the device, least recently used first."""
         return list(self._order)
+
+    def in_flight(self) -> int:
+        """Copies not yet known to have completed."""
+        self._reap()
+        return sum(len(v) for v in self._busy.values()) + sum(len(c) for c, _ in self._retired)

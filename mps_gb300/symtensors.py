@@ -27,7 +27,8 @@ __all__ = [
     "mpsupdateleft",
     "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision", "_svd_",
     "svdtrunc", "svd_complex", "dots", "lincomb", "truncatedsizes", "small_eigh",
-    "eigsolve_heff2", "EigInfo", "Heff2",
+    "eigsolve_heff2", "EigInfo", "Heff2", "HostBuffer", "Copy", "download_async",
+    "upload_async",
 ]
 
 
@@ -381,6 +382,82 @@ def meta(charge, space) -> SymTensor:
 def from_flat(charge, space, flat, ctx=None) -> SymTensor:
     t = zeros(charge, space, ctx)
     return t.upload(flat)
+
+
+class HostBuffer:
+    """Page-locked host memory for ``n`` doubles (``mpsg_host_alloc``); ``array`` is a NumPy view
+    of it. Asynchronous copies overlap compute only from such memory."""
+
+    def __init__(self, n: int):
+        p = C.c_void_p()
+        call("mpsg_host_alloc", int(n), C.byref(p))
+        self._p = p
+        self.n = int(n)
+        self.array = np.ctypeslib.as_array(C.cast(p, _lib.PF64), shape=(max(self.n, 1),))[:self.n]
+
+    @property
+    def ptr(self):
+        return self._p
+
+    def __del__(self):
+        try:
+            if self._p:
+                self.array = None
+                _lib.lib.mpsg_host_free(self._p)
+                self._p = None
+        except Exception:
+            pass
+
+
+class Copy:
+    """A host<->device copy running on the context's copy stream (``mpsg_copy``). The library
+    keeps the tensor's device memory until the copy has completed; this object keeps the host
+    buffer, and releasing it first waits for the copy."""
+
+    def __init__(self, h, ctx, host):
+        self._h, self.ctx, self._host = h, ctx, host
+
+    def wait(self):
+        """Orders later work on the context stream after the copy (no host wait)."""
+        call("mpsg_copy_wait", self.ctx.handle, self._h)
+
+    def query(self) -> bool:
+        d = C.c_int32()
+        call("mpsg_copy_query", self._h, C.byref(d))
+        return bool(d.value)
+
+    def synchronize(self):
+        call("mpsg_copy_synchronize", self._h)
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.lib.mpsg_copy_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def download_async(t: SymTensor, host: HostBuffer) -> Copy:
+    """Starts the copy of ``t``'s flat data into ``host.array[:t.numel()]`` after the work queued
+    so far on ``t``'s context stream (``mpsg_tensor_download_async``)."""
+    n = t.numel()
+    if host.n < n:
+        raise MPSGError(_lib.ERR_ARGUMENT, "download_async: host buffer too small")
+    h = C.c_void_p()
+    call("mpsg_tensor_download_async", t.ctx.handle, t.handle, host.ptr, n, C.byref(h))
+    return Copy(h, t.ctx, host)
+
+
+def upload_async(t: SymTensor, host: HostBuffer) -> Copy:
+    """Starts the copy of ``host.array[:t.numel()]`` into ``t``; call ``wait()`` on the result
+    before queueing work that reads ``t`` (``mpsg_tensor_upload_async``)."""
+    n = t.numel()
+    if host.n < n:
+        raise MPSGError(_lib.ERR_ARGUMENT, "upload_async: host buffer too small")
+    h = C.c_void_p()
+    call("mpsg_tensor_upload_async", t.ctx.handle, t.handle, host.ptr, n, C.byref(h))
+    return Copy(h, t.ctx, host)
 
 
 def from_blocks(charge, space, blocks, ctx=None) -> SymTensor:

@@ -42,3 +42,155 @@ def test_window_and_exact_round_trips():
         st[10]
     with pytest.raises(ValueError):
         OffloadedEnvs(envs, window=0, load=load)
+
+
+# ---- asynchronous transfers: a fake copy stream whose copies finish when the test says so -----
+class _Stream:
+    def __init__(self):
+        self.queue = []  # copies in issue order (one in-order copy stream)
+
+    def complete(self, k=None):
+        k = len(self.queue) if k is None else min(k, len(self.queue))
+        for _ in range(k):
+            self.queue.pop(0).run()
+
+    def run_until(self, c):
+        while c in self.queue:
+            self.complete(1)
+
+
+class _Buf:
+    def __init__(self, n):
+        self.n, self.data, self.users = n, np.full(max(n, 1), np.nan), 0
+
+
+class _Copy:
+    def __init__(self, stream, fn, buf):
+        self.done, self.fn, self.buf = False, fn, buf
+        buf.users += 1
+        stream.queue.append(self)
+
+    def run(self):
+        self.fn()
+        self.done = True
+        self.buf.users -= 1
+
+
+class _T:
+    """Device tensor stand-in; ``space = (name, index, n)`` carries its size."""
+
+    def __init__(self, charge, space, flat):
+        self.charge, self.space, self.flat = charge, space, flat
+        self.unordered = None  # upload the context stream is not yet ordered after
+        self.after = None
+
+    def numel(self):
+        return self.space[2]
+
+
+class _FakeAsync:
+    def __init__(self, stream):
+        from mps_gb300.envstore import PinnedPool
+        self.stream = stream
+        self.pool = PinnedPool(alloc=_Buf, keep=2)
+
+    def download(self, t):
+        buf = self.pool.take(t.numel())
+        assert buf.users == 0, "pinned buffer reused while a copy still uses it"
+        n = t.numel()
+        c = _Copy(self.stream, lambda: buf.data.__setitem__(slice(0, n), t.flat), buf)
+        return (t.charge, t.space, buf), c
+
+    def upload(self, entry):
+        charge, space, buf = entry
+        n = space[2]
+        t = _T(charge, space, np.full(n, np.nan))
+        c = _Copy(self.stream, lambda: t.flat.__setitem__(slice(None), buf.data[:n]), buf)
+        c.dst = t
+        t.unordered = c
+        return t, c
+
+    def ready(self, c):
+        return c.done
+
+    def order(self, c):
+        c.dst.unordered = None
+        c.dst.after = c
+
+    def release(self, entry):
+        assert entry[2].users == 0, "host copy released while a copy still uses it"
+        self.pool.give(entry[2])
+
+
+def _read(stream, t):
+    """What a kernel on the context stream sees when it reads t."""
+    assert t.unordered is None, "read before the context stream was ordered after the upload"
+    if t.after is not None:
+        stream.run_until(t.after)
+    return t.flat.copy()
+
+
+@pytest.mark.parametrize("seed,lazy", [(0, False), (1, False), (2, True), (3, True)])
+def test_async_transfers_in_a_sweep_pattern(seed, lazy):
+    """lazy: copies finish only when a read needs them, so downloads are still running when
+    their entries are overwritten or their buffers come up for reuse."""
+    rng = np.random.default_rng(seed)
+    lx = 12
+    stream = _Stream()
+    sizes = [int(rng.integers(3, 9)) for _ in range(lx + 2)]
+    envs = [_T(0, ("E", i, sizes[i]), rng.standard_normal(sizes[i])) for i in range(lx + 2)]
+    want = {i: e.flat.copy() for i, e in enumerate(envs)}
+    st = OffloadedEnvs(envs, window=3, transfer=_FakeAsync(stream))
+
+    def check(i):
+        got = _read(stream, st[i])
+        np.testing.assert_array_equal(got, want[i])
+        return got
+
+    def write(i, base):
+        flat = base + 0.5 * i
+        want[i] = flat.copy()
+        st[i] = _T(0, ("E", i, flat.size), flat)
+
+    for _ in range(2):  # two full sweeps, copies finishing at random points
+        for l in range(1, lx - 1):
+            st.prefetch(min(l + 3, lx + 1))
+            stream.complete(0 if lazy else int(rng.integers(0, 3)))
+            check(l + 2)
+            write(l, np.resize(check(l - 1), sizes[l]))
+            assert len(st.resident()) <= 4
+        for l in range(lx - 1, 1, -1):
+            st.prefetch(l - 2)
+            stream.complete(0 if lazy else int(rng.integers(0, 3)))
+            check(l - 1)
+            write(l + 1, np.resize(check(l + 2), sizes[l + 1]))
+    stream.complete()
+    assert st.in_flight() == 0
+    for i in range(lx + 2):
+        check(i)
+    assert st.prefetches > 0 and st.prefetch_hits > 0
+    assert st.clean_evictions > 0 and st.downloads > 0 and st.uploads > 0
+
+
+def test_overwrite_during_copies_defers_the_buffer():
+    """An entry overwritten while its download (or a prefetched upload) is still running keeps
+    its host buffer out of the pool until those copies finish."""
+    stream = _Stream()
+    tr = _FakeAsync(stream)
+    a = _T(0, ("E", 0, 4), np.arange(4.0))
+    b = _T(0, ("E", 1, 4), np.arange(4.0) + 10)
+    st = OffloadedEnvs([a, b], window=1, transfer=tr)  # a's download is queued, not finished
+    assert st.downloads == 1 and st.in_flight() == 1
+    st[0] = _T(0, ("E", 0, 4), np.zeros(4))           # overwrite: the download still runs
+    # (and 1 leaves the one-entry window: a second download)
+    assert st.downloads == 2 and st.in_flight() == 2 and not tr.pool._free
+    stream.complete()
+    assert st.in_flight() == 0 and len(tr.pool._free) == 1
+    # now 1 is on the host; prefetch it, then overwrite it before it is read
+    assert st.prefetch(1)
+    st[1] = _T(0, ("E", 1, 4), np.ones(4))
+    assert st.in_flight() >= 1
+    stream.complete()
+    assert st.in_flight() == 0
+    np.testing.assert_array_equal(_read(stream, st[1]), np.ones(4))
+    np.testing.assert_array_equal(_read(stream, st[0]), np.zeros(4))

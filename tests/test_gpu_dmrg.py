@@ -202,9 +202,11 @@ def test_independent_chains_concurrently_equal_one_by_one():
     assert all(e < 0 for e in one)
 
 
-def test_sweep_with_offloaded_environments_is_bit_identical():
-    """A sweep whose environments live in a 3-entry device window (the rest in host memory)
-    gives exactly the energies of the all-resident sweep."""
+@pytest.mark.parametrize("mode", ["async", "blocking"])
+def test_sweep_with_offloaded_environments_is_bit_identical(mode):
+    """A sweep whose environments live in a 3-entry device window (the rest in host memory,
+    moved by asynchronous copies with prefetch, or by blocking ones) gives exactly the energies
+    of the all-resident sweep."""
     from mps_gb300.envstore import OffloadedEnvs
     lx, chi = 16, 32
     _, md, _, Wd, _, ed = heisenberg_setup(lx, chi, seed=3)
@@ -213,10 +215,14 @@ def test_sweep_with_offloaded_environments_is_bit_identical():
         mps = gd.MPState([mg.copy(A) for A in md.As], center=1)
         env = [None if e is None else mg.copy(e) for e in ed]
         if window:
-            env = OffloadedEnvs(env, window=window)
+            load = (lambda c, s, f: mg.from_flat(c, s, f)) if mode == "blocking" else None
+            env = OffloadedEnvs(env, window=window, load=load)
         es = gd.dmrg2sitesweep(mps, Wd, env, maxdim=chi, tol=1e-10, krylovdim=4,
                                krylovmaxiter=8)
         res.append(es)
         if window:
             assert env.downloads > 0 and env.uploads > 0
+            assert env.prefetches > 0 and env.clean_evictions > 0
+            if mode == "async":  # blocking prefetches finish at once: nothing is pending
+                assert env.prefetch_hits > 0
     assert res[0] == res[1]
