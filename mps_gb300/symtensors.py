@@ -386,23 +386,28 @@ def from_flat(charge, space, flat, ctx=None) -> SymTensor:
 
 class HostBuffer:
     """Page-locked host memory for ``n`` doubles (``mpsg_host_alloc``); ``array`` is a NumPy view
-    of it. Asynchronous copies overlap compute only from such memory."""
+    of it that keeps the memory alive. Asynchronous copies overlap compute only from such
+    memory."""
 
     def __init__(self, n: int):
         p = C.c_void_p()
         call("mpsg_host_alloc", int(n), C.byref(p))
         self._p = p
         self.n = int(n)
-        self.array = np.ctypeslib.as_array(C.cast(p, _lib.PF64), shape=(max(self.n, 1),))[:self.n]
 
     @property
     def ptr(self):
         return self._p
 
+    @property
+    def array(self) -> np.ndarray:
+        raw = (C.c_double * max(self.n, 1)).from_address(self._p.value)
+        raw._owner = self  # the view's base holds the buffer
+        return np.frombuffer(raw, dtype=np.float64, count=self.n)
+
     def __del__(self):
         try:
             if self._p:
-                self.array = None
                 _lib.lib.mpsg_host_free(self._p)
                 self._p = None
         except Exception:
