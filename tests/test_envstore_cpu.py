@@ -194,3 +194,17 @@ def test_overwrite_during_copies_defers_the_buffer():
     assert st.in_flight() == 0
     np.testing.assert_array_equal(_read(stream, st[1]), np.ones(4))
     np.testing.assert_array_equal(_read(stream, st[0]), np.zeros(4))
+
+
+def test_pinned_pool_best_fit_and_bound():
+    from mps_gb300.envstore import PinnedPool
+    pool = PinnedPool(alloc=_Buf, keep=2)
+    a, b, c = pool.take(10), pool.take(40), pool.take(15)
+    assert pool.allocated == 3
+    for x in (a, b, c):
+        pool.give(x)
+    assert len(pool._free) == 2            # the oldest free buffer was dropped
+    assert pool.take(8) is c               # smallest free buffer within 2x
+    assert pool.take(8) is not b           # b (40) is more than twice 8: a new buffer
+    assert pool.allocated == 4
+    assert pool.take(25) is b              # 40 <= 2 * 25
