@@ -52,6 +52,13 @@ int mpsg_ctx_synchronize(mpsg_ctx* ctx);
 /* Counters: kernels launched by this library and algorithmic block-GEMM flops issued. */
 int mpsg_ctx_counters(mpsg_ctx* ctx, int64_t* kernel_launches, double* gemm_flops);
 int mpsg_ctx_clear_caches(mpsg_ctx* ctx);
+/* Debug library only (libmpsgb300_checked.so, built with MPSG_DEVICE_CHECKS): the copy kernel
+ * recomputes every block offset it decodes by plain division, checks every address against its
+ * task's span, and records a violation instead of making the access (no counterpart in the
+ * reference, whose arrays are bounds-checked by Julia). Returns the violations since the last
+ * reset and the first one as {kind (1 task lookup, 2 decode, 3 span), task, index, detail};
+ * reset = 1 clears them. The normal library returns MPSG_ERR_UNSUPPORTED. */
+int mpsg_device_checks(mpsg_ctx* ctx, int32_t reset, int64_t* violations, int64_t* first);
 /* The context's cudaStream_t, so callers can order their own work (or events) with it. */
 int mpsg_ctx_stream(mpsg_ctx* ctx, void** stream);
 /* Per-kernel CUDA-event timing: when enabled, every launch of kernel class `kind`

@@ -70,6 +70,7 @@ SIGNATURES = {
     "mpsg_tensor_upload": [P, PF64, I64],
     "mpsg_tensor_download": [P, PF64, I64],
     "mpsg_tensor_device_ptr": [P, PP],
+    "mpsg_device_checks": [P, I32, PI64, PI64],
     "mpsg_host_alloc": [I64, PP],
     "mpsg_host_free": [P],
     "mpsg_tensor_download_async": [P, P, P, I64, PP],
@@ -130,7 +131,9 @@ SIGNATURES = {
 
 
 def _load():
-    path = _build.build()  # no-op when the in-tree library is up to date
+    # MPSG_LIBRARY=checked selects the device-checked debug library (same ABI)
+    checked = os.environ.get("MPSG_LIBRARY", "") == "checked"
+    path = _build.build(checked=checked)  # no-op when the in-tree library is up to date
     lib = C.CDLL(path)
     for name, argt in SIGNATURES.items():
         fn = getattr(lib, name)

@@ -3,6 +3,10 @@
 Each translation unit is compiled in parallel into ``mps_gb300/_build/`` and linked into
 ``mps_gb300/libmpsgb300.so``.  Used by ``__graft_entry__.build()`` and by the package on first
 import when the library is missing.  Run ``python -m mps_gb300.build`` to rebuild by hand.
+
+``build(checked=True)`` (``python -m mps_gb300.build --checked``) makes the device-checked debug
+library ``libmpsgb300_checked.so`` instead (objects in ``_build_checked/``, compiled with
+``MPSG_DEVICE_CHECKS``); ``MPSG_LIBRARY=checked`` makes the package load it.
 """
 from __future__ import annotations
 
@@ -39,8 +43,11 @@ def _stale(obj: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, force: bool = False, checked: bool = False) -> str:
+    build_dir = BUILD + "_checked" if checked else BUILD
+    lib = LIB.replace(".so", "_checked.so") if checked else LIB
+    flags = CFLAGS + (["-DMPSG_DEVICE_CHECKS"] if checked else [])
+    os.makedirs(build_dir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".hpp", ".cuh"))]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "mpsgb300.h"))
     cc = nvcc()
@@ -48,10 +55,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
     objs = []
     for src in SOURCES:
         path = os.path.join(CSRC, src)
-        obj = os.path.join(BUILD, src + ".o")
+        obj = os.path.join(build_dir, src + ".o")
         objs.append(obj)
         if force or _stale(obj, [path] + headers):
-            jobs.append([cc, *ARCH, *CFLAGS, "-c", path, "-o", obj])
+            jobs.append([cc, *ARCH, *flags, "-c", path, "-o", obj])
 
     def run(cmd):
         if verbose:
@@ -65,12 +72,12 @@ def build(verbose: bool = False, force: bool = False) -> str:
         for msg in ex.map(run, jobs):
             if verbose and msg:
                 print(msg, flush=True)
-    if force or jobs or not os.path.exists(LIB):
-        tmp = LIB + ".tmp"
+    if force or jobs or not os.path.exists(lib):
+        tmp = lib + ".tmp"
         run([cc, *ARCH, "-shared", "-o", tmp, *objs, *LIBS])
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose=True, force="--force" in sys.argv))
+    print(build(verbose=True, force="--force" in sys.argv, checked="--checked" in sys.argv))

@@ -228,6 +228,15 @@ int mpsg_tensor_download(const mpsg_tensor* t, double* host, int64_t n) {
   });
 }
 
+int mpsg_device_checks(mpsg_ctx* ctx, int32_t reset, int64_t* violations, int64_t* first) {
+  return guarded([&] {
+#ifdef MPSG_DEVICE_CHECKS
+    need(ctx, "ctx");
+#endif
+    mpsg::read_device_checks(ctx ? &ctx->c : nullptr, reset != 0, violations, first);
+  });
+}
+
 struct mpsg_copy {
   std::unique_ptr<mpsg::AsyncCopy> c;
 };

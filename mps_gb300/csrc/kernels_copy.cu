@@ -15,14 +15,35 @@
 //              unit is 256 consecutive destination positions in destination-stride order, one
 //              per lane and step, each decoded to its source address. Writes stay coalesced and
 //              reads follow the source's short runs through the caches.
+//
+// Built with MPSG_DEVICE_CHECKS (the device-checked debug library), the kernel also recomputes
+// every decoded offset by plain division, checks every address against its task's span, records
+// the first violation and a count in device memory (read_device_checks) and skips the access.
 #include <algorithm>
 #include <cstring>
 
+#include "copy_decode.hpp"
 #include "runtime.hpp"
 
 namespace mpsg {
 
 namespace {
+
+#ifdef MPSG_DEVICE_CHECKS
+enum CheckKind { kChkTask = 1, kChkDecode = 2, kChkSpan = 3 };
+__device__ unsigned long long g_chk_count;
+__device__ long long g_chk_first[4];  // kind, task, index, detail
+
+__device__ __noinline__ void chk_fail(int kind, long long task, long long index,
+                                      long long detail) {
+  if (atomicAdd(&g_chk_count, 1ull) == 0ull) {
+    g_chk_first[0] = kind;
+    g_chk_first[1] = task;
+    g_chk_first[2] = index;
+    g_chk_first[3] = detail;
+  }
+}
+#endif
 
 constexpr int kWarps = 8;          // warps per CTA
 // target elements per row-mode unit: small enough that a copy of a few MB spreads over every
@@ -49,13 +70,35 @@ struct WarpView {
   int64_t ext[kMaxTaskDims], sstr[kMaxTaskDims], dstr[kMaxTaskDims];
   uint32_t mag[kMaxTaskDims], shf[kMaxTaskDims];
   int32_t order[kMaxTaskDims];
+#ifdef MPSG_DEVICE_CHECKS
+  int64_t slo, shi, dlo, dhi;  // address spans of the task
+#endif
 };
 
 typedef double TileBuf[kT][kT + 1];
 
-__device__ __forceinline__ uint32_t fdiv(uint32_t n, uint32_t m, uint32_t s) {
-  return (__umulhi(n, m) + n) >> s;
+#ifdef MPSG_DEVICE_CHECKS
+// Offsets of position q over every axis except skip0 / skip1, by plain division, compared with
+// the kernel's magic-number decode; records a mismatch and returns false.
+__device__ bool chk_decode(const WarpView& v, int skip0, int skip1, int64_t q, int64_t so,
+                           int64_t dof) {
+  int ax[kMaxTaskDims];
+  int nax = 0;
+  for (int i = 0; i < v.nd; ++i)
+    if (i != skip0 && i != skip1) ax[nax++] = i;
+  int64_t rs = v.soff, rd = v.doff;
+  ref_decode(v.ext, v.sstr, v.dstr, ax, nax, q, rs, rd);
+  if (rs == so && rd == dof) return true;
+  chk_fail(kChkDecode, v.task, q, rs != so ? so - rs : dof - rd);
+  return false;
 }
+
+__device__ __forceinline__ bool chk_addr(const WarpView& v, int64_t s, int64_t d) {
+  if (s >= v.slo && s <= v.shi && d >= v.dlo && d <= v.dhi) return true;
+  chk_fail(kChkSpan, v.task, s, d);
+  return false;
+}
+#endif
 
 // Dynamic shared memory: kWarps task views, then (only for plans with tile-mode tasks) kWarps
 // transpose tiles; plans without tiles launch with the views alone. 64 registers per thread
@@ -78,6 +121,12 @@ __global__ void __launch_bounds__(32 * kWarps, 4) copy_tasks_kernel(
       if (__ldg(prefix + mid) <= u) lo = mid;
       else hi = mid - 1;
     }
+#ifdef MPSG_DEVICE_CHECKS
+    if (lo < 0 || lo >= ntasks || __ldg(prefix + lo) > u || __ldg(prefix + lo + 1) <= u) {
+      if (lane == 0) chk_fail(kChkTask, lo, u, 0);
+      continue;
+    }
+#endif
     if (lo != v.task) {
       __syncwarp();
       const CopyTask& T = tasks[lo];
@@ -102,6 +151,10 @@ __global__ void __launch_bounds__(32 * kWarps, 4) copy_tasks_kernel(
         v.doff = T.doff;
         v.first = prefix[lo];
         v.task = lo;
+#ifdef MPSG_DEVICE_CHECKS
+        task_span(T.ext, T.sstr, nd, T.soff, v.slo, v.shi);
+        task_span(T.ext, T.dstr, nd, T.doff, v.dlo, v.dhi);
+#endif
       }
       __syncwarp();
     }
@@ -132,15 +185,29 @@ __global__ void __launch_bounds__(32 * kWarps, 4) copy_tasks_kernel(
           so += ii * v.sstr[i];
           dof += ii * v.dstr[i];
         }
+#ifdef MPSG_DEVICE_CHECKS
+        if (row >= v.outer || c0 < 0 || c1 > ea || !chk_decode(v, a, -1, row, so, dof)) {
+          if (lane == 0 && (row >= v.outer || c0 < 0 || c1 > ea)) chk_fail(kChkSpan, v.task, row, c1);
+          continue;
+        }
+#endif
         // four loads in flight per lane before the stores
         for (int64_t ia = c0 + lane; ia < c1; ia += 128) {
           double x[4];
+          bool ok[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            ok[k] = ia + 32 * k < c1;
+#ifdef MPSG_DEVICE_CHECKS
+            if (ok[k]) ok[k] = chk_addr(v, so + ia + 32 * k, dof + ia + 32 * k);
+#endif
+          }
 #pragma unroll
           for (int k = 0; k < 4; ++k)
-            if (ia + 32 * k < c1) x[k] = __ldg(src + so + ia + 32 * k);
+            if (ok[k]) x[k] = __ldg(src + so + ia + 32 * k);
 #pragma unroll
           for (int k = 0; k < 4; ++k)
-            if (ia + 32 * k < c1) dst[dof + ia + 32 * k] = x[k];
+            if (ok[k]) dst[dof + ia + 32 * k] = x[k];
         }
       }
     } else if (v.mode == kModeTile) {
@@ -162,15 +229,28 @@ __global__ void __launch_bounds__(32 * kWarps, 4) copy_tasks_kernel(
         so += ii * v.sstr[i];
         dof += ii * v.dstr[i];
       }
+#ifdef MPSG_DEVICE_CHECKS
+      if (!chk_decode(v, a, b, q, so, dof)) continue;  // uniform over the warp
+#endif
       const int64_t a0 = ia * kT, b0 = ib * kT;
       const int64_t sa = v.sstr[a], db = v.dstr[b];
 #pragma unroll 8
-      for (int r = 0; r < kT; ++r)  // rows along a, lanes along b (source-contiguous)
-        if (a0 + r < ea && b0 + lane < eb) tile[r][lane] = __ldg(src + so + (a0 + r) * sa + b0 + lane);
+      for (int r = 0; r < kT; ++r) {  // rows along a, lanes along b (source-contiguous)
+        bool ok = a0 + r < ea && b0 + lane < eb;
+#ifdef MPSG_DEVICE_CHECKS
+        if (ok) ok = chk_addr(v, so + (a0 + r) * sa + b0 + lane, dof);
+#endif
+        if (ok) tile[r][lane] = __ldg(src + so + (a0 + r) * sa + b0 + lane);
+      }
       __syncwarp();
 #pragma unroll 8
-      for (int c = 0; c < kT; ++c)  // columns along b, lanes along a (destination-contiguous)
-        if (a0 + lane < ea && b0 + c < eb) dst[dof + a0 + lane + (b0 + c) * db] = tile[lane][c];
+      for (int c = 0; c < kT; ++c) {  // columns along b, lanes along a (destination-contiguous)
+        bool ok = a0 + lane < ea && b0 + c < eb;
+#ifdef MPSG_DEVICE_CHECKS
+        if (ok) ok = chk_addr(v, so, dof + a0 + lane + (b0 + c) * db);
+#endif
+        if (ok) dst[dof + a0 + lane + (b0 + c) * db] = tile[lane][c];
+      }
       __syncwarp();
     } else {
       // decode all of this lane's positions first, then issue every load, then every store
@@ -192,6 +272,18 @@ __global__ void __launch_bounds__(32 * kWarps, 4) copy_tasks_kernel(
           so[k] += ii * v.sstr[i];
           if (dof[k] >= 0) dof[k] += ii * v.dstr[i];
         }
+#ifdef MPSG_DEVICE_CHECKS
+        if (dof[k] >= 0) {
+          int64_t rs = v.soff, rd = v.doff;
+          ref_decode(v.ext, v.sstr, v.dstr, v.order, nd, p, rs, rd);
+          if (rs != so[k] || rd != dof[k]) {
+            chk_fail(kChkDecode, v.task, p, rs != so[k] ? so[k] - rs : dof[k] - rd);
+            dof[k] = -1;
+          } else if (!chk_addr(v, so[k], dof[k])) {
+            dof[k] = -1;
+          }
+        }
+#endif
       }
       double x[kPer];
 #pragma unroll
@@ -204,19 +296,38 @@ __global__ void __launch_bounds__(32 * kWarps, 4) copy_tasks_kernel(
   }
 }
 
-void magic_u31(uint32_t d, uint32_t& m, uint32_t& s) {
-  uint32_t l = 0;
-  while (((uint64_t)1 << l) < d) ++l;
-  m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << l) - d)) / d + 1);
-  s = l;
-}
-
 constexpr size_t kViewSmem = sizeof(WarpView) * kWarps;
 constexpr size_t kTileSmem = kViewSmem + sizeof(TileBuf) * kWarps;
 
 }  // namespace
 
 size_t copy_aux_bytes() { return sizeof(TaskAux); }
+
+void read_device_checks(Context* ctx, bool reset, int64_t* count, int64_t* first) {
+#ifdef MPSG_DEVICE_CHECKS
+  MPSG_CUDA(cudaSetDevice(ctx->device));
+  MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  unsigned long long n = 0;
+  long long f[4] = {0, 0, 0, 0};
+  MPSG_CUDA(cudaMemcpyFromSymbol(&n, g_chk_count, sizeof(n)));
+  MPSG_CUDA(cudaMemcpyFromSymbol(f, g_chk_first, sizeof(f)));
+  if (count) *count = (int64_t)n;
+  if (first)
+    for (int i = 0; i < 4; ++i) first[i] = f[i];
+  if (reset) {
+    const unsigned long long z = 0;
+    const long long zf[4] = {0, 0, 0, 0};
+    MPSG_CUDA(cudaMemcpyToSymbol(g_chk_count, &z, sizeof(z)));
+    MPSG_CUDA(cudaMemcpyToSymbol(g_chk_first, zf, sizeof(zf)));
+  }
+#else
+  (void)ctx;
+  (void)reset;
+  (void)count;
+  (void)first;
+  throw Error(kErrUnsupported, "library built without device checks (MPSG_DEVICE_CHECKS)");
+#endif
+}
 
 void DevCopyPlan::upload(const std::vector<CopyTask>& tasks, bool identity_, cudaStream_t st) {
   release();

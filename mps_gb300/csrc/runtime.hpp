@@ -66,6 +66,9 @@ struct DevCopyPlan {
   void release();
 };
 size_t copy_aux_bytes();  // bytes of launch data per copy task
+// Device-checked build only (MPSG_DEVICE_CHECKS): violations recorded by the copy kernel since
+// the last reset, and the first one (kind, task, index, detail); kErrUnsupported otherwise.
+void read_device_checks(Context* ctx, bool reset, int64_t* count, int64_t* first);
 
 // FP64 GEMM tasks split by shape: tiled (64 x 64 tiles), thin-N (one thread per output row) and
 // thin-M (one thread per output column), each with its work-unit prefix sums.

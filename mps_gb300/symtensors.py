@@ -28,7 +28,7 @@ __all__ = [
     "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision", "_svd_",
     "svdtrunc", "svd_complex", "dots", "lincomb", "truncatedsizes", "small_eigh",
     "eigsolve_heff2", "EigInfo", "Heff2", "HostBuffer", "Copy", "download_async",
-    "upload_async",
+    "upload_async", "device_checks", "checked_library",
 ]
 
 
@@ -382,6 +382,22 @@ def meta(charge, space) -> SymTensor:
 def from_flat(charge, space, flat, ctx=None) -> SymTensor:
     t = zeros(charge, space, ctx)
     return t.upload(flat)
+
+
+def device_checks(reset: bool = False, ctx=None):
+    """Violations recorded by the device-checked library (``MPSG_LIBRARY=checked``): (count,
+    first) with first = (kind, task, index, detail), kind 1 task lookup, 2 decode, 3 span.
+    Raises MPSGError (status 5) with the normal library."""
+    n = C.c_int64()
+    first = (C.c_int64 * 4)()
+    h = None if ctx is None and not checked_library() else _ctx(ctx).handle
+    call("mpsg_device_checks", h, int(bool(reset)), C.byref(n), first)
+    return n.value, tuple(first)
+
+
+def checked_library() -> bool:
+    """Whether the loaded library is the device-checked debug build."""
+    return _lib.LIB_PATH.endswith("_checked.so")
 
 
 class HostBuffer:
