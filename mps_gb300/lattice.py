@@ -14,7 +14,10 @@ open terms in the order they started, start last.
 
 ``cylinder_heisenberg_terms`` gives the J1 Heisenberg model on a W x L cylinder (periodic
 around the circumference, open along the length) with the column-major site order of the
-reference (y fastest, src/model3.jl:86-87): bond dimension 2 + 3 W.
+reference (y fastest, src/model3.jl:86-87): bond dimension 2 + 3 W. ``j1j2_chain_terms`` and
+``triangular_terms`` give the reference's j1j2 chain and triangular-lattice spin models
+(src/spinmodels.jl:14-110), the latter with its four-spin ring exchange, expanded into products
+of single-site operators by ``ring_exchange_terms``.
 """
 from __future__ import annotations
 
@@ -45,6 +48,96 @@ def cylinder_heisenberg_terms(width, length, J=1.0):
                 terms += heisenberg_bond_terms(site(x, y), site(x, (y + 1) % width), J)
             if x + 1 < length:
                 terms += heisenberg_bond_terms(site(x, y), site(x + 1, y), J)
+    return terms
+
+
+def j1j2_chain_terms(lx, j1, j2):
+    """Heisenberg chain with nearest (j1) and next-nearest (j2) neighbour couplings, open ends
+    (``j1j2model``, src/spinmodels.jl:14-40)."""
+    terms = []
+    for i in range(lx):
+        if j1 != 0 and i + 1 < lx:
+            terms += heisenberg_bond_terms(i, i + 1, j1)
+        if j2 != 0 and i + 2 < lx:
+            terms += heisenberg_bond_terms(i, i + 2, j2)
+    return terms
+
+
+def _op_basis_expansion(H, n):
+    """Amplitudes of an n-site operator (2^n x 2^n, site 0 most significant) on the products of
+    Sz, S+, S-, 1: the four are orthogonal under tr(A^T B), so each amplitude is a trace ratio
+    (the decomposition of ``nbodyopexpansion``, src/spin_definitions.jl:86-130)."""
+    names = ("Z", "P", "M", "I")
+    out = []
+    for idx in np.ndindex(*(4,) * n):
+        M = np.ones((1, 1))
+        norm = 1.0
+        for k in idx:
+            op = OPS[names[k]][0]
+            M = np.kron(M, op)
+            norm *= float(np.sum(op * op))
+        amp = float(np.sum(M * H)) / norm
+        if abs(amp) > 1e-14:
+            out.append((tuple(names[k] for k in idx), amp))
+    return out
+
+
+def _ring_matrix(n):
+    """C + C^-1 for the cyclic shift of n spins (``ringexchangeoperator``,
+    src/spin_definitions.jl:74-84): a basis state's bits rotate by one place."""
+    P = np.zeros((2 ** n, 2 ** n))
+    for j in range(2 ** n):
+        i = (j >> 1) | ((j & 1) << (n - 1))
+        P[i, j] = 1.0
+    return P + P.T
+
+
+_RING4 = None
+
+
+def ring_exchange_terms(sites, k):
+    """k (C + C^-1 - 1/4) on four sites in their cyclic order (the reference's ring term R4,
+    src/spinmodels.jl:79-81): traceless, so every product term has at least one non-identity
+    factor; identity factors are dropped and the factors sorted by site."""
+    global _RING4
+    if _RING4 is None:
+        _RING4 = _op_basis_expansion(_ring_matrix(4) - 0.25 * np.eye(16), 4)
+    terms = []
+    for names, amp in _RING4:
+        pairs = sorted((s, o) for s, o in zip(sites, names) if o != "I")
+        terms.append((tuple(s for s, _ in pairs), tuple(o for _, o in pairs), k * amp))
+    return terms
+
+
+def triangular_terms(ly, lx, j1, j2, j3, k1=0.0, k2=0.0, k3=0.0, periodic_y=False):
+    """Spin-1/2 model on the ly x lx triangular lattice (``triangularspinmodel``,
+    src/spinmodels.jl:42-110): Heisenberg couplings j1, j2, j3 along the (dy, dx) offsets (0, 1),
+    (1, 0), (1, -1) and ring exchanges k1, k2, k3 on the plaquettes given there, sites numbered
+    x * ly + y (y fastest), open along x, open or periodic (ly > 2) along y."""
+    if periodic_y and ly <= 2:
+        raise ValueError("periodic y needs ly > 2")
+
+    def site(y, x):
+        if periodic_y:
+            y %= ly
+        if not (0 <= y < ly and 0 <= x < lx):
+            return None
+        return x * ly + y
+
+    bonds = ((j1, (0, 1)), (j2, (1, 0)), (j3, (1, -1)))
+    rings = ((k1, ((0, 0), (0, 1), (1, 1), (1, 0))), (k2, ((0, 0), (0, 1), (1, 0), (1, -1))),
+             (k3, ((0, 0), (1, 0), (0, 1), (-1, 1))))
+    terms = []
+    for x in range(lx):
+        for y in range(ly):
+            for J, (dy, dx) in bonds:
+                t = site(y + dy, x + dx)
+                if J != 0 and t is not None:
+                    terms += heisenberg_bond_terms(site(y, x), t, J)
+            for K, offs in rings:
+                ss = [site(y + dy, x + dx) for dy, dx in offs]
+                if K != 0 and None not in ss:
+                    terms += ring_exchange_terms(ss, K)
     return terms
 
 
