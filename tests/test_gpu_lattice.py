@@ -30,3 +30,24 @@ def test_cylinder_dmrg_matches_exact_diagonalisation(cfg):
     idx = np.where(pop == n // 2)[0]
     e0 = np.linalg.eigvalsh(H[np.ix_(idx, idx)])[0]
     assert abs(es[-1] - e0) < 1e-9 * abs(e0)
+
+
+def test_triangular_ladder_with_ring_exchange_dmrg_matches_exact_diagonalisation():
+    """The (2, 5) triangular ladder with four-spin ring exchange (MPO bond dimension up to 86,
+    33 product terms per plaquette): DMRG at full bond dimension = ED."""
+    ly, lx = 2, 5
+    n = ly * lx
+    terms = lt.triangular_terms(ly, lx, 0.3, 1.0, 1.0, 0.4, 0.7, 0.0)
+    Ws = lt.device_mpo(n, terms)
+    assert max(W.space[0].dim() for W in Ws) == 86
+    mps = gd.mps_from_host(gd.random_mps_host(n, n // 2, 32, seed=5))
+    gd.center_at(mps, 1)
+    env = gd.initialenv(mps, Ws)
+    for _ in range(4):
+        es = gd.dmrg2sitesweep(mps, Ws, env, maxdim=32, tol=1e-12, lanczostol=1e-10,
+                               krylovdim=6, krylovmaxiter=30, tieband=1e-9)
+    H = lt.dense_mpo(lt.mpo_blocks(n, terms))
+    pop = np.array([bin(k).count("1") for k in range(2 ** n)])
+    idx = np.where(pop == n // 2)[0]
+    e0 = np.linalg.eigvalsh(H[np.ix_(idx, idx)])[0]
+    assert abs(es[-1] - e0) < 1e-9 * abs(e0)
