@@ -173,3 +173,24 @@ def test_heff_chain_structure_at_chi2048():
     assert 1_700_000 < v.numel() < 1_900_000
     f = dmrg.heff_flops_meta(*prob)
     assert 9.0e9 < f < 10.5e9
+
+
+def test_empty_structures_match_oracle():
+    """A charge no sector can carry gives a tensor without blocks; relegs, SymMatrix and
+    contractions of it stay empty, as in the reference (SortedDicts without entries)."""
+    Vo = st.VectorSpace([(0, 2), (1, 3)])
+    W = st.VectorSpace([(-1, 1), (0, 2)])
+    T = st.fill(0.0, 5, (Vo, Vo, W))
+    m = mg_meta(T)
+    assert m.sectors() == [] and m.numel() == 0
+    assert_same_structure(m, T)
+    assert_same_structure(mg.permutelegs(m, (3, 1, 2)), st.permutelegs(T, [3, 1, 2]))
+    F = st.fuselegs(T, 1, 2)
+    mf = mg.fuselegs(m, 1, 2)
+    assert_same_structure(mf, F)
+    assert_same_structure(mg.splitleg(mf, 1, [to_mg_space(Vo), to_mg_space(Vo)]),
+                          st.splitleg(F, 1, (Vo, Vo)))
+    assert_same_structure(mg.SymMatrix(m, [1, 3], [2]), st.symmatrix(T, [1, 3], [2]))
+    B = st.fill(0.0, 0, (st.dual_space(W), Vo))
+    assert_same_structure(mg.contract(m, (1, 2, -1), mg_meta(B), (-1, 3)),
+                          st.contract(T, (1, 2, -1), B, (-1, 3)))
