@@ -47,6 +47,53 @@ class SyncTransfer:
         pass
 
 
+class FileTransfer:
+    """Host copies in files, one per environment (what src/dmrg_envio.jl:5-39 does with JLD2
+    files): ``to_flat()`` is written to ``directory`` as raw FP64 and read back through
+    ``load(charge, space, flat)``; a file is deleted once its entry is overwritten."""
+
+    def __init__(self, directory, load):
+        import itertools
+        import os
+        os.makedirs(directory, exist_ok=True)
+        self.directory = directory
+        self.load = load
+        self._ids = itertools.count()
+        self.bytes_down = self.bytes_up = 0
+
+    def download(self, t):
+        import os
+
+        import numpy as np
+        flat = np.ascontiguousarray(t.to_flat(), dtype=np.float64)
+        path = os.path.join(self.directory, f"env{next(self._ids)}.f64")
+        flat.tofile(path)
+        self.bytes_down += flat.nbytes
+        return (t.charge, t.space, path, flat.size), None
+
+    def upload(self, entry):
+        import numpy as np
+        charge, space, path, n = entry
+        flat = np.fromfile(path, dtype=np.float64, count=n)
+        if flat.size != n:
+            raise OSError(f"environment file {path} is truncated")
+        self.bytes_up += flat.nbytes
+        return self.load(charge, space, flat), None
+
+    def ready(self, copy):
+        return True
+
+    def order(self, copy):
+        pass
+
+    def release(self, entry):
+        import os
+        try:
+            os.remove(entry[2])
+        except FileNotFoundError:
+            pass
+
+
 class PinnedPool:
     """Reusable page-locked host buffers (``HostBuffer``): a request takes the smallest free
     buffer of at least ``n`` and at most ``2 n`` doubles, else a new one; at most ``keep``
@@ -116,7 +163,8 @@ class OffloadedEnvs:
     """List-like store of environments with a device-resident window of ``window`` entries.
 
     ``transfer`` moves the data (default: ``AsyncTransfer`` on ``ctx``; ``load`` given instead
-    selects blocking ``SyncTransfer`` copies with that loader)."""
+    selects blocking ``SyncTransfer`` copies with that loader; ``FileTransfer`` keeps the host
+    copies in files)."""
 
     def __init__(self, envs, window: int = 6, ctx=None, load=None, transfer=None):
         if window < 1:

@@ -1,5 +1,7 @@
 """Environment residency store: window, least-recently-used eviction to host copies, exact
 round trips (host logic with stand-in tensors)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -208,3 +210,24 @@ def test_pinned_pool_best_fit_and_bound():
     assert pool.take(8) is not b           # b (40) is more than twice 8: a new buffer
     assert pool.allocated == 4
     assert pool.take(25) is b              # 40 <= 2 * 25
+
+
+def test_file_transfer_round_trips_and_cleans_up(tmp_path):
+    """Host copies in files (as the reference's environment I/O keeps them): exact round trips
+    in a sweep-like pattern, and no file outlives its entry's overwrite."""
+    from mps_gb300.envstore import FileTransfer
+    rng = np.random.default_rng(4)
+    envs = [Fake(i, ("V", i), rng.standard_normal(7)) for i in range(8)]
+    want = {i: e.flat.copy() for i, e in enumerate(envs)}
+    st = OffloadedEnvs(envs, window=2, transfer=FileTransfer(str(tmp_path), load))
+    assert len(list(tmp_path.iterdir())) == 6
+    for i in list(range(8)) + list(range(7, -1, -1)):
+        np.testing.assert_array_equal(st[i].flat, want[i])
+    for i in range(8):  # overwrite everything: the old files go
+        st[i] = Fake(i, ("V", i), np.full(7, float(i)))
+    for i in range(8):
+        np.testing.assert_array_equal(st[i].flat, np.full(7, float(i)))
+    # every file left belongs to a current host copy, one file each
+    assert sorted(p.name for p in tmp_path.iterdir()) == sorted(
+        os.path.basename(e[2]) for e in st._host.values())
+    assert st.transfer.bytes_down > 0 and st.transfer.bytes_up > 0
