@@ -425,12 +425,14 @@ void launch_copy(Context* ctx, const DevCopyPlan& p, const double* src, double* 
                                 ctx->stream));
     return;
   }
-  static bool attr = false;  // per process: the attribute belongs to the kernel, not a device
-  if (!attr) {
+  // once per process (the attribute belongs to the kernel, not a device); a thread-safe static,
+  // retried on the next call if setting it failed
+  static const bool attr = [] {
     MPSG_CUDA(cudaFuncSetAttribute(copy_tasks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kTileSmem));
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   const size_t smem = p.has_tile ? kTileSmem : kViewSmem;
   const int64_t ctas = (p.ntiles + kWarps - 1) / kWarps;
   const int64_t grid = std::min<int64_t>(ctas, (int64_t)ctx->num_sms * (p.has_tile ? 3 : 8));

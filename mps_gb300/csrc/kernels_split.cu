@@ -1137,15 +1137,16 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
     }
   }
   if (!(what & kRunGemm)) return;
-  static bool attr_set = false;
-  if (!attr_set) {
+  // once per process and slice count (thread-safe static, retried if setting it failed)
+  static const bool attr_set = [] {
     MPSG_CUDA(cudaFuncSetAttribute(split_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    CF::kSmemBytes));
     if (S <= 3)
       MPSG_CUDA(cudaFuncSetAttribute(split_gemm_fast_kernel<S <= 3 ? S : 3>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, FCF::kSmemBytes));
-    attr_set = true;
-  }
+    return true;
+  }();
+  (void)attr_set;
   const int grid = (int)std::min<int64_t>(sp.ntiles, (int64_t)ctx->num_sms);
   KernelTimer timer(ctx, kKindGemmSplit, sp.flops);
   if (sp.fast) {
