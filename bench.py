@@ -108,6 +108,20 @@ def replica_rate(t_local, flops, ws, device=None):
     return t, ws * flops / t / 1e9
 
 
+def clock_soak(run_batch, sync, seconds, per_batch):
+    """Runs batches of the step, untimed, for at least ``seconds`` (synchronising after each
+    batch), so that the clock sampler (one sample per 200 ms) sees the GPU under this step's load
+    before the short timed region. Returns (seconds spent, steps run)."""
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        run_batch()
+        sync()
+        n += per_batch
+        if time.perf_counter() - t0 >= seconds:
+            return time.perf_counter() - t0, n
+
+
 class ClockSampler:
     """nvidia-smi samples (200 ms) of SM clock and throttle reasons during the timed region."""
 
@@ -367,12 +381,21 @@ def run_ours(args):
         for _ in range(args.warmup):
             del_out = o(v)
             del del_out
-    barrier()
-    launches0, _ = ctx.counters()
+    def soak_batch():
+        with torch.cuda.stream(stream):
+            for _ in range(20):
+                flush.zero_()
+                out = op(v)
+                del out
+
     with ClockSampler(local) as cs:
+        soak_s, soak_steps = clock_soak(soak_batch, torch.cuda.synchronize, 1.0, 20)
+        barrier()
+        launches0, _ = ctx.counters()
         ms = timed_steps(op, args.steps)
-    launches = ctx.counters()[0] - launches0
+        launches = ctx.counters()[0] - launches0
     clocks = cs.summary()
+    clocks["soak"] = f"{soak_steps} untimed steps ({soak_s:.2f} s) just before the timed ones"
     t, value = replica_rate(sum(ms) / len(ms) / 1e3, flops, ws, f"cuda:{local}")
 
     # the plain FP64 drop-in on the same inputs

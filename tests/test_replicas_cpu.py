@@ -90,3 +90,13 @@ def test_replica_rate_single_rank():
     t, value = bench.replica_rate(0.004, FLOPS, 1)
     assert t == 0.004
     assert value == pytest.approx(FLOPS / 0.004 / 1e9, rel=1e-15)
+
+
+def test_clock_soak_runs_whole_batches_for_the_requested_time():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    calls = {"batch": 0, "sync": 0}
+    s, n = bench.clock_soak(lambda: calls.__setitem__("batch", calls["batch"] + 1),
+                            lambda: calls.__setitem__("sync", calls["sync"] + 1), 0.05, 20)
+    assert s >= 0.05 and n == 20 * calls["batch"] and calls["sync"] == calls["batch"] >= 1
