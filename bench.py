@@ -58,6 +58,9 @@ def parse(argv=None):
                    help="instead of the H_eff line: mixed-precision 2-site DMRG sweeps of the "
                         "J1 Heisenberg 6 x 24 cylinder at maxdim --sweep-chi (default 1024)")
     p.add_argument("--sweeps", type=int, default=2, help="sweeps of the --cylinder run")
+    p.add_argument("--mpo-shared-prefixes", action="store_true",
+                   help="--cylinder with the MPO whose open terms share channels (w = 20 "
+                        "instead of 26)")
     p.add_argument("--small-chain", action="store_true",
                    help="instead of the H_eff line: 4 FP64 sweeps of the L=32, maxdim 64 "
                         "Heisenberg chain, with the CPU oracle timed on the same sweeps")
@@ -601,7 +604,8 @@ def run_cylinder(args):
     n = width * length
     chi = args.sweep_chi or 1024
     ctx = mg.get_context(0)
-    Ws = lt.device_mpo(n, lt.cylinder_heisenberg_terms(width, length), ctx=ctx)
+    Ws = lt.device_mpo(n, lt.cylinder_heisenberg_terms(width, length), ctx=ctx,
+                       share_prefixes=args.mpo_shared_prefixes)
     mps = gd.mps_from_host(gd.binomial_mps_host(n, n // 2, chi, 13), ctx)
     t0 = time.perf_counter()
     gd.center_at(mps, 1, svd="gram", normalize=True)  # 144 random sites: keep the norm at 1
@@ -623,7 +627,8 @@ def run_cylinder(args):
         "metric": "DMRG sweep s, J1 Heisenberg 6x24 cylinder", "value": times[-1], "unit": "s",
         "higher_is_better": False, "n_gpus": 1, "data": "synthetic (seeded Philox initial MPS)",
         "config": {"workload": f"6x24 cylinder (PBC around, OBC along), J1=1, Sz=0, maxdim {chi}, "
-                               "cutoff 1e-10, Krylov dim 4, maxiter 8", "mixed": SWEEP_MIXED},
+                               "cutoff 1e-10, Krylov dim 4, maxiter 8", "mixed": SWEEP_MIXED,
+                   "mpo": "shared prefixes" if args.mpo_shared_prefixes else "one channel per term"},
         "sweep_s": times, "energy_per_sweep": energies, "energy_per_site": energies[-1] / n,
         "matvecs_per_sweep": matvecs, "init_s": t_init,
         "max_mpo_bond": max(W.space[2].dim() for W in Ws),

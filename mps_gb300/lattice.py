@@ -148,52 +148,82 @@ def chain_xxz_terms(lx, delta):
     return terms
 
 
-def mpo_blocks(n_sites, terms):
+def mpo_blocks(n_sites, terms, share_prefixes=False):
     """Per site: (space, {sector: block}) of the MPO tensor W(Vl, d, dual(Vr), dual(d)).
-    Spaces are (charges, dims, isdual) triples per leg, usable with VectorSpace."""
+    Spaces are (charges, dims, isdual) triples per leg, usable with VectorSpace.
+
+    By default every open term has its own channel, as in the reference. With
+    ``share_prefixes`` a channel stands for the operators placed so far: open terms with the
+    same placed (site, operator) sequence share it until they diverge, and each term's amplitude
+    sits on its finishing edge (summed over terms with the same full sequence). Every path from
+    the start channel to the done channel is then the sequence of exactly one distinct term, so
+    the MPO is the same Hamiltonian with fewer channels."""
     terms = sorted(((tuple(s), tuple(o), float(a)) for s, o, a in terms), key=lambda t: t[0])
     for s, o, _ in terms:
         if len(s) != len(o) or list(s) != sorted(s) or len(set(s)) != len(s):
             raise ValueError(f"term sites must increase: {s}")
         if s[-1] >= n_sites:
             raise ValueError(f"term beyond the lattice: {s}")
+
+    def key(k, p):  # the channel of term k once its first p operators are placed
+        if not share_prefixes:
+            return ("t", k)
+        s, o, _ = terms[k]
+        return ("p",) + tuple(zip(s[:p], o[:p]))
+
+    def channels(open_terms):
+        seen, out = set(), []
+        for k, p, c in open_terms:
+            name = key(k, p)
+            if name not in seen:
+                seen.add(name)
+                out.append((c, name))
+        return out
+
     open_terms = []  # (term index, next op position, accumulated charge), in start order
     out = []
     ti = 0
     for n in range(n_sites):
-        # left channels: [(charge, name)]: done, open terms, start
+        # left channels: [(charge, name)]: done, open terms (or prefixes), start
         left = []
         if n > 0:
             left.append((0, "done"))
-            left += [(c, ("t", k)) for (k, p, c) in open_terms]
+            left += channels(open_terms)
         left.append((0, "start"))
-        trans = []  # (left name, right name, op, amplitude)
+        trans = {}  # (left name, right name, op) -> amplitude
+
+        def add(ln, rn, op, amp, finishing):
+            if finishing:  # amplitudes of terms with the same full sequence add up
+                trans[(ln, rn, op)] = trans.get((ln, rn, op), 0.0) + amp
+            else:  # an edge shared by several terms has weight 1
+                trans[(ln, rn, op)] = amp
+
         new_open = []
         if n > 0:
-            trans.append(("done", "done", "I", 1.0))
+            add("done", "done", "I", 1.0, False)
         for (k, p, c) in open_terms:
             s, o, a = terms[k]
             if s[p] == n:
                 if p == len(s) - 1:
-                    trans.append((("t", k), "done", o[p], a))
+                    add(key(k, p), "done", o[p], a, True)
                 else:
-                    trans.append((("t", k), ("t", k), o[p], 1.0))
+                    add(key(k, p), key(k, p + 1), o[p], 1.0, False)
                     new_open.append((k, p + 1, c + OPS[o[p]][1]))
             else:
-                trans.append((("t", k), ("t", k), "I", 1.0))
+                add(key(k, p), key(k, p), "I", 1.0, False)
                 new_open.append((k, p, c))
         while ti < len(terms) and terms[ti][0][0] == n:
             s, o, a = terms[ti]
             if len(s) == 1:
-                trans.append(("start", "done", o[0], a))
+                add("start", "done", o[0], a, True)
             else:
-                trans.append(("start", ("t", ti), o[0], 1.0))
+                add("start", key(ti, 1), o[0], 1.0, False)
                 new_open.append((ti, 1, OPS[o[0]][1]))
             ti += 1
         if n < n_sites - 1:
-            trans.append(("start", "start", "I", 1.0))
+            add("start", "start", "I", 1.0, False)
         open_terms = new_open
-        right = [(0, "done")] + [(c, ("t", k)) for (k, p, c) in open_terms]
+        right = [(0, "done")] + channels(open_terms)
         if n < n_sites - 1:
             right.append((0, "start"))
         else:
@@ -202,7 +232,7 @@ def mpo_blocks(n_sites, terms):
             right = [(0, "done")]
         if n == 0:
             left = [(0, "start")]
-        out.append(_site_tensor(left, right, trans))
+        out.append(_site_tensor(left, right, [(l, r, op, a) for (l, r, op), a in trans.items()]))
     return out
 
 
@@ -241,13 +271,13 @@ def _site_tensor(left, right, trans):
     return (Vl, d, Vr, dd), blocks
 
 
-def device_mpo(n_sites, terms, ctx=None, meta_only=False):
+def device_mpo(n_sites, terms, ctx=None, meta_only=False, share_prefixes=False):
     """The MPO of ``terms`` as library tensors W(Vl, d, dual(Vr), dual(d)) (zero blocks for the
-    allowed sectors no term touches)."""
+    allowed sectors no term touches); ``share_prefixes`` as in ``mpo_blocks``."""
     from . import symtensors as mg
     from .dmrg import _tensor_from_partial_blocks
     out = []
-    for legs, blocks in mpo_blocks(n_sites, terms):
+    for legs, blocks in mpo_blocks(n_sites, terms, share_prefixes=share_prefixes):
         sp = tuple(mg.VectorSpace(list(zip(c, dims)), isd) for c, dims, isd in legs)
         out.append(_tensor_from_partial_blocks(sp, blocks, ctx=ctx, meta_only=meta_only))
     return out

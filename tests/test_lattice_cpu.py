@@ -164,3 +164,50 @@ def test_ring_expansion_reassembles_the_ring_operator():
     terms = lt.ring_exchange_terms([0, 1, 2, 3], 1.0)
     H = lt.dense_mpo(lt.mpo_blocks(4, terms))
     np.testing.assert_allclose(H, _perm_dense(4, [0, 1, 2, 3]) - 0.25 * np.eye(16), atol=1e-14)
+
+
+# ---- channels shared by open terms with the same placed operators ----
+def _max_bond(blocks):
+    return max(sum(Vl[1]) for (Vl, _, _, _), _ in blocks)
+
+
+@pytest.mark.parametrize("n,make", [
+    (8, lambda: lt.chain_xxz_terms(8, 0.7)),
+    (9, lambda: lt.j1j2_chain_terms(9, 1.0, 0.3)),
+    (8, lambda: lt.triangular_terms(2, 4, 0.3, 1.0, 1.0, 0.4, 0.7)),
+    (6, lambda: lt.triangular_terms(3, 2, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, periodic_y=True)),
+    (9, lambda: lt.cylinder_heisenberg_terms(3, 3)),
+])
+def test_shared_prefix_mpo_is_the_same_hamiltonian(n, make):
+    terms = make()
+    full = lt.mpo_blocks(n, terms)
+    shared = lt.mpo_blocks(n, terms, share_prefixes=True)
+    np.testing.assert_allclose(lt.dense_mpo(shared), lt.dense_mpo(full), atol=1e-12)
+    np.testing.assert_allclose(lt.dense_mpo(shared), dense_from_terms(n, terms), atol=1e-12)
+    assert _max_bond(shared) <= _max_bond(full)
+
+
+def test_shared_prefixes_shrink_the_bond_dimension():
+    """The 6 x 24 cylinder reaches w = 2 + 3 W = 20 at every cut (26 with one channel per
+    term); the j1j2 chain 8 (11); the ring-exchange ladder 33 (86)."""
+    cases = [(144, lt.cylinder_heisenberg_terms(6, 24), 26, 20),
+             (64, lt.j1j2_chain_terms(64, 1.0, 0.3), 11, 8),
+             (64, lt.triangular_terms(2, 32, 0.3, 1.0, 1.0, 0.4, 0.7), 86, 33)]
+    for n, terms, w_full, w_shared in cases:
+        assert _max_bond(lt.mpo_blocks(n, terms)) == w_full
+        assert _max_bond(lt.mpo_blocks(n, terms, share_prefixes=True)) == w_shared
+
+
+def test_duplicate_terms_add_on_the_shared_finishing_edge():
+    terms = [((0, 2), ("Z", "Z"), 0.25), ((0, 2), ("Z", "Z"), 0.5), ((1,), ("Z",), 1.0),
+             ((1,), ("Z",), -0.5)]
+    shared = lt.mpo_blocks(3, terms, share_prefixes=True)
+    np.testing.assert_allclose(lt.dense_mpo(shared), dense_from_terms(3, terms), atol=1e-15)
+    assert _max_bond(shared) == 3  # done, the one shared Z channel, start
+
+
+def test_structure_only_device_mpo_with_shared_prefixes():
+    Ws = lt.device_mpo(144, lt.cylinder_heisenberg_terms(6, 24), meta_only=True,
+                       share_prefixes=True)
+    assert max(W.space[0].dim() for W in Ws) == 20
+    assert Ws[0].space[0].dim() == 1 and Ws[-1].space[2].dim() == 1
