@@ -231,3 +231,16 @@ def test_file_transfer_round_trips_and_cleans_up(tmp_path):
     assert sorted(p.name for p in tmp_path.iterdir()) == sorted(
         os.path.basename(e[2]) for e in st._host.values())
     assert st.transfer.bytes_down > 0 and st.transfer.bytes_up > 0
+
+
+def test_file_transfer_rejects_a_truncated_file(tmp_path):
+    from mps_gb300.envstore import FileTransfer
+    tr = FileTransfer(str(tmp_path), load)
+    entry, _ = tr.download(Fake(0, ("V", 0), np.arange(6.0)))
+    with open(entry[2], "r+b") as f:
+        f.truncate(8 * 5)
+    with pytest.raises(OSError):
+        tr.upload(entry)
+    tr.release(entry)
+    assert not os.path.exists(entry[2])
+    tr.release(entry)  # releasing twice is harmless
