@@ -129,3 +129,48 @@ def test_two_point_function_of_an_evolved_state():
         assert abs(val.imag) < 1e-12
         assert abs(val.real - ot.szsz(psi, LX, i, j)) < 1e-11
     assert abs(td.norm2(ops, As) - 1.0) < 1e-11
+
+
+def _hermitian_problem(seed=0):
+    ops = oracle_ops()
+    rng = np.random.default_rng(seed)
+    V = U1Space((0, 5), (1, 6), (2, 4))
+    blocks = {}
+    for c, n in V.sectors:
+        B = rng.standard_normal((n, n))
+        blocks[(c, c)] = B + B.T
+    H = st.from_blocks(0, (dual_space(V), V), blocks)
+    W = (dual_space(U1Space((0, 1))), V)
+    x = ct.CTensor(rand_tensor(0, W, rng), rand_tensor(0, W, rng))
+    f = lambda v: ct.ccontract(ops, v, (1, -1), H, (-1, 2))
+    return ops, f, x, st.array(H)
+
+
+def test_exponentiate_takes_several_steps_when_the_basis_is_small():
+    """x lives in a 5-dimensional sector; a Krylov dimension of 4 cannot take t = -0.1i within
+    1e-10 in one step: the step is cut, the integration restarts from the new vector, and the
+    result still equals expm (a basis of 5 would be exact in one step)."""
+    ops, f, x, Hd = _hermitian_problem()
+    w, Q = np.linalg.eigh(Hd)
+    t = -0.1j
+    y, info = ct.exponentiate(ops, f, t, x, krylovdim=4, tol=1e-10, maxiter=2000)
+    ref = dense_site(ops, x)[0] @ (Q @ np.diag(np.exp(t * w)) @ Q.T)
+    assert info.converged and info.numsteps > 1 and info.numops == 4 * info.numsteps
+    assert np.linalg.norm(dense_site(ops, y)[0] - ref) < 1e-10 * np.linalg.norm(ref)
+    y5, info5 = ct.exponentiate(ops, f, t, x, krylovdim=5, tol=1e-10)
+    assert info5.numsteps == 1
+    assert np.linalg.norm(dense_site(ops, y5)[0] - ref) < 1e-12 * np.linalg.norm(ref)
+
+
+def test_exponentiate_reports_an_unfinished_integration():
+    ops, f, x, _ = _hermitian_problem()
+    y, info = ct.exponentiate(ops, f, -3.0j, x, krylovdim=2, tol=1e-14, maxiter=1)
+    assert not info.converged and info.numsteps == 1
+
+
+def test_exponentiate_of_zero_is_zero():
+    ops, f, x, _ = _hermitian_problem()
+    z = ct.cscale(ops, x, 0.0)
+    y, info = ct.exponentiate(ops, f, -1.0j, z)
+    assert info.converged and info.numops == 0
+    assert np.all(dense_site(ops, y)[0] == 0)
