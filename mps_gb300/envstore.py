@@ -19,6 +19,13 @@ The stored values are exact copies: a sweep gives bit-identical results with any
 from __future__ import annotations
 
 
+def _nbytes(t):
+    """Device bytes of a stored tensor (``numel()`` doubles; stand-ins without it: their flat
+    data)."""
+    n = getattr(t, "numel", None)
+    return 8 * int(n()) if n is not None else int(t.to_flat().nbytes)
+
+
 class SyncTransfer:
     """Blocking copies through NumPy arrays: ``to_flat()`` down, ``load(charge, space, flat)``
     up. Works with any tensor type that has ``charge``, ``space`` and ``to_flat()``."""
@@ -164,16 +171,23 @@ class OffloadedEnvs:
 
     ``transfer`` moves the data (default: ``AsyncTransfer`` on ``ctx``; ``load`` given instead
     selects blocking ``SyncTransfer`` copies with that loader; ``FileTransfer`` keeps the host
-    copies in files)."""
+    copies in files). ``budget_bytes`` also bounds the device bytes of the resident entries
+    (the most recently used entry always stays), for environments whose sizes vary along the
+    chain."""
 
-    def __init__(self, envs, window: int = 6, ctx=None, load=None, transfer=None):
+    def __init__(self, envs, window: int = 6, ctx=None, load=None, transfer=None,
+                 budget_bytes=None):
         if window < 1:
             raise ValueError("window must be at least 1")
+        if budget_bytes is not None and budget_bytes <= 0:
+            raise ValueError("budget_bytes must be positive")
         if transfer is None:
             transfer = SyncTransfer(load) if load is not None else AsyncTransfer(ctx)
         self.transfer = transfer
         self.window = window
+        self.budget_bytes = budget_bytes  # also evict while the resident entries hold more
         self._n = len(envs)
+        self._size = {}      # index -> bytes of the device-resident entry
         self._dev = {}       # index -> device tensor
         self._host = {}      # index -> host entry (valid copy of the entry's current value)
         self._busy = {}      # index -> copies in flight that use the host entry's buffer
@@ -221,14 +235,22 @@ class OffloadedEnvs:
                 self.transfer.release(entry)
         self._retired = keep
 
+    def resident_bytes(self) -> int:
+        return sum(self._size.values())
+
+    def _over_budget(self):
+        return (self.budget_bytes is not None and len(self._dev) > 1
+                and self.resident_bytes() > self.budget_bytes)
+
     def _evict(self):
-        while len(self._dev) > self.window:
+        while len(self._dev) > self.window or self._over_budget():
             # prefetched entries the sweep has not read yet go last
             cand = [j for j in self._order if j not in self._pending] or self._order
             j = cand[0]
             self._order.remove(j)
             self._pending.pop(j, None)
             t = self._dev.pop(j)
+            self._size.pop(j, None)
             if j in self._host:
                 self.clean_evictions += 1
                 continue
@@ -248,6 +270,7 @@ class OffloadedEnvs:
             else:
                 self._pending[i] = c
         self._dev[i] = t
+        self._size[i] = _nbytes(t)
         self._touch(i)
         self._evict()
         return t
@@ -285,10 +308,12 @@ class OffloadedEnvs:
         self._pending.pop(i, None)
         if t is None:
             self._dev.pop(i, None)
+            self._size.pop(i, None)
             if i in self._order:
                 self._order.remove(i)
             return
         self._dev[i] = t
+        self._size[i] = _nbytes(t)
         self._touch(i)
         self._evict()
 

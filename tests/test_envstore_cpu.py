@@ -244,3 +244,19 @@ def test_file_transfer_rejects_a_truncated_file(tmp_path):
     tr.release(entry)
     assert not os.path.exists(entry[2])
     tr.release(entry)  # releasing twice is harmless
+
+
+def test_byte_budget_bounds_the_resident_entries():
+    sizes = [4, 40, 8, 16, 4, 64, 8]
+    envs = [Fake(i, ("V", i), np.arange(float(n))) for i, n in enumerate(sizes)]
+    want = {i: e.flat.copy() for i, e in enumerate(envs)}
+    budget = 8 * 48
+    st = OffloadedEnvs(envs, window=7, load=load, budget_bytes=budget)
+    assert st.resident_bytes() <= budget
+    for i in list(range(7)) + list(range(6, -1, -1)):
+        np.testing.assert_array_equal(st[i].flat, want[i])
+        # the entry just read stays even when it alone exceeds the budget (index 5: 64 doubles)
+        assert st.resident()[-1] == i
+        assert st.resident_bytes() <= max(budget, 8 * sizes[i])
+    with pytest.raises(ValueError):
+        OffloadedEnvs(envs, load=load, budget_bytes=0)
