@@ -30,6 +30,20 @@ def test_oracle_reproduces_heff_fixture():
     assert np.array_equal(st.flatten(om.applymps2site(O[0], O[1], O[2], W, W)), g["out"])
 
 
+def test_oracle_reproduces_sweep_fixture():
+    g = np.load(os.path.join(GOLD, "sweep_L10.npz"))
+    lx, chi = int(g["lx"]), int(g["chi"])
+    sites = gd.random_mps_host(lx, lx // 2, chi, seed=int(g["seed"]))
+    mps = om.MPState([st.from_flat(c, conv(sp), f) for c, sp, f in sites], 0)
+    om.center_at(mps, 1)
+    Ws = om.xxz_u1mpo(lx, 1.0)
+    env = om.initialenv(mps, Ws)
+    es = om.dmrg2sitesweep(mps, Ws, env, maxdim=chi, tol=1e-10, lanczostol=1e-7, krylovdim=4,
+                           krylovmaxiter=8, tieband=1e-12)
+    # (LAPACK eigen-solvers inside: the last bits may depend on the BLAS thread count)
+    np.testing.assert_allclose(np.array(es), g["energies"], rtol=1e-12, atol=0)
+
+
 @pytest.mark.gpu
 def test_library_matches_heff_fixture():
     import mps_gb300 as mg
