@@ -193,15 +193,20 @@ def profile_traffic(kernel_key):
 
 
 # ---------------------------------------------------------------------------------------------
+def workload_config(chi):
+    """The ``config`` object of the H_eff line, identical in both arms."""
+    return {"workload": f"H_eff matvec, XXZ Delta=0.5, chi={chi} on both bonds, 25 charges "
+                        "binomial profile, d=2, MPO bond 5",
+            "chi": chi,
+            "l2": "GPU steps: L2 flushed before every timed step (512 MiB write); the CPU arm "
+                  "has no device cache to flush"}
+
+
 def oracle_inputs(chi):
-    from mps_gb300 import dmrg as gd
+    """(v, envL, envR, W, W) of the workload as oracle tensors: the same Philox draws the device
+    path uploads, generated by the oracle itself (no library code involved)."""
     from oracle import mps as om
-    from oracle import symtensors as st
-    (sv, sl, sr), flats = gd.heff_inputs_host(chi)
-    conv = lambda sp: tuple(st.VectorSpace(V.sectors, V.isdual) for V in sp)
-    O = [st.from_flat(0, conv(s), f) for s, f in zip((sv, sl, sr), flats)]
-    W = om.xxz_u1mpo(3, 0.5)[1]
-    return O + [W, W]
+    return list(om.heff_workload(chi))
 
 
 def cpu_heff_rate(chi, flops, budget_s=15.0, max_reps=40):
@@ -221,17 +226,18 @@ def cpu_heff_rate(chi, flops, budget_s=15.0, max_reps=40):
 
 
 def run_reference(args):
-    """--impl reference: the reference algorithm's CPU path (the oracle restatement; Julia is not
-    available) timed on the host cores, same metric and workload."""
+    """--impl reference: the reference algorithm's CPU path (the NumPy/OpenBLAS restatement;
+    Julia is not available) timed on the host cores, same metric, unit and workload.  Nothing of
+    the GPU library is imported or loaded here: the inputs come from the oracle's own Philox
+    draws and the flop count from the oracle's own sector GEMMs."""
     ws, rank, _ = dist_info()
     if rank != 0:
         return
     os.environ.setdefault("OPENBLAS_NUM_THREADS", str(os.cpu_count() or 1))
-    from mps_gb300 import dmrg as gd
     from oracle import mps as om
-    flops = gd.heff_flops_meta(*gd.heff_problem(args.chi, meta_only=True))
     O = oracle_inputs(args.chi)
-    for _ in range(max(1, min(args.warmup, 2))):
+    flops = om.heff_flops(*O)  # counts the reference-order sector GEMMs of one application
+    for _ in range(max(0, min(args.warmup, 2) - 1)):
         om.applymps2site(*O)
     times = []
     for _ in range(args.steps):
@@ -246,9 +252,8 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Philox N(0,1) blocks)",
-        "config": {"workload": f"H_eff matvec, XXZ Delta=0.5, chi={args.chi} on both bonds, "
-                               "25 charges binomial profile, d=2, MPO bond 5",
-                   "chi": args.chi},
+        "config": workload_config(args.chi),
+        "gflop_per_step": flops / 1e9,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{args.steps} full H_eff matvecs (NumPy/OpenBLAS oracle; "
                                    "Julia is absent)"},
@@ -431,8 +436,33 @@ def run_ours(args):
         t1 = time.perf_counter()
         if i >= args.warmup:
             e2e_t.append(t1 - t0)
-    e2e_err = float(np.linalg.norm(host_out.numpy() - y64) / np.linalg.norm(y64))
+    e2e_out = host_out.numpy().copy()
+    e2e_err = float(np.linalg.norm(e2e_out - y64) / np.linalg.norm(y64))
     _, e2e_value = replica_rate(statistics.mean(e2e_t), flops, ws, f"cuda:{local}")
+    # the same reference-facing call in plain FP64 (the drop-in), fewer steps
+    e2e64_t = []
+    for i in range(2 + max(3, min(args.steps, 10))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mg.applymps2site_host(*dev, host_in, host_out, precision=0)
+        t1 = time.perf_counter()
+        if i >= 2:
+            e2e64_t.append(t1 - t0)
+    _, e2e64_value = replica_rate(statistics.mean(e2e64_t), flops, ws, f"cuda:{local}")
+    e2e64_out = host_out.numpy().copy()
+
+    # every result of this step against the oracle (the NumPy restatement of the reference's
+    # contraction path, on the host cores) on the same inputs
+    vs_oracle = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import mps as om
+        from oracle import symtensors as ost
+        want = ost.flatten(om.applymps2site(*oracle_inputs(args.chi)))
+        nw = np.linalg.norm(want)
+        rel = lambda y_: float(np.linalg.norm(y_ - want) / nw)
+        vs_oracle = {"headline": rel(y), "fp64": rel(y64), "e2e": rel(e2e_out),
+                     "e2e_fp64": rel(e2e64_out),
+                     "oracle": "NumPy/OpenBLAS restatement of _applymps2site (apply.jl:93-105)"}
 
     peaks = measured_peaks()
     step_ms = sum(ms) / len(ms)
@@ -496,15 +526,17 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": dtype,
         "data": "synthetic (seeded Philox N(0,1) blocks)",
-        "config": {"workload": f"H_eff matvec, XXZ Delta=0.5, chi={args.chi} on both bonds, "
-                               "25 charges binomial profile, d=2, MPO bond 5",
-                   "chi": args.chi, "precision_slices": S, "gflop_per_step": flops / 1e9,
-                   "op_build_ms": op_build_ms,
-                   "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "l2": "flushed before every timed step (512 MiB write)"},
+        "config": workload_config(args.chi),
+        "run": {"precision_slices": S, "gflop_per_step": flops / 1e9,
+                "op_build_ms": op_build_ms,
+                "parallelism": "replicas" if ws > 1 else "single GPU"},
         "fp64": {"value": value64, "unit": UNIT, "ms_per_step": t64 * 1e3,
-                 "speedup_mixed_vs_fp64": t64 / t},
+                 "speedup_mixed_vs_fp64": t64 / t,
+                 "e2e": {"value": e2e64_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                         "d2h_bytes_per_step": d2h,
+                         "call": "mpsg_applymps2site_host, precision 0 (FP64 drop-in)"}},
         "rel_err_vs_fp64": rel_err,
+        "rel_err_vs_oracle": vs_oracle,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "rel_err_vs_fp64": e2e_err,
                 "call": "mpsg_applymps2site_host (uploads on a copy stream overlapped with the "

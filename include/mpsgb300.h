@@ -155,7 +155,10 @@ int mpsg_contract_complex(mpsg_ctx* ctx, const mpsg_tensor* ar, const mpsg_tenso
  * MPSG_ERR_UNSUPPORTED, a fully contracted (scalar) one too. The first call on a device looks
  * up that array's address: make it before any stream capture. Calls share the array, so calls
  * whose kernels overlap on the GPU (different streams or contexts of one device) race; calls
- * on one context are ordered. Returns when the result is complete. */
+ * on one context are ordered. a, b and out must belong to ctx (MPSG_ERR_ARGUMENT otherwise).
+ * Each call plans on the host, stages its task tables and waits for ctx's stream: in a loop it
+ * costs that host work and one synchronisation per call, which mpsg_contract's cached plans do
+ * not. Returns when the result is complete. */
 int mpsg_contract_noalloc(mpsg_ctx* ctx, const mpsg_tensor* a, const int32_t* idxa,
                           const mpsg_tensor* b, const int32_t* idxb, mpsg_tensor* out);
 /* Algorithmic flops of contract(A, idxA, B, idxB) as planned (sum of 2*M*N*K over sectors). */

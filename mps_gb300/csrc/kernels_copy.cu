@@ -425,14 +425,8 @@ void launch_copy(Context* ctx, const DevCopyPlan& p, const double* src, double* 
                                 ctx->stream));
     return;
   }
-  // once per process (the attribute belongs to the kernel, not a device); a thread-safe static,
-  // retried on the next call if setting it failed
-  static const bool attr = [] {
-    MPSG_CUDA(cudaFuncSetAttribute(copy_tasks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)kTileSmem));
-    return true;
-  }();
-  (void)attr;
+  static std::once_flag smem_set[kMaxDevices];  // the attribute is per device
+  set_smem_limit_once(ctx, smem_set, copy_tasks_kernel, (int)kTileSmem);
   const size_t smem = p.has_tile ? kTileSmem : kViewSmem;
   const int64_t ctas = (p.ntiles + kWarps - 1) / kWarps;
   const int64_t grid = std::min<int64_t>(ctas, (int64_t)ctx->num_sms * (p.has_tile ? 3 : 8));

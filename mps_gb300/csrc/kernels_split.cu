@@ -1137,16 +1137,13 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
     }
   }
   if (!(what & kRunGemm)) return;
-  // once per process and slice count (thread-safe static, retried if setting it failed)
-  static const bool attr_set = [] {
-    MPSG_CUDA(cudaFuncSetAttribute(split_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   CF::kSmemBytes));
-    if (S <= 3)
-      MPSG_CUDA(cudaFuncSetAttribute(split_gemm_fast_kernel<S <= 3 ? S : 3>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, FCF::kSmemBytes));
-    return true;
-  }();
-  (void)attr_set;
+  // per device and slice count (one flag array per instantiation of this launcher)
+  static std::once_flag exact_set[kMaxDevices], fast_set[kMaxDevices];
+  if (sp.fast)
+    set_smem_limit_once(ctx, fast_set, split_gemm_fast_kernel<S <= 3 ? S : 3>,
+                        (int)FCF::kSmemBytes);
+  else
+    set_smem_limit_once(ctx, exact_set, split_gemm_kernel<S>, (int)CF::kSmemBytes);
   const int grid = (int)std::min<int64_t>(sp.ntiles, (int64_t)ctx->num_sms);
   KernelTimer timer(ctx, kKindGemmSplit, sp.flops);
   if (sp.fast) {

@@ -19,6 +19,11 @@
 // here accumulates into scratch: the task tables are written by a host-to-device copy and the
 // fused operands and the GEMM output are fully rewritten by the copy and GEMM kernels of each
 // call, so no part of the array needs clearing between calls.
+//
+// Cost: every call plans the contraction on the host, rebuilds its task tables and waits for the
+// context's stream before it returns (the tables are staged from host memory owned by the call).
+// mpsg_contract caches both and returns without waiting, so in a loop this variant pays the
+// host planning and one stream synchronisation per call.
 #include <cstring>
 #include <mutex>
 
@@ -98,6 +103,10 @@ extern "C" int mpsg_contract_noalloc(mpsg_ctx* ctx, const mpsg_tensor* a, const 
     mpsg_capi::need(idxb, "idxb");
     mpsg_capi::need(out, "out");
     Context* c = &ctx->c;
+    // a tensor of another context may live on another device: its pointer would be written
+    // by this device's kernels
+    if (a->t.ctx != c || b->t.ctx != c || out->t.ctx != c)
+      throw Error(kErrArgument, "mpsg_contract_noalloc: a, b and out must belong to ctx");
     unsigned char* dev = scratch_base(c->device);
     auto plan = plan_contract(a->t.meta, mpsg_capi::ivec(idxa, a->t.meta.N()), b->t.meta,
                               mpsg_capi::ivec(idxb, b->t.meta.N()));

@@ -215,6 +215,28 @@ struct KernelTimer {
 };
 void collect_kernel_times(Context* ctx);
 
+// Raises a kernel's dynamic shared-memory limit on the context's device.  A function attribute
+// belongs to one device's context, so it is set once per device: ``flags`` is the caller's
+// per-kernel array of once-flags, indexed by device ordinal.  Thread-safe; a failed attempt
+// throws and is retried on the next launch.
+constexpr int kMaxDevices = 64;
+template <class Kernel>
+void set_smem_limit_once(Context* ctx, std::once_flag (&flags)[kMaxDevices], Kernel kernel,
+                         int bytes) {
+  if (ctx->device < 0 || ctx->device >= kMaxDevices)
+    throw Error(kErrArgument, "device ordinal out of range");
+  std::call_once(flags[ctx->device], [&] {
+    int cur = -1;
+    MPSG_CUDA(cudaGetDevice(&cur));
+    if (cur != ctx->device) MPSG_CUDA(cudaSetDevice(ctx->device));
+    const cudaError_t e =
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (cur != ctx->device) cudaSetDevice(cur);
+    if (e != cudaSuccess)
+      throw Error(kErrCuda, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  });
+}
+
 // ---- kernel launchers (kernels_*.cu) ----
 void launch_copy(Context* ctx, const DevCopyPlan& p, const double* src, double* dst);
 void launch_gemm_f64(Context* ctx, const DevGemmPlan& p, const double* A, const double* B,

@@ -244,8 +244,10 @@ class OffloadedEnvs:
 
     def _evict(self):
         while len(self._dev) > self.window or self._over_budget():
-            # prefetched entries the sweep has not read yet go last
-            cand = [j for j in self._order if j not in self._pending] or self._order
+            # the entry just read, written or fetched (the last in the order) stays; among the
+            # others, prefetched entries the sweep has not read yet go last
+            others = self._order[:-1] if len(self._order) > 1 else self._order
+            cand = [j for j in others if j not in self._pending] or others
             j = cand[0]
             self._order.remove(j)
             self._pending.pop(j, None)

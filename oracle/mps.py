@@ -300,3 +300,65 @@ def binomial_bond_dims(lx, site, M, chimax, d=2):
     cmax = min(M, (d - 1) * site)
     return [(c, max(1, min(chimax, math.comb(site, c), math.comb(lx - site, M - c))))
             for c in range(cmin, cmax + 1)]
+
+
+# ---------------------------------------------------------------------------------------------
+# The chi-dimensional two-site H_eff input (synthetic: the reference publishes no dataset).  Legs
+# follow the reference's conventions: v (Vl, d, d, dual(Vr)) as a two-site MPS tensor
+# (symmps.jl:63-64), envL (dual(Vl), dual(Vw), Vl) and envR (Vr, Vw, dual(Vr)) (dmrg.jl:25-26),
+# W the middle XXZ MPO tensor (symmpo.jl:45-97).
+# ---------------------------------------------------------------------------------------------
+def binomial_profile(chi: int, ncharges: int = 25):
+    """Bond dimensions per charge: chi * C(n-1, k) / 2^(n-1), at least one state per charge,
+    rounded by largest remainder in mirror-symmetric pairs so that they sum to chi."""
+    n = ncharges - 1
+    exact = [chi * math.comb(n, k) / 2.0 ** n for k in range(ncharges)]
+    dims = [max(1, int(math.floor(x))) for x in exact]
+    left = chi - sum(dims)
+    rank = sorted(range(ncharges), key=lambda k: (-(exact[k] - math.floor(exact[k])),
+                                                  abs(k - n / 2)))
+    sgn = 1 if left > 0 else -1
+    for i in range(10 * ncharges):
+        if left == 0:
+            break
+        k = rank[i % ncharges]
+        m = n - k
+        if k == m:
+            if dims[k] + sgn >= 1:
+                dims[k] += sgn
+                left -= sgn
+        elif abs(left) >= 2 and dims[k] + sgn >= 1 and dims[m] + sgn >= 1:
+            dims[k] += sgn
+            dims[m] += sgn
+            left -= 2 * sgn
+    if left != 0:
+        dims[n // 2] += left
+    return dims
+
+
+def heff_workload(chi: int, delta: float = 0.5, seed: int = 1911, ncharges: int = 25):
+    """(v, envL, envR, W, W) of the two-site H_eff benchmark: both bonds carry charges
+    0..ncharges-1 with the binomial profile of ``chi`` states, the site space is (0=>1, 1=>1),
+    and every block of v, envL, envR (in that order, each in reference block order, each block
+    column-major) is drawn N(0,1) from one Philox(seed) stream."""
+    Vb = st.VectorSpace([(k, dk) for k, dk in enumerate(binomial_profile(chi, ncharges))])
+    d = U1Space((0, 1), (1, 1))
+    Vw = U1Space((-1, 1), (0, 3), (1, 1))
+    spaces = ((Vb, d, d, dual_space(Vb)), (dual_space(Vb), dual_space(Vw), Vb),
+              (Vb, Vw, dual_space(Vb)))
+    rng = np.random.Generator(np.random.Philox(seed))
+    out = []
+    for sp in spaces:
+        sects, sizes = st.allsectorsandsizes(0, sp)
+        n = sum(int(np.prod(z)) for z in sizes)
+        out.append(st.from_flat(0, sp, rng.standard_normal(n)))
+    W = xxz_u1mpo(3, delta)[1]
+    return out[0], out[1], out[2], W, W
+
+
+def heff_flops(v, envL, envR, W1, W2) -> float:
+    """Algorithmic flops (sum of 2*M*N*K over the sector GEMMs) of one ``applymps2site`` in the
+    reference's contraction order, counted by running it once."""
+    with st.FlopCount() as fc:
+        applymps2site(v, envL, envR, W1, W2)
+    return fc.flops

@@ -27,8 +27,29 @@ __all__ = [
     "splitleg", "symmatrix", "symvector", "matmul", "split_matrix", "contract",
     "contract_index_perm", "dual", "array", "fill", "fill_linearindex", "eye", "from_blocks",
     "dot", "norm", "axpy", "axpby", "rmul", "scaled", "similar_zeros", "svd_", "svdtrunc",
-    "truncatedsizes", "flatten", "from_flat", "SpaceMismatch",
+    "truncatedsizes", "flatten", "from_flat", "SpaceMismatch", "FlopCount",
 ]
+
+
+class FlopCount:
+    """Context manager that sums the algorithmic flops of the sector GEMMs ``matmul`` performs
+    while it is active: 2*M*N*K for every output block whose two partner blocks exist
+    (contract.jl:284-291); allowed sectors without a partner (contract.jl:292-294) cost nothing.
+    This is the flop count of the reference's own contraction order, which the benchmark's
+    GFLOP/s figures use.  ``FlopCount().flops`` after the ``with`` block holds the total."""
+
+    _active: list = []
+
+    def __init__(self):
+        self.flops = 0.0
+
+    def __enter__(self):
+        FlopCount._active.append(self)
+        return self
+
+    def __exit__(self, *exc):
+        FlopCount._active.remove(self)
+        return False
 
 
 class SpaceMismatch(Exception):
@@ -556,7 +577,10 @@ def matmul(A: SymTensor, B: SymTensor) -> SymTensor:
             sa = (c1, A.charge - _c1)
             sb = (-B.charge + _c2, c2)
         if sa in A.blocks and sb in B.blocks:
-            blocks[(c1, c2)] = _blockmat(A, sa) @ _blockmat(B, sb)
+            a, b = _blockmat(A, sa), _blockmat(B, sb)
+            for fc in FlopCount._active:
+                fc.flops += 2.0 * a.shape[0] * b.shape[1] * a.shape[1]
+            blocks[(c1, c2)] = a @ b
         else:
             blocks[(c1, c2)] = np.zeros(z, dtype=dt)
     return SymTensor(charge, space, blocks, check=False)

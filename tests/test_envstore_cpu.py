@@ -260,3 +260,28 @@ def test_byte_budget_bounds_the_resident_entries():
         assert st.resident_bytes() <= max(budget, 8 * sizes[i])
     with pytest.raises(ValueError):
         OffloadedEnvs(envs, load=load, budget_bytes=0)
+
+
+def test_byte_budget_keeps_the_entry_just_used_beside_pending_prefetches():
+    """A budget below two entries while the only other resident entries are prefetches that the
+    sweep has not read: eviction takes a prefetch, never the entry just read."""
+    stream = _Stream()
+    tr = _FakeAsync(stream)
+    n = 6
+    envs = [_T(0, ("E", i, 4), np.arange(4.0) + 10 * i) for i in range(n)]
+    st = OffloadedEnvs(envs, window=n, transfer=tr, budget_bytes=8 * 4 + 8)
+    stream.complete()
+    assert st.resident() == [n - 1]
+    assert st.prefetch(0)       # its upload is pending: the sweep has not read it yet
+    assert st.resident()[-1] == 0 and 0 in st.resident()
+    uploads = st.uploads
+    got = _read(stream, st[2])  # a read while prefetch 0 is pending
+    np.testing.assert_array_equal(got, np.arange(4.0) + 20)
+    assert st.resident() == [2]  # the pending prefetch went, the entry just read stayed
+    assert st.uploads == uploads + 1
+    np.testing.assert_array_equal(_read(stream, st[2]), np.arange(4.0) + 20)
+    assert st.uploads == uploads + 1  # read again without another upload
+    stream.complete()
+    for i in range(n):
+        np.testing.assert_array_equal(_read(stream, st[i]), np.arange(4.0) + 10 * i)
+        assert st.resident()[-1] == i

@@ -3,7 +3,10 @@
 Both entry points run the same planner and kernels; the no-alloc one keeps its task tables and
 fused operands in a fixed device array instead of allocated buffers. The results must agree to
 the FP64 contraction tolerance on consecutive calls of different shapes (the array keeps the
-previous call's contents). Collected last so that it also runs after every other GPU test.
+previous call's contents), and a call must leave the device's memory use where it found it: the
+bytes in use in the default memory pool (where stream-ordered allocations come from) and the
+device's free memory (which any cudaMalloc would lower) are read through the CUDA driver before
+and after. Collected last so that it also runs after every other GPU test.
 """
 import ctypes as C
 
@@ -28,6 +31,24 @@ def noalloc(A, ia, B, ib, out):
     _lib.call("mpsg_contract_noalloc", A.ctx.handle, A.handle, _lib.i32arr(ia), B.handle,
               _lib.i32arr(ib), out.handle)
     return out
+
+
+_CU_MEMPOOL_ATTR_USED_MEM_CURRENT = 7  # CUmemPool_attribute (cuda.h)
+
+
+def device_memory_in_use(device=0):
+    """(bytes in use in the device's default memory pool, free bytes on the device), read with
+    the driver API after the device has finished all work."""
+    cu = C.CDLL("libcuda.so.1")
+    assert cu.cuCtxSynchronize() == 0
+    pool = C.c_void_p()
+    assert cu.cuDeviceGetDefaultMemPool(C.byref(pool), C.c_int(device)) == 0
+    used = C.c_uint64()
+    assert cu.cuMemPoolGetAttribute(pool, C.c_int(_CU_MEMPOOL_ATTR_USED_MEM_CURRENT),
+                                    C.byref(used)) == 0
+    free, total = C.c_size_t(), C.c_size_t()
+    assert cu.cuMemGetInfo_v2(C.byref(free), C.byref(total)) == 0
+    return used.value, free.value
 
 
 def heff_chain(ctx, chi, seed):
@@ -59,6 +80,24 @@ def test_noalloc_matches_contract_on_consecutive_calls():
         assert prev_out is not None
 
 
+def test_noalloc_allocates_nothing():
+    """Two calls in a row, after one untimed call that looks up the scratch array (and loads the
+    kernels): neither changes the pool's bytes in use nor the device's free memory."""
+    ctx = mg.Context(0)
+    a, b = heff_chain(ctx, 128, 8)
+    ia, ib = STEPS[0]
+    ref = mg.contract(a[0], ia, b[0], ib, precision=0)
+    outs = [mg.zeros(ref.charge, ref.space, ctx) for _ in range(3)]
+    noalloc(a[0], ia, b[0], ib, outs[0])
+    before = device_memory_in_use()
+    noalloc(a[0], ia, b[0], ib, outs[1])
+    noalloc(a[0], ia, b[0], ib, outs[2])
+    after = device_memory_in_use()
+    assert after == before, (before, after)
+    for out in outs:
+        assert relerr(out.to_flat(), ref.to_flat()) <= RTOL
+
+
 def test_noalloc_rejects_what_it_cannot_do():
     ctx = mg.Context(0)
     a, b = heff_chain(ctx, 64, 7)
@@ -82,3 +121,13 @@ def test_noalloc_rejects_what_it_cannot_do():
         noalloc(big, (-1, 1), vec, (-1, 2), res)
     assert e.value.code == _lib.ERR_UNSUPPORTED
     assert "64 MiB" in str(e.value)
+    # every tensor must belong to the calling context
+    other = mg.Context(0)
+    out_other = mg.zeros(ref.charge, ref.space, other)
+    with pytest.raises(mg.MPSGError) as e:
+        noalloc(a[0], STEPS[0][0], b[0], STEPS[0][1], out_other)
+    assert e.value.code == _lib.ERR_ARGUMENT
+    with pytest.raises(mg.MPSGError) as e:  # operands of ctx called through another context
+        _lib.call("mpsg_contract_noalloc", other.handle, a[0].handle, _lib.i32arr(STEPS[0][0]),
+                  b[0].handle, _lib.i32arr(STEPS[0][1]), out_other.handle)
+    assert e.value.code == _lib.ERR_ARGUMENT
