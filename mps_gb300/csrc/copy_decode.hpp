@@ -7,6 +7,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 
 #if defined(__CUDACC__)
 #define MPSG_HD __host__ __device__ __forceinline__
@@ -67,6 +68,54 @@ MPSG_HD void task_span(const int64_t* ext, const int64_t* str, int nd, int64_t o
     const int64_t step = (ext[i] > 0 ? ext[i] - 1 : 0) * str[i];
     if (step < 0) lo += step;
     else hi += step;
+  }
+}
+
+// One unit of the row path: element i < len (len <= the unit bound) goes from
+// src + soff + i * sstr to dst + doff + i * dstr. Rows with sstr == 1 are staged through shared
+// memory by bulk asynchronous copies; the others are read element by element.
+struct BulkRow {
+  int64_t soff, doff;
+  int32_t len, sstr, dstr, pad;
+};
+
+// 16-byte-aligned interior [i0, i1) of the byte span of len doubles starting at byte address a0
+// (i1 == i0 when there is none): the part of a row a bulk asynchronous copy can move. At most
+// one element before i0 and one after i1 remain.
+MPSG_HD void row_interior(uint64_t a0, int64_t len, uint64_t& i0, uint64_t& i1) {
+  const uint64_t a1 = a0 + 8 * (uint64_t)len;
+  i0 = (a0 + 15) & ~(uint64_t)15;
+  i1 = a1 & ~(uint64_t)15;
+  if (i1 < i0) i1 = i0;
+}
+
+// Appends the rows of a task along axis a: one row per position of the other axes (decoded by
+// plain division, the first other axis fastest), each cut into ceil(ext[a] / max_elems) pieces
+// of nearly equal length. Strides along a must fit in 32 bits.
+inline void append_bulk_rows(int nd, const int64_t* ext, const int64_t* sstr,
+                             const int64_t* dstr, int64_t soff, int64_t doff, int a,
+                             int max_elems, std::vector<BulkRow>& rows) {
+  int ax[16];
+  int nax = 0;
+  int64_t outer = 1;
+  for (int i = 0; i < nd; ++i)
+    if (i != a) {
+      ax[nax++] = i;
+      outer *= ext[i];
+    }
+  const int64_t len = ext[a];
+  const int64_t pieces = (len + max_elems - 1) / max_elems;
+  const int64_t base = len / pieces, extra = len % pieces;  // `extra` pieces get one more
+  for (int64_t q = 0; q < outer; ++q) {
+    int64_t so = soff, dof = doff;
+    ref_decode(ext, sstr, dstr, ax, nax, q, so, dof);
+    int64_t c = 0;
+    for (int64_t p = 0; p < pieces; ++p) {
+      const int64_t n = base + (p < extra ? 1 : 0);
+      rows.push_back(BulkRow{so + c * sstr[a], dof + c * dstr[a], (int32_t)n, (int32_t)sstr[a],
+                             (int32_t)dstr[a], 0});
+      c += n;
+    }
   }
 }
 

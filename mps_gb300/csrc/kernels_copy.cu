@@ -16,10 +16,20 @@
 //              per lane and step, each decoded to its source address. Writes stay coalesced and
 //              reads follow the source's short runs through the caches.
 //
+// Tasks whose source and destination share a unit-stride axis of at least 32 elements (the
+// bulk of every fusion and split of the contraction path) do not go through the warp units:
+// the host cuts them into rows of at most 512 elements and copy_rows_bulk_kernel moves them.
+// Each warp keeps a ring of kBulkStages row slots in shared memory; one lane stages the
+// 16-byte-aligned interior of each row with a bulk asynchronous copy (cp.async.bulk, completion
+// counted on the slot's mbarrier) several rows ahead, and the warp writes the row out with
+// coalesced stores, reading the at most two unaligned end elements straight from global memory.
+// A few KB per warp in flight keep HBM busy with one load instruction per row.
+//
 // Built with MPSG_DEVICE_CHECKS (the device-checked debug library), the kernel also recomputes
 // every decoded offset by plain division, checks every address against its task's span, records
 // the first violation and a count in device memory (read_device_checks) and skips the access.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "copy_decode.hpp"
@@ -299,6 +309,142 @@ __global__ void __launch_bounds__(32 * kWarps, 4) copy_tasks_kernel(
 constexpr size_t kViewSmem = sizeof(WarpView) * kWarps;
 constexpr size_t kTileSmem = kViewSmem + sizeof(TileBuf) * kWarps;
 
+// ---- TMA-staged rows --------------------------------------------------------------------------
+constexpr int kBulkWarps = 8;
+constexpr int kBulkStages = 3;
+constexpr int kSlotBytes = kBulkMaxRow * 8;  // a row's aligned interior is at most its bytes
+constexpr size_t kBulkSmem = (size_t)kBulkWarps * kBulkStages * kSlotBytes +
+                             sizeof(uint64_t) * kBulkWarps * kBulkStages;
+constexpr long long kBulkWaitCycles = 4000000000LL;  // about 2 s at the maximum SM clock
+enum BulkError { kBulkErrWait = 1, kBulkErrDrain = 2 };
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool bulk_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for a slot's phase; false after about 2 s.
+__device__ __forceinline__ bool bulk_wait(uint64_t* bar, uint32_t parity) {
+  if (bulk_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!bulk_try_wait(bar, parity))
+    if (clock64() - t0 > kBulkWaitCycles) return false;
+  return true;
+}
+
+// Byte span [i0, i1) of row r's 16-byte-aligned interior in the source.
+__device__ __forceinline__ void row_span(const double* src, const BulkRow& r, uint64_t& a0,
+                                         uint64_t& i0, uint64_t& i1) {
+  a0 = (uint64_t)(uintptr_t)(src + r.soff);
+  row_interior(a0, r.len, i0, i1);
+}
+
+// Lane 0: stage row u's interior into `slot`, completion counted on `bar` (a strided row or an
+// empty interior just arrives, so the phase still completes).
+__device__ __forceinline__ void bulk_issue(const BulkRow* rows, int64_t u, const double* src,
+                                           unsigned char* slot, uint64_t* bar) {
+  const BulkRow r = rows[u];
+  uint64_t a0, i0, i1;
+  row_span(src, r, a0, i0, i1);
+  const uint32_t bytes = r.sstr == 1 ? (uint32_t)(i1 - i0) : 0u;
+  if (bytes == 0) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+    return;
+  }
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(slot)),
+      "l"(i0), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Persistent grid; warp w of the grid moves rows w, w + W, w + 2W, ... (W = warps in the grid),
+// kBulkStages rows in flight. A wait that expires records kBulkErrWait in *err, and the warp
+// stops after draining the copies it has in flight (bounded as well; kBulkErrDrain if that
+// expires too).
+__global__ void __launch_bounds__(32 * kBulkWarps, 2) copy_rows_bulk_kernel(
+    const BulkRow* __restrict__ rows, int64_t nrows, const double* __restrict__ src,
+    double* __restrict__ dst, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char bulk_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char* slots = bulk_smem + (size_t)warp * kBulkStages * kSlotBytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(bulk_smem + (size_t)kBulkWarps * kBulkStages *
+                                                               kSlotBytes) +
+                   warp * kBulkStages;
+  const int64_t W = (int64_t)gridDim.x * kBulkWarps;
+  const int64_t first = (int64_t)blockIdx.x * kBulkWarps + warp;
+  const int64_t mine = first < nrows ? (nrows - 1 - first) / W + 1 : 0;
+  if (mine == 0) return;
+  if (lane == 0) {
+    for (int s = 0; s < kBulkStages; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[s])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    for (int64_t j = 0; j < mine && j < kBulkStages; ++j)
+      bulk_issue(rows, first + j * W, src, slots + j * kSlotBytes, &bars[j]);
+  }
+  __syncwarp();
+  for (int64_t j = 0; j < mine; ++j) {
+    const int s = (int)(j % kBulkStages);
+    const uint32_t parity = (uint32_t)((j / kBulkStages) & 1);
+    const bool ok = bulk_wait(&bars[s], parity);
+    if (!__all_sync(0xffffffffu, ok)) {
+      // give up: wait (bounded) for every copy this warp still has in flight, this row's
+      // included, before the block's shared memory goes away
+      if (lane == 0) {
+        atomicCAS(err, 0, kBulkErrWait);
+        for (int64_t k = j; k < mine && k < j + kBulkStages; ++k)
+          if (!bulk_wait(&bars[k % kBulkStages], (uint32_t)((k / kBulkStages) & 1))) {
+            atomicCAS(err, kBulkErrWait, kBulkErrDrain);
+            break;
+          }
+      }
+      __syncwarp();
+      return;
+    }
+    const BulkRow r = rows[first + j * W];
+    uint64_t a0, i0, i1;
+    row_span(src, r, a0, i0, i1);
+    const double* slot = reinterpret_cast<const double*>(slots + s * kSlotBytes);
+    const double* gsrc = src + r.soff;
+    double* gdst = dst + r.doff;
+    if (r.sstr == 1 && r.dstr == 1) {
+#pragma unroll 4
+      for (int i = lane; i < r.len; i += 32) {
+        const uint64_t g = a0 + 8 * (uint64_t)i;
+        gdst[i] = (g >= i0 && g < i1) ? slot[(g - i0) >> 3] : __ldg(gsrc + i);
+      }
+    } else if (r.sstr == 1) {
+      for (int i = lane; i < r.len; i += 32) {
+        const uint64_t g = a0 + 8 * (uint64_t)i;
+        gdst[(int64_t)i * r.dstr] = (g >= i0 && g < i1) ? slot[(g - i0) >> 3] : __ldg(gsrc + i);
+      }
+    } else {  // a strided source row: plain loads
+      for (int i = lane; i < r.len; i += 32)
+        gdst[(int64_t)i * r.dstr] = __ldg(gsrc + (int64_t)i * r.sstr);
+    }
+    __syncwarp();  // every lane has read the slot before it is refilled
+    if (lane == 0 && j + kBulkStages < mine) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bulk_issue(rows, first + (j + kBulkStages) * W, src, slots + s * kSlotBytes, &bars[s]);
+    }
+  }
+}
+
 }  // namespace
 
 size_t copy_aux_bytes() { return sizeof(TaskAux); }
@@ -332,109 +478,197 @@ void read_device_checks(Context* ctx, bool reset, int64_t* count, int64_t* first
 void DevCopyPlan::upload(const std::vector<CopyTask>& tasks, bool identity_, cudaStream_t st) {
   release();
   stream = st;
+  std::vector<CopyTask> rest;
   std::vector<int64_t> prefix;
   std::vector<unsigned char> aux;
-  build_host(tasks, identity_, prefix, aux);
-  if (ntasks == 0) return;
+  std::vector<BulkRow> rows;
+  build_host(tasks, identity_, rest, prefix, aux, rows);
   // stream-ordered: no device-wide synchronisation, so contexts on one GPU do not serialise on
   // plan uploads (pageable sources are staged before the calls return)
-  MPSG_CUDA(cudaMallocAsync((void**)&d_tasks, sizeof(CopyTask) * ntasks, st));
-  MPSG_CUDA(cudaMallocAsync((void**)&d_prefix, sizeof(int64_t) * (ntasks + 1), st));
-  MPSG_CUDA(cudaMallocAsync(&d_aux, aux.size(), st));
-  MPSG_CUDA(cudaMemcpyAsync(d_tasks, tasks.data(), sizeof(CopyTask) * ntasks,
-                            cudaMemcpyHostToDevice, st));
-  MPSG_CUDA(cudaMemcpyAsync(d_prefix, prefix.data(), sizeof(int64_t) * (ntasks + 1),
-                            cudaMemcpyHostToDevice, st));
-  MPSG_CUDA(cudaMemcpyAsync(d_aux, aux.data(), aux.size(), cudaMemcpyHostToDevice, st));
+  if (ntasks > 0) {
+    MPSG_CUDA(cudaMallocAsync((void**)&d_tasks, sizeof(CopyTask) * ntasks, st));
+    MPSG_CUDA(cudaMallocAsync((void**)&d_prefix, sizeof(int64_t) * (ntasks + 1), st));
+    MPSG_CUDA(cudaMallocAsync(&d_aux, aux.size(), st));
+    MPSG_CUDA(cudaMemcpyAsync(d_tasks, rest.data(), sizeof(CopyTask) * ntasks,
+                              cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(d_prefix, prefix.data(), sizeof(int64_t) * (ntasks + 1),
+                              cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(d_aux, aux.data(), aux.size(), cudaMemcpyHostToDevice, st));
+  }
+  if (nrows > 0) {
+    MPSG_CUDA(cudaMallocAsync((void**)&d_rows, sizeof(BulkRow) * nrows, st));
+    MPSG_CUDA(cudaMemcpyAsync(d_rows, rows.data(), sizeof(BulkRow) * nrows,
+                              cudaMemcpyHostToDevice, st));
+  }
 }
 
 void DevCopyPlan::build_host(const std::vector<CopyTask>& tasks, bool identity_,
-                             std::vector<int64_t>& prefix, std::vector<unsigned char>& aux_bytes) {
+                             std::vector<CopyTask>& rest, std::vector<int64_t>& prefix,
+                             std::vector<unsigned char>& aux_bytes, std::vector<BulkRow>& rows) {
   identity = identity_;
   has_tile = false;
-  ntasks = (int)tasks.size();
-  prefix.assign(ntasks + 1, 0);
-  std::vector<TaskAux> aux(ntasks);
+  rest.clear();
+  rows.clear();
+  aux_bytes.clear();
+  prefix.assign(1, 0);
   elems = 0;
-  for (int k = 0; k < ntasks; ++k) {
+  // axis roles per task: a = destination's fastest axis, b = source's fastest axis
+  const size_t nt = tasks.size();
+  std::vector<int> ta(nt), tb(nt);
+  int64_t bulk_elems = 0, other_rows = 0, bulk_rows = 0;
+  for (size_t k = 0; k < nt; ++k) {
     const CopyTask& T = tasks[k];
-    TaskAux& X = aux[k];
-    std::memset(&X, 0, sizeof(X));
     int a = 0, b = 0;
     for (int i = 1; i < T.nd; ++i) {
       if (T.dstr[i] < T.dstr[a]) a = i;
       if (T.sstr[i] < T.sstr[b]) b = i;
     }
+    ta[k] = a;
+    tb[k] = b;
     const int64_t n = T.numel();
     if (n >= ((int64_t)1 << 31)) throw Error(kErrUnsupported, "copy task above 2^31 elements");
     elems += n;
-    for (int i = 0; i < T.nd; ++i) magic_u31((uint32_t)T.ext[i], X.mag[i], X.shf[i]);
-    const bool unit_a = T.dstr[a] == 1, unit_b = T.sstr[b] == 1;
-    int64_t units;
-    if (a == b && unit_a && unit_b && T.ext[a] >= 32) {
-      X.mode = kModeRow;
-      X.outer = n / T.ext[a];
-      if (T.ext[a] > kRowElems) {  // long rows: several warps share a row
-        const int64_t cpr = (T.ext[a] + kRowElems - 1) / kRowElems;
-        X.rows_per_unit = -(int32_t)cpr;
-        units = X.outer * cpr;
-      } else {
-        X.rows_per_unit =
-            (int)std::max<int64_t>(1, std::min<int64_t>(X.outer, kRowElems / T.ext[a]));
-        units = (X.outer + X.rows_per_unit - 1) / X.rows_per_unit;
-      }
-    } else if (a != b && unit_a && unit_b && T.ext[a] >= 16 && T.ext[b] >= 16) {
-      X.mode = kModeTile;
-      has_tile = true;
-      const int64_t rest = n / (T.ext[a] * T.ext[b]);
-      X.outer = ((T.ext[a] + kT - 1) / kT) * ((T.ext[b] + kT - 1) / kT) * rest;
-      units = X.outer;
+    if (n == 0) continue;
+    const int64_t ea = T.nd > 0 ? T.ext[a] : 1;
+    const int64_t nrow = (n / ea) * ((ea + kBulkMaxRow - 1) / kBulkMaxRow);
+    if (T.nd > 0 && a == b && T.dstr[a] == 1 && T.sstr[a] == 1 && ea >= kBulkMinRow) {
+      bulk_elems += n;
+      bulk_rows += nrow;
     } else {
-      X.mode = kModeGather;
-      X.outer = n;
-      for (int i = 0; i < T.nd; ++i) X.order[i] = i;
-      std::stable_sort(X.order, X.order + T.nd,
-                       [&](int x, int y) { return T.dstr[x] < T.dstr[y]; });
-      units = (n + kGatherUnit - 1) / kGatherUnit;
+      other_rows += nrow;
     }
-    X.a = a;
-    X.b = b;
-    prefix[k + 1] = prefix[k] + units;
   }
-  ntiles = prefix[ntasks];
-  aux_bytes.resize(sizeof(TaskAux) * ntasks);
-  if (ntasks) std::memcpy(aux_bytes.data(), aux.data(), aux_bytes.size());
+  // the row table when nearly everything is long unit-stride rows and the other tasks add few
+  // rows (each row costs one table entry and one pass of a warp)
+  bool strides_fit = true;
+  for (size_t k = 0; k < nt && strides_fit; ++k)
+    if (tasks[k].nd > 0 && (std::abs(tasks[k].sstr[ta[k]]) >= ((int64_t)1 << 31) ||
+                            std::abs(tasks[k].dstr[ta[k]]) >= ((int64_t)1 << 31)))
+      strides_fit = false;
+  const bool use_rows = !identity && strides_fit && bulk_elems > 0 &&
+                        20 * (elems - bulk_elems) <= elems &&
+                        other_rows <= std::max<int64_t>(4096, bulk_rows / 4);
+  if (use_rows) {
+    for (size_t k = 0; k < nt; ++k) {
+      const CopyTask& T = tasks[k];
+      if (T.numel() == 0) continue;
+      if (T.nd == 0) {
+        rows.push_back(BulkRow{T.soff, T.doff, 1, 1, 1, 0});
+        continue;
+      }
+      append_bulk_rows(T.nd, T.ext, T.sstr, T.dstr, T.soff, T.doff, ta[k], kBulkMaxRow, rows);
+    }
+  } else {
+    std::vector<TaskAux> aux;
+    for (size_t k = 0; k < nt; ++k) {
+      const CopyTask& T = tasks[k];
+      const int64_t n = T.numel();
+      if (n == 0) continue;
+      const int a = ta[k], b = tb[k];
+      const bool unit_a = T.nd > 0 && T.dstr[a] == 1, unit_b = T.nd > 0 && T.sstr[b] == 1;
+      TaskAux X;
+      std::memset(&X, 0, sizeof(X));
+      for (int i = 0; i < T.nd; ++i) magic_u31((uint32_t)T.ext[i], X.mag[i], X.shf[i]);
+      int64_t units;
+      if (a == b && unit_a && unit_b && T.ext[a] >= 32) {
+        X.mode = kModeRow;
+        X.outer = n / T.ext[a];
+        if (T.ext[a] > kRowElems) {  // long rows: several warps share a row
+          const int64_t cpr = (T.ext[a] + kRowElems - 1) / kRowElems;
+          X.rows_per_unit = -(int32_t)cpr;
+          units = X.outer * cpr;
+        } else {
+          X.rows_per_unit =
+              (int)std::max<int64_t>(1, std::min<int64_t>(X.outer, kRowElems / T.ext[a]));
+          units = (X.outer + X.rows_per_unit - 1) / X.rows_per_unit;
+        }
+      } else if (a != b && unit_a && unit_b && T.ext[a] >= 16 && T.ext[b] >= 16) {
+        X.mode = kModeTile;
+        has_tile = true;
+        const int64_t rest_ = n / (T.ext[a] * T.ext[b]);
+        X.outer = ((T.ext[a] + kT - 1) / kT) * ((T.ext[b] + kT - 1) / kT) * rest_;
+        units = X.outer;
+      } else {
+        X.mode = kModeGather;
+        X.outer = n;
+        for (int i = 0; i < T.nd; ++i) X.order[i] = i;
+        std::stable_sort(X.order, X.order + T.nd,
+                         [&](int x, int y) { return T.dstr[x] < T.dstr[y]; });
+        units = (n + kGatherUnit - 1) / kGatherUnit;
+      }
+      X.a = a;
+      X.b = b;
+      rest.push_back(T);
+      aux.push_back(X);
+      prefix.push_back(prefix.back() + units);
+    }
+    aux_bytes.resize(sizeof(TaskAux) * aux.size());
+    if (!aux.empty()) std::memcpy(aux_bytes.data(), aux.data(), aux_bytes.size());
+  }
+  ntasks = (int)rest.size();
+  ntiles = prefix.back();
+  nrows = (int64_t)rows.size();
 }
 
 void DevCopyPlan::release() {
   if (d_tasks) cudaFreeAsync(d_tasks, stream);
   if (d_prefix) cudaFreeAsync(d_prefix, stream);
   if (d_aux) cudaFreeAsync(d_aux, stream);
+  if (d_rows) cudaFreeAsync(d_rows, stream);
   d_tasks = nullptr;
   d_prefix = nullptr;
   d_aux = nullptr;
+  d_rows = nullptr;
   ntasks = 0;
   ntiles = 0;
+  nrows = 0;
 }
 
 void launch_copy(Context* ctx, const DevCopyPlan& p, const double* src, double* dst) {
-  if (p.ntiles == 0) return;
+  if (p.elems == 0) return;
   if (p.identity) {
     if (src != dst)
       MPSG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * p.elems, cudaMemcpyDeviceToDevice,
                                 ctx->stream));
     return;
   }
-  static std::once_flag smem_set[kMaxDevices];  // the attribute is per device
-  set_smem_limit_once(ctx, smem_set, copy_tasks_kernel, (int)kTileSmem);
-  const size_t smem = p.has_tile ? kTileSmem : kViewSmem;
-  const int64_t ctas = (p.ntiles + kWarps - 1) / kWarps;
-  const int64_t grid = std::min<int64_t>(ctas, (int64_t)ctx->num_sms * (p.has_tile ? 3 : 8));
-  KernelTimer timer(ctx, kKindCopy);
-  copy_tasks_kernel<<<(unsigned)grid, 32 * kWarps, smem, ctx->stream>>>(
-      p.d_tasks, p.d_prefix, (const TaskAux*)p.d_aux, p.ntasks, p.ntiles, src, dst);
-  MPSG_CUDA(cudaGetLastError());
-  ctx->kernel_launches++;
+  if (p.nrows > 0) {
+    static std::once_flag bulk_set[kMaxDevices];
+    set_smem_limit_once(ctx, bulk_set, copy_rows_bulk_kernel, (int)kBulkSmem);
+    const int64_t ctas = (p.nrows + kBulkWarps - 1) / kBulkWarps;
+    const int64_t grid = std::min<int64_t>(ctas, (int64_t)ctx->num_sms * 2);
+    KernelTimer timer(ctx, kKindCopy);
+    copy_rows_bulk_kernel<<<(unsigned)grid, 32 * kBulkWarps, kBulkSmem, ctx->stream>>>(
+        p.d_rows, p.nrows, src, dst, ctx->d_copy_err);
+    MPSG_CUDA(cudaGetLastError());
+    ctx->kernel_launches++;
+  }
+  if (p.ntiles > 0) {
+    static std::once_flag smem_set[kMaxDevices];  // the attribute is per device
+    set_smem_limit_once(ctx, smem_set, copy_tasks_kernel, (int)kTileSmem);
+    const size_t smem = p.has_tile ? kTileSmem : kViewSmem;
+    const int64_t ctas = (p.ntiles + kWarps - 1) / kWarps;
+    const int64_t grid = std::min<int64_t>(ctas, (int64_t)ctx->num_sms * (p.has_tile ? 3 : 8));
+    KernelTimer timer(ctx, kKindCopy);
+    copy_tasks_kernel<<<(unsigned)grid, 32 * kWarps, smem, ctx->stream>>>(
+        p.d_tasks, p.d_prefix, (const TaskAux*)p.d_aux, p.ntasks, p.ntiles, src, dst);
+    MPSG_CUDA(cudaGetLastError());
+    ctx->kernel_launches++;
+  }
+  if (ctx->debug_sync && p.nrows > 0) {
+    const int e = read_copy_error(ctx);
+    if (e)
+      throw Error(kErrCuda, "block copy: a bounded wait expired (code " + std::to_string(e) + ")");
+  }
+}
+
+int read_copy_error(Context* ctx) {
+  int e = 0;
+  MPSG_CUDA(cudaMemcpyAsync(&e, ctx->d_copy_err, sizeof(int), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  MPSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (e) MPSG_CUDA(cudaMemsetAsync(ctx->d_copy_err, 0, sizeof(int), ctx->stream));
+  return e;
 }
 
 }  // namespace mpsg

@@ -61,25 +61,32 @@ unsigned char* scratch_base(int device) {
 
 size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 
-// Places the tables of one copy plan in the staging image at `cur` and points the plan there.
+// Places the tables of one copy plan (warp-unit tasks, their prefix sums and launch data, and
+// the rows of the TMA-staged path) in the staging image at `cur` and points the plan there.
 void stage_copy(mpsg::DevCopyPlan& p, const std::vector<mpsg::CopyTask>& tasks, bool identity,
                 std::vector<unsigned char>& img, size_t& cur, unsigned char* dev) {
+  std::vector<mpsg::CopyTask> rest;
   std::vector<int64_t> prefix;
   std::vector<unsigned char> aux;
-  p.build_host(tasks, identity, prefix, aux);
-  if (p.ntasks == 0 || p.identity) return;
-  const size_t bt = sizeof(mpsg::CopyTask) * tasks.size();
+  std::vector<mpsg::BulkRow> rows;
+  p.build_host(tasks, identity, rest, prefix, aux, rows);
+  if (p.identity) return;
+  const size_t bt = sizeof(mpsg::CopyTask) * rest.size();
   const size_t bp = sizeof(int64_t) * prefix.size();
-  const size_t o1 = cur, o2 = align256(o1 + bt), o3 = align256(o2 + bp);
-  cur = align256(o3 + aux.size());
+  const size_t br = sizeof(mpsg::BulkRow) * rows.size();
+  const size_t o1 = cur, o2 = align256(o1 + bt), o3 = align256(o2 + bp),
+               o4 = align256(o3 + aux.size());
+  cur = align256(o4 + br);
   if (cur > kScratchBytes) return;  // reported by the caller's size check
   img.resize(cur);
-  std::memcpy(img.data() + o1, tasks.data(), bt);
+  if (bt) std::memcpy(img.data() + o1, rest.data(), bt);
   std::memcpy(img.data() + o2, prefix.data(), bp);
-  std::memcpy(img.data() + o3, aux.data(), aux.size());
+  if (!aux.empty()) std::memcpy(img.data() + o3, aux.data(), aux.size());
+  if (br) std::memcpy(img.data() + o4, rows.data(), br);
   p.d_tasks = (mpsg::CopyTask*)(dev + o1);
   p.d_prefix = (int64_t*)(dev + o2);
   p.d_aux = dev + o3;
+  p.d_rows = (mpsg::BulkRow*)(dev + o4);
 }
 
 bool same_structure(const mpsg::TensorMeta& x, const mpsg::TensorMeta& y) {

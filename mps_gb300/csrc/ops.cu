@@ -37,6 +37,8 @@ void context_init(Context* ctx, int device) {
   uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
   MPSG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
   MPSG_CUDA(cudaMalloc(&ctx->d_partials, sizeof(double) * (ctx->num_sms * 4 + 64)));
+  MPSG_CUDA(cudaMalloc(&ctx->d_copy_err, sizeof(int)));
+  MPSG_CUDA(cudaMemset(ctx->d_copy_err, 0, sizeof(int)));
   MPSG_CUDA(cudaMallocHost(&ctx->h_pinned, sizeof(double) * 64));
   const char* dbg = std::getenv("MPSG_DEBUG_SYNC");
   ctx->debug_sync = dbg && dbg[0] == '1';
@@ -102,6 +104,7 @@ Context::~Context() {
   if (copy_stream) cudaStreamDestroy(copy_stream);
   if (solver && solver_destroy) solver_destroy(solver);
   if (d_partials) cudaFree(d_partials);
+  if (d_copy_err) cudaFree(d_copy_err);
   if (h_pinned) cudaFreeHost(h_pinned);
   if (stream) cudaStreamDestroy(stream);
 }

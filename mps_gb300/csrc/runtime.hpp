@@ -12,6 +12,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "copy_decode.hpp"
 #include "planner.hpp"
 
 namespace mpsg {
@@ -47,22 +48,32 @@ struct DeviceTensor {
   double* data() const { return buf ? buf->ptr : nullptr; }
 };
 
-// Copy-task list on the device with per-task tile prefix sums.
+// Copy-task list on the device, in one of two forms. When nearly all elements sit in tasks
+// whose source and destination share a unit-stride axis of at least kBulkMinRow elements, every
+// task becomes rows of a table moved by the TMA-staged row kernel (the few other tasks as
+// strided rows along their destination's fastest axis). Otherwise every task keeps its unit
+// prefix sums and launch data for the warp-unit kernel.
+constexpr int kBulkMinRow = 32;    // shortest unit-stride row that counts as bulk (elements)
+constexpr int kBulkMaxRow = 512;   // longest row unit of the row kernel (elements)
 struct DevCopyPlan {
-  int ntasks = 0;
-  int64_t ntiles = 0;
+  int ntasks = 0;                // tasks of the warp-unit kernel
+  int64_t ntiles = 0;            // ... and their units
+  int64_t nrows = 0;             // rows of the TMA-staged kernel
   int64_t elems = 0;
   bool identity = false;
   bool has_tile = false;         // some task is a transpose staged through shared memory
   CopyTask* d_tasks = nullptr;
   int64_t* d_prefix = nullptr;   // ntasks+1 tile prefix
   void* d_aux = nullptr;         // per task: tile shape, axis roles, division constants
+  BulkRow* d_rows = nullptr;     // nrows rows of the TMA-staged path
   cudaStream_t stream = nullptr;  // tables are allocated and freed in this stream's order
   void upload(const std::vector<CopyTask>& tasks, bool identity_, cudaStream_t st);
-  // Host half of upload: tile prefix sums and per-task launch data; sets every field except the
-  // device pointers (used by callers that place the tables in memory they own).
-  void build_host(const std::vector<CopyTask>& tasks, bool identity_,
-                  std::vector<int64_t>& prefix, std::vector<unsigned char>& aux_bytes);
+  // Host half of upload: either the row table (`rows`, `rest` empty) or the warp-unit tasks
+  // (`rest` with their unit prefix sums and launch data); sets every field except the device
+  // pointers (used by callers that place the tables in memory they own).
+  void build_host(const std::vector<CopyTask>& tasks, bool identity_, std::vector<CopyTask>& rest,
+                  std::vector<int64_t>& prefix, std::vector<unsigned char>& aux_bytes,
+                  std::vector<BulkRow>& rows);
   void release();
 };
 size_t copy_aux_bytes();  // bytes of launch data per copy task
@@ -164,6 +175,7 @@ struct Context : std::enable_shared_from_this<Context> {
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   double* d_partials = nullptr;   // reduction partials (one per CTA of a reduction launch)
+  int* d_copy_err = nullptr;      // set by the TMA-staged copy kernel when a bounded wait expires
   double* h_pinned = nullptr;     // small pinned host scratch for scalar results
   PlanCache<DevContract> contract_cache;
   std::unordered_map<std::string, std::shared_ptr<DevReleg>> releg_cache;
@@ -239,6 +251,9 @@ void set_smem_limit_once(Context* ctx, std::once_flag (&flags)[kMaxDevices], Ker
 
 // ---- kernel launchers (kernels_*.cu) ----
 void launch_copy(Context* ctx, const DevCopyPlan& p, const double* src, double* dst);
+// Error code of the TMA-staged copy kernel since the last call (0 = none), then cleared;
+// synchronises the context's stream.
+int read_copy_error(Context* ctx);
 void launch_gemm_f64(Context* ctx, const DevGemmPlan& p, const double* A, const double* B,
                      double* C);
 void launch_fill(Context* ctx, double* x, int64_t n, double v);
