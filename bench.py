@@ -58,6 +58,10 @@ def parse(argv=None):
                    help="instead of the H_eff line: mixed-precision 2-site DMRG sweeps of the "
                         "J1 Heisenberg 6 x 24 cylinder at maxdim --sweep-chi (default 1024)")
     p.add_argument("--sweeps", type=int, default=2, help="sweeps of the --cylinder run")
+    p.add_argument("--compare-fp64", action="store_true",
+                   help="--cylinder: run the last sweep also as the FP64 drop-in (FP64 "
+                        "contractions, exact SVD) from the same state and report |dE| for every "
+                        "energy of that sweep")
     p.add_argument("--mpo-shared-prefixes", action="store_true",
                    help="--cylinder with the MPO whose open terms share channels (w = 20 "
                         "instead of 26)")
@@ -645,16 +649,37 @@ def run_cylinder(args):
     ctx.synchronize()
     t_init = time.perf_counter() - t0
     times, energies, matvecs = [], [], []
-    for _ in range(args.sweeps):
+    kw = dict(maxdim=chi, tol=1e-10, lanczostol=1e-7, krylovdim=4, krylovmaxiter=8)
+    compare = None
+    for k in range(args.sweeps):
+        saved = None
+        if args.compare_fp64 and k == args.sweeps - 1:  # the state the last sweep starts from
+            saved = ([mg.copy(A) for A in mps.As], [None if e is None else mg.copy(e) for e in env])
         stats = []
         ctx.synchronize()
         t0 = time.perf_counter()
-        es = gd.dmrg2sitesweep(mps, Ws, env, maxdim=chi, tol=1e-10, lanczostol=1e-7,
-                               krylovdim=4, krylovmaxiter=8, stats=stats, **SWEEP_MIXED)
+        es = gd.dmrg2sitesweep(mps, Ws, env, stats=stats, **kw, **SWEEP_MIXED)
         ctx.synchronize()
         times.append(time.perf_counter() - t0)
         energies.append(es[-1])
         matvecs.append(sum(i.numops for i in stats))
+        if saved is not None:
+            m64 = gd.MPState(saved[0], center=1)
+            e64_env = saved[1]
+            del saved
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            e64 = gd.dmrg2sitesweep(m64, Ws, e64_env, **kw, **SWEEP_FP64)
+            ctx.synchronize()
+            t64 = time.perf_counter() - t0
+            de = [abs(a - b) for a, b in zip(es, e64)]
+            compare = {"fp64_sweep_s": t64, "mixed_sweep_s": times[-1],
+                       "speedup_mixed_vs_fp64": t64 / times[-1],
+                       "energy_fp64": e64[-1], "energy_mixed": es[-1],
+                       "dE_final": de[-1], "dE_max_over_sweep": max(de),
+                       "dE_rel_max_over_sweep": max(de) / abs(e64[-1]),
+                       "energies_compared": len(de), "fp64_config": SWEEP_FP64}
+            del m64, e64_env
     line = {
         "metric": "DMRG sweep s, J1 Heisenberg 6x24 cylinder", "value": times[-1], "unit": "s",
         "higher_is_better": False, "n_gpus": 1, "data": "synthetic (seeded Philox initial MPS)",
@@ -664,6 +689,7 @@ def run_cylinder(args):
         "sweep_s": times, "energy_per_sweep": energies, "energy_per_site": energies[-1] / n,
         "matvecs_per_sweep": matvecs, "init_s": t_init,
         "max_mpo_bond": max(W.space[2].dim() for W in Ws),
+        **({"last_sweep_vs_fp64": compare} if compare else {}),
     }
     print(json.dumps(line), flush=True)
 

@@ -108,6 +108,30 @@ __global__ void top_eigpairs_kernel(double* __restrict__ X, double* __restrict__
   }
 }
 
+// S[i] = |Y[:, i]| (one warp per column, FP64), then S[i] = min(S[i], S[i-1]) over i (one
+// thread, after the norms): the singular values of A as the column norms of A^T U (or A V) for
+// the Gram eigenvectors U (V). Their absolute error is about eps * max(S), where sqrt of the
+// Gram eigenvalue is off by about eps * max(S)^2 / S for small values. The running minimum keeps
+// the order where round-off ties neighbouring values.
+__global__ void col_norms_kernel(const double* __restrict__ Y, double* __restrict__ S,
+                                 int64_t rows, int64_t k) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp; c < k; c += nwarps) {
+    const double* y = Y + c * rows;
+    double acc = 0.0;
+    for (int64_t r = lane; r < rows; r += 32) acc = fma(y[r], y[r], acc);
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) S[c] = sqrt(acc);
+  }
+}
+
+__global__ void running_min_kernel(double* __restrict__ S, int64_t k) {
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    for (int64_t i = 1; i < k; ++i) S[i] = fmin(S[i], S[i - 1]);
+}
+
 // X[:, i] /= S[i] (columns with S[i] == 0 become zero)
 __global__ void scale_cols_inv_kernel(double* __restrict__ X, const double* __restrict__ S,
                                       int64_t rows, int64_t k) {
@@ -315,6 +339,9 @@ void run_gram(Context* ctx, cudaStream_t st, cusolverDnHandle_t h, cublasHandle_
     MPSG_BLAS(cublasDgemm(bl, CUBLAS_OP_N, CUBLAS_OP_N, (int)M, (int)k, (int)N, &one, A, (int)M,
                           X, (int)N, &zero, Y, (int)M));
   const int64_t rows = left ? N : M;
+  col_norms_kernel<<<(unsigned)std::min<int64_t>((k + 7) / 8, 1184), 256, 0, st>>>(Y, B.S->ptr,
+                                                                                 rows, k);
+  running_min_kernel<<<1, 1, 0, st>>>(B.S->ptr, k);
   scale_cols_inv_kernel<<<grid_for(rows * k), 256, 0, st>>>(Y, B.S->ptr, rows, k);
   MPSG_CUDA(cudaGetLastError());
 }
@@ -405,7 +432,7 @@ SVDResult svd_blocks(Context* ctx, const DeviceTensor& A, bool truncate, int64_t
     else run_gram(ctx, L.st[lane], L.sol[lane], L.blas[lane], Ab, blocks[b],
                   method == kSvdGramLeft, dinfo + b);
   });
-  ctx->kernel_launches += (int64_t)nb * (method == kSvdExact ? 1 : 2);
+  ctx->kernel_launches += (int64_t)nb * (method == kSvdExact ? 1 : 4);
   std::vector<int> info(nb, 0);
   if (nb)
     MPSG_CUDA(cudaMemcpyAsync(info.data(), dinfo, sizeof(int) * nb, cudaMemcpyDeviceToHost,
