@@ -379,12 +379,14 @@ void launch_scale(Context* ctx, int64_t n, double a, const double* x, double* y)
   ctx->kernel_launches++;
 }
 
+int dots_grid(Context* ctx, int64_t nmax) { return std::min(vec_grid(ctx, nmax), 64); }
+
 void dots_host(Context* ctx, const std::vector<VecPair>& pairs, double* out) {
   const int np = (int)pairs.size();
   if (np == 0) return;
   int64_t nmax = 1;
   for (const VecPair& p : pairs) nmax = std::max(nmax, p.n);
-  const int g = std::min(vec_grid(ctx, nmax), 64);
+  const int g = dots_grid(ctx, nmax);
   cudaStream_t st = ctx->stream;
   VecPair* d_pairs = nullptr;
   double* d_part = nullptr;
@@ -421,6 +423,24 @@ void launch_lincomb(Context* ctx, int64_t n, const std::vector<const double*>& x
   ctx->kernel_launches++;
   MPSG_CUDA(cudaFreeAsync(d_xs, st));
   MPSG_CUDA(cudaFreeAsync(d_c, st));
+}
+
+void launch_dots_device(Context* ctx, const VecPair* d_pairs, int np, int64_t nmax,
+                        double* d_part, double* d_out) {
+  if (np == 0) return;
+  const int g = dots_grid(ctx, nmax);
+  dots_partial_kernel<<<dim3((unsigned)g, (unsigned)np), 256, 0, ctx->stream>>>(d_pairs, d_part);
+  dots_sum_kernel<<<(unsigned)np, 256, 0, ctx->stream>>>(g, d_part, d_out);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches += 2;
+}
+
+void launch_lincomb_device(Context* ctx, int64_t n, int m, const double* const* d_xs,
+                           const double* d_c, double* y) {
+  if (n == 0) return;
+  lincomb_kernel<<<vec_grid(ctx, n), 256, 0, ctx->stream>>>(n, m, d_xs, d_c, y);
+  MPSG_CUDA(cudaGetLastError());
+  ctx->kernel_launches++;
 }
 
 void launch_dot(Context* ctx, int64_t n, const double* x, const double* y, double* d_out) {

@@ -10,14 +10,17 @@
 //     (|t_0| <= 2^beta, |t_p| <= 2^(beta-1)); slice p stores t_p * 2^(e(i,c)-R(i)-beta(p+1)),
 //     exactly representable in bf16.  All of this is integer arithmetic on the FP64 bit
 //     pattern: GB300 executes FP64 at a small fraction of its FP32 rate.
-//   * MMA.  For every slice pair (p, q) with p + q < S, tcgen05.mma (M=128, N=64, K=16, bf16
-//     in, FP32 out) accumulates into TMEM accumulator g = p + q.  Within one chunk every product
-//     of group g is an integer multiple of one power of two and the sum stays below 2^24 units
-//     (chunk * 2^12 * max(4, g + 3) <= 2^24, exact_chunk), so the FP32 accumulation is exact.
-//   * Epilogue.  After each chunk the 4 epilogue warps drain the S accumulators (tcgen05.ld)
+//   * MMA.  For every slice pair (p, q) with p + q < S, tcgen05.mma (M=128, N=64 or 128, K=16,
+//     bf16 in, FP32 out) accumulates group g = p + q into a TMEM accumulator: its own for
+//     g <= S - 3, one shared by groups S - 2 and S - 1 (exact_accs).  Within one chunk every
+//     product of an exact group g is an integer multiple of one power of two and the sum stays
+//     below 2^24 units (chunk * 2^12 * max(4, g + 3) <= 2^24, exact_chunk), so its FP32
+//     accumulation is exact; the shared accumulator of the two smallest groups rounds at
+//     2^-24 of a sum weighted 2^(-7(S-2)), below the slicing error.
+//   * Epilogue.  After each chunk the epilogue warps drain the S - 1 accumulators (tcgen05.ld)
 //     into a double-single (hi, lo) FP32 pair per output element (TwoSum, exact up to 2^-48),
-//     release TMEM to the MMA warp (double-buffered), and after the last chunk assemble
-//     (hi + lo) * 2^(R(i) + C(j)) as an FP64 number with integer instructions only.
+//     release TMEM to the MMA warp (double-buffered where it fits), and after the last chunk
+//     assemble (hi + lo) * 2^(R(i) + C(j)) as an FP64 number with integer instructions only.
 //
 // Accuracy: slicing error <= 2^(-beta*S) relative to the row/column scale, so S = 2 is the
 // classic "bf16x3" (3 products), S = 3 gives about 21 bits (6 products), S = 4 about 28 bits,
@@ -483,20 +486,21 @@ __device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
 // Exact mode. The K step is 64 (128-byte swizzle) up to 3 slices; with 4..7 slices it is 32
 // (64-byte swizzle) so that a pipeline stage holding all S slices of both operands fits 2 to 4
 // times in shared memory. A chunk (the K range between exact FP32 flushes, exact_chunk) is a
-// multiple of 64.
-template <int S>
+// multiple of 64. BN (the N tile) is exact_bn(S) or 64.
+template <int S, int BN = exact_bn(S)>
 struct Cfg {
   static constexpr int kBK = S <= 3 ? 64 : 32;
   static constexpr int kPerRow = 64 / kBK;  // K steps per 64-wide packed row
   static constexpr int kPairs = S * (S + 1) / 2;
   static constexpr int kChunk = exact_chunk(S);
   static constexpr int kChunkSteps = kChunk / kBK;
-  static constexpr int kBN = exact_bn(S);
+  static constexpr int kBN = BN;
   static constexpr int kABytes = BM * kBK * 2;
   static constexpr int kBBytes = kBN * kBK * 2;
   static constexpr int kStageBytes = S * (kABytes + kBBytes);
   static constexpr int kStages = (220 * 1024) / kStageBytes > 4 ? 4 : (220 * 1024) / kStageBytes;
-  static constexpr int kAccCols = S * kBN;
+  static constexpr int kAccs = exact_accs(S);
+  static constexpr int kAccCols = kAccs * kBN;
   static constexpr int kBufs = (2 * kAccCols <= 512) ? 2 : 1;
   static constexpr int kTmemCols = (kBufs * kAccCols <= 128) ? 128
                                    : (kBufs * kAccCols <= 256) ? 256 : 512;
@@ -506,7 +510,7 @@ struct Cfg {
   static constexpr int kEpiCols = kBN * 4 / kEpiWarps;
   static constexpr int kThreads = 32 * (2 + kEpiWarps);
 };
-constexpr int kExactThreads = 576;  // Cfg<S>::kThreads (launch bound of the exact kernel)
+constexpr int kExactThreads = 576;  // Cfg<S, BN>::kThreads (launch bound of the exact kernel)
 
 // Static schedule shared by the three roles: the host sorts output tiles by decreasing K and the
 // CTAs deal them out in snake order (b, 2G-1-b, 2G+b, ...), which balances ragged sectors.
@@ -516,13 +520,13 @@ __device__ __forceinline__ int64_t sched_pos(int64_t i, int G, int b) {
 
 // 18 warps put 5 warps on one SM sub-partition (16K registers), which caps a thread at 96
 // registers; the epilogue drains TMEM in 16-column pieces to stay close to that
-template <int S>
+template <int S, int BN>
 __global__ void __launch_bounds__(kExactThreads, 1) split_gemm_kernel(
     const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
     const Problem* __restrict__ probs, const int4* __restrict__ tiles, int64_t ntiles,
     const int32_t* __restrict__ RA, const int32_t* __restrict__ CB, double* __restrict__ C,
     int* __restrict__ err) {
-  using CF = Cfg<S>;
+  using CF = Cfg<S, BN>;
   static_assert(CF::kThreads == kExactThreads, "launch bound and epilogue warp count disagree");
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -614,8 +618,8 @@ __global__ void __launch_bounds__(kExactThreads, 1) split_gemm_kernel(
             for (int pa = 0; pa < S; ++pa) {
 #pragma unroll
               for (int qb = 0; qb < S - pa; ++qb) {
-                const int g = pa + qb;
-                const uint32_t dcol = tmem_base + (uint32_t)((buf * S + g) * CF::kBN);
+                const int g = pa + qb < CF::kAccs ? pa + qb : CF::kAccs - 1;  // accumulator
+                const uint32_t dcol = tmem_base + (uint32_t)((buf * CF::kAccs + g) * CF::kBN);
                 const uint64_t ad = CF::kBK == 64 ? sw128_desc(sA + pa * CF::kABytes)
                                                   : sw64_desc(sA + pa * CF::kABytes);
                 const uint64_t bd = CF::kBK == 64 ? sw128_desc(sB + qb * CF::kBBytes)
@@ -678,9 +682,11 @@ __global__ void __launch_bounds__(kExactThreads, 1) split_gemm_kernel(
 #pragma unroll
         for (int h = 0; h < NC / 16; ++h) {  // 16-column pieces keep few registers live
 #pragma unroll
-          for (int g = 0; g < S; ++g) {
+          for (int g = 0; g < CF::kAccs; ++g) {
             uint32_t v[16];
-            tmem_ld16(tmem_base + lane_addr + (uint32_t)((buf * S + g) * CF::kBN + col0 + h * 16), v);
+            tmem_ld16(tmem_base + lane_addr +
+                          (uint32_t)((buf * CF::kAccs + g) * CF::kBN + col0 + h * 16),
+                      v);
 #pragma unroll
             for (int j = 0; j < 16; ++j) two_sum_acc(hi[h * 16 + j], lo[h * 16 + j], __uint_as_float(v[j]));
           }
@@ -974,14 +980,19 @@ size_t DevGemmPlan::device_bytes() const {
 
 namespace split {
 
-void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
+void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_, Tuning tune) {
   release();
   S = S_;
   if (S < 2 || S > kMaxSlices)
     throw Error(kErrUnsupported, "split precision supports 2..7 slices");
   const char* ex = std::getenv("MPSG_SPLIT_EXACT");
   fast = S <= 3 && !(ex && ex[0] == '1');
-  bn = fast ? BNF : exact_bn(S);
+  if (tune.bn != 0 && tune.bn != 64 && tune.bn != exact_bn(S))
+    throw Error(kErrArgument, "split GEMM N tile must be 64 or " + std::to_string(exact_bn(S)));
+  if (tune.order != kOrderK && tune.order != kOrderProblem)
+    throw Error(kErrArgument, "unknown split GEMM tile order");
+  bn = fast ? BNF : (tune.bn ? tune.bn : exact_bn(S));
+  order = tune.order;
   chunk = fast ? (1 << 30) : chunk_for(S);
   seg = fast ? 256 : chunk;
   probs.clear();
@@ -1031,13 +1042,15 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_) {
   }
   nprob = (int)probs.size();
   ntiles = tile_prefix.back();
-  // output tiles ordered by decreasing K (ties: problem, then M tile) for the snake schedule
+  // output tiles problem by problem (N tile, then M tile), for the snake schedule by decreasing
+  // K (ties keep that order) unless the tuning asks for the problem order
   std::vector<int4> tl;
   tl.reserve(ntiles);
   for (int p = 0; p < nprob; ++p)
     for (int ni = 0; ni < probs[p].nt; ++ni)
       for (int mi = 0; mi < probs[p].mt; ++mi) tl.push_back(make_int4(p, mi, ni, probs[p].nks));
-  std::stable_sort(tl.begin(), tl.end(), [](const int4& a, const int4& b) { return a.w > b.w; });
+  if (order == kOrderK)
+    std::stable_sort(tl.begin(), tl.end(), [](const int4& a, const int4& b) { return a.w > b.w; });
   tilesA = tA;
   tilesB = tB;
   rowsA = tA * BM;
@@ -1099,11 +1112,34 @@ void SplitPlan::release() {
   nprob = 0;
 }
 
+// The exact kernel at N tile BN (the fast kernel when the plan is in fast mode).
+template <int S, int BN>
+static void launch_gemm_t(Context* ctx, SplitPlan& sp, double* C) {
+  using CF = Cfg<S, BN>;
+  using FCF = FastCfg<S <= 3 ? S : 3>;
+  // per device, slice count and N tile (one flag array per instantiation of this launcher)
+  static std::once_flag exact_set[kMaxDevices], fast_set[kMaxDevices];
+  if (sp.fast)
+    set_smem_limit_once(ctx, fast_set, split_gemm_fast_kernel<S <= 3 ? S : 3>,
+                        (int)FCF::kSmemBytes);
+  else
+    set_smem_limit_once(ctx, exact_set, split_gemm_kernel<S, BN>, (int)CF::kSmemBytes);
+  const int grid = (int)std::min<int64_t>(sp.ntiles, (int64_t)ctx->num_sms);
+  KernelTimer timer(ctx, kKindGemmSplit, sp.flops);
+  if (sp.fast) {
+    if (S > 3) throw Error(kErrUnsupported, "fast split mode needs S <= 3");
+    split_gemm_fast_kernel<S <= 3 ? S : 3><<<grid, 192, FCF::kSmemBytes, ctx->stream>>>(
+        sp.tmA, sp.tmB, sp.d_probs, sp.d_tiles, sp.ntiles, sp.d_RA, sp.d_CB, C, sp.d_err);
+  } else {
+    split_gemm_kernel<S, BN><<<grid, CF::kThreads, CF::kSmemBytes, ctx->stream>>>(
+        sp.tmA, sp.tmB, sp.d_probs, sp.d_tiles, sp.ntiles, sp.d_RA, sp.d_CB, C, sp.d_err);
+  }
+  MPSG_CUDA(cudaGetLastError());
+}
+
 template <int S>
 static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double* B, double* C,
                      int what) {
-  using CF = Cfg<S>;
-  using FCF = FastCfg<S <= 3 ? S : 3>;
   const int chunk = sp.chunk;
   for (int side = 0; side < 2; ++side) {
     if (!(what & (side ? kPackB : kPackA))) continue;
@@ -1137,24 +1173,10 @@ static void launch_t(Context* ctx, SplitPlan& sp, const double* A, const double*
     }
   }
   if (!(what & kRunGemm)) return;
-  // per device and slice count (one flag array per instantiation of this launcher)
-  static std::once_flag exact_set[kMaxDevices], fast_set[kMaxDevices];
-  if (sp.fast)
-    set_smem_limit_once(ctx, fast_set, split_gemm_fast_kernel<S <= 3 ? S : 3>,
-                        (int)FCF::kSmemBytes);
+  if (!sp.fast && sp.bn == 64 && exact_bn(S) != 64)
+    launch_gemm_t<S, 64>(ctx, sp, C);
   else
-    set_smem_limit_once(ctx, exact_set, split_gemm_kernel<S>, (int)CF::kSmemBytes);
-  const int grid = (int)std::min<int64_t>(sp.ntiles, (int64_t)ctx->num_sms);
-  KernelTimer timer(ctx, kKindGemmSplit, sp.flops);
-  if (sp.fast) {
-    if (S > 3) throw Error(kErrUnsupported, "fast split mode needs S <= 3");
-    split_gemm_fast_kernel<S <= 3 ? S : 3><<<grid, 192, FCF::kSmemBytes, ctx->stream>>>(
-        sp.tmA, sp.tmB, sp.d_probs, sp.d_tiles, sp.ntiles, sp.d_RA, sp.d_CB, C, sp.d_err);
-  } else {
-    split_gemm_kernel<S><<<grid, CF::kThreads, CF::kSmemBytes, ctx->stream>>>(
-        sp.tmA, sp.tmB, sp.d_probs, sp.d_tiles, sp.ntiles, sp.d_RA, sp.d_CB, C, sp.d_err);
-  }
-  MPSG_CUDA(cudaGetLastError());
+    launch_gemm_t<S, exact_bn(S)>(ctx, sp, C);
   ctx->kernel_launches++;
   ctx->gemm_flops += sp.flops;
   if (ctx->debug_sync) {

@@ -271,5 +271,13 @@ void dots_host(Context* ctx, const std::vector<VecPair>& pairs, double* out);
 // y = sum_i c[i] xs[i] (elementwise, n elements; y may alias an operand)
 void launch_lincomb(Context* ctx, int64_t n, const std::vector<const double*>& xs,
                     const std::vector<double>& c, double* y);
+// The same two operations with every table in device memory and no host synchronisation:
+// d_out[i] = dot(pairs[i]) (d_part holds np * dots_grid(ctx, nmax) partial sums, nmax = the
+// longest pair), and y = sum_i d_c[i] d_xs[i] over m operands.
+int dots_grid(Context* ctx, int64_t nmax);
+void launch_dots_device(Context* ctx, const VecPair* d_pairs, int np, int64_t nmax,
+                        double* d_part, double* d_out);
+void launch_lincomb_device(Context* ctx, int64_t n, int m, const double* const* d_xs,
+                           const double* d_c, double* y);
 
 }  // namespace mpsg

@@ -12,15 +12,35 @@ constexpr int BM = 128, BN = 64, BK = 64;
 constexpr int kSliceBits = 7;  // beta: bits per bf16 slice digit
 constexpr int kMaxSlices = 7;  // 49 bits: the FP64-class setting
 
-// K chunk of the exact mode: the longest K range whose group sums stay exact FP32 integers.
-// Balanced digits satisfy |t_0| <= 2^7 and |t_p| <= 2^6 (p >= 1), so one K index adds at most
-// 2^14 to group 0 and 2 * 2^13 + (g - 1) * 2^12 = 2^12 (g + 3) to group g >= 1; with g <= S-1
-// the chunk is 2^24 / (2^12 max(4, S + 2)), rounded down to a multiple of 64 (one packed row).
-constexpr int exact_chunk(int S) { return ((4096 / (S + 2 > 4 ? S + 2 : 4)) / 64) * 64; }
+// Accumulators of the exact mode. The products of slice pair (p, q) form group g = p + q, of
+// relative weight 2^(-7 g). Groups g <= S - 3 keep one accumulator each, summed exactly within a
+// chunk; the two smallest groups (S - 2 and S - 1) share one FP32 accumulator. Its rounding
+// (2^-24 of a sum of weight 2^(-7(S-2))) stays about 2^-10 below the 2^(-7 S) slicing error
+// even after a few thousand K indices, and it frees one accumulator of TMEM per tile.
+constexpr int exact_accs(int S) { return S >= 2 ? S - 1 : 1; }
 
-// N tile of the exact mode: S accumulators of exact_bn columns must fit the 512 TMEM columns;
-// 128-column MMAs halve the shared-memory operand traffic per MAC of 64-column ones.
-constexpr int exact_bn(int S) { return S <= 4 ? 128 : 64; }
+// K chunk of the exact mode: the longest K range whose exact group sums stay FP32 integers.
+// Balanced digits satisfy |t_0| <= 2^7 and |t_p| <= 2^6 (p >= 1), so one K index adds at most
+// 2^14 to group 0 and 2 * 2^13 + (g - 1) * 2^12 = 2^12 (g + 3) to group g >= 1; with exact
+// groups g <= S - 3 the chunk is 2^24 / (2^12 max(4, S)), rounded down to a multiple of 64 (one
+// packed row): 1024 up to S = 4, 576 at S = 7.
+constexpr int exact_chunk(int S) { return ((4096 / (S > 4 ? S : 4)) / 64) * 64; }
+
+// N tile of the exact mode: exact_accs(S) accumulators of exact_bn columns must fit the 512
+// TMEM columns; 128-column MMAs halve the shared-memory operand traffic per MAC of 64-column
+// ones.
+constexpr int exact_bn(int S) { return exact_accs(S) * 128 <= 512 ? 128 : 64; }
+
+// Kernel configuration of one grouped GEMM, chosen by the tuner (batch.cu) or left at the
+// defaults: the N tile of the exact mode (0 = exact_bn(S); else 64 or exact_bn(S)), and the
+// order in which output tiles are dealt to the persistent CTAs (kOrderK: decreasing K, which
+// balances ragged sectors; kOrderProblem: problem by problem, N tile by N tile, which keeps the
+// CTAs of one wave on the same operands).
+enum { kOrderK = 0, kOrderProblem = 1 };
+struct Tuning {
+  int bn = 0;
+  int order = kOrderK;
+};
 
 // One sector GEMM as the split kernels see it (column-major A: M x K, B: K x N, C: M x N).
 struct Problem {
@@ -38,6 +58,7 @@ struct SplitPlan {
   cudaStream_t stream = nullptr;  // storage is allocated and freed in this stream's order
   bool fast = false;   // one FP32 accumulator, 128 x 256 tiles (S <= 3); else exact chunked mode
   int bn = 64;         // rows of a packed B tile = N of an output tile
+  int order = kOrderK; // output tile order (Tuning)
   int chunk = 0;       // K columns per exact chunk (whole K in fast mode)
   int seg = 0;         // K columns per exponent-pass work item
   int nprob = 0;
@@ -55,7 +76,7 @@ struct SplitPlan {
   int4* d_tiles = nullptr;  // output tiles (problem, M tile, N tile, K steps), descending K
   alignas(64) CUtensorMap tmA;
   alignas(64) CUtensorMap tmB;
-  void build(Context* ctx, const std::vector<GemmTask>& g, int S);
+  void build(Context* ctx, const std::vector<GemmTask>& g, int S, Tuning t = Tuning());
   void release();
   ~SplitPlan() { release(); }
 };
