@@ -277,6 +277,39 @@ int mpsg_heff2_flops(const mpsg_heff* op, double* flops);
  * pass 8 read + 2 S written per element); 0 for precision 0. For HBM rooflines of those kernels. */
 int mpsg_heff2_traffic(const mpsg_heff* op, double* copy_bytes, double* pack_bytes);
 int mpsg_heff2_free(mpsg_heff* op);
+
+/* ---- many independent chains at once (no counterpart in the reference, which runs one DMRG
+ * chain per process: src/dmrg.jl:58-179) --------------------------------------------------- */
+/* The two-site H_eff of n chains (any structures, one slice count `precision` = 2..7) prepared
+ * together: every phase of an application (block copies, operand packing, the two sector-GEMM
+ * stages) is one launch over all chains, the split GEMMs one persistent grouped launch each
+ * over every chain's sector problems. Kernel tile shape and tile order come from the tuner
+ * (mpsg_ctx_tuner; on unless MPSG_AUTOTUNE=0). With use_graph != 0 the application is captured
+ * in a CUDA graph at its second use and replayed after that. */
+typedef struct mpsg_heff_batch mpsg_heff_batch;
+int mpsg_heff2_batch_create(mpsg_ctx* ctx, int32_t n, const mpsg_tensor* const* v_like,
+                            const mpsg_tensor* const* envl, const mpsg_tensor* const* envr,
+                            const mpsg_tensor* const* w1, const mpsg_tensor* const* w2,
+                            int32_t precision, int32_t use_graph, mpsg_heff_batch** out);
+/* out[i] = H_eff_i(v[i]) for every chain, in one batched application. */
+int mpsg_heff2_batch_apply(mpsg_heff_batch* b, const mpsg_tensor* const* v, mpsg_tensor** out);
+/* mpsg_eigsolve_heff2 for every chain from x0[i] (at most 128 chains), the Lanczos recurrences
+ * run in lock step: one batched application per Krylov step and a fixed number of launches
+ * for all chains' vector updates. Outputs are arrays of n (normres .. converged may be NULL). */
+int mpsg_heff2_batch_eigsolve(mpsg_heff_batch* b, const mpsg_tensor* const* x0, int32_t krylovdim,
+                              int32_t maxiter, double tol, double* eigenvalues,
+                              mpsg_tensor** eigenvectors, double* normres, int32_t* numiter,
+                              int32_t* numops, int32_t* converged);
+/* Reference 4-step flops of one batched application, kernels per graph replay (0 before the
+ * graph exists), applications so far, and the tuned configuration tuning[4] = (N tile, tile
+ * order) of the first and of the second GEMM stage (N tile 0 = the kernel's default). */
+int mpsg_heff2_batch_info(const mpsg_heff_batch* b, double* ref_flops, int64_t* graph_kernels,
+                          int64_t* applies, int32_t* tuning);
+int mpsg_heff2_batch_free(mpsg_heff_batch* b);
+/* Split-GEMM tuner of the context: enable = 1 / 0 switches tuning of single prepared operators
+ * on / off (-1 leaves it); runs = shape classes timed so far, hits = choices served from the
+ * context's table. */
+int mpsg_ctx_tuner(mpsg_ctx* ctx, int32_t enable, int64_t* runs, int64_t* hits);
 /* Host self-check of the tensor-core H_eff plans for these structures (any tensors, also
  * structure-only ones): every copy and GEMM window in bounds, every output element written
  * once, and the composed intermediate copy equal to the two-step copy. */

@@ -111,6 +111,12 @@ SIGNATURES = {
     "mpsg_heff2_flops": [P, PF64],
     "mpsg_heff2_free": [P],
     "mpsg_plan_heff2_check": [P, P, P, P, P],
+    "mpsg_heff2_batch_create": [P, I32, PP, PP, PP, PP, PP, I32, I32, PP],
+    "mpsg_heff2_batch_apply": [P, PP, PP],
+    "mpsg_heff2_batch_eigsolve": [P, PP, I32, I32, F64, PF64, PP, PF64, PI32, PI32, PI32],
+    "mpsg_heff2_batch_info": [P, PF64, PI64, PI64, PI32],
+    "mpsg_heff2_batch_free": [P],
+    "mpsg_ctx_tuner": [P, I32, PI64, PI64],
     "mpsg_meta_create": [I32, I32, PI32, PI32, PI64, PI32, PP],
     "mpsg_plan_permutelegs": [P, PI32, PP],
     "mpsg_plan_fuselegs": [P, I32, I32, I32, PP],

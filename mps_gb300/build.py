@@ -22,7 +22,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmpsgb300.so")
 
 SOURCES = ["planner.cpp", "ops.cu", "capi.cu", "kernels_copy.cu", "kernels_f64.cu", "linalg.cu",
-           "krylov.cu", "kernels_split.cu", "noalloc.cu"]
+           "krylov.cu", "kernels_split.cu", "noalloc.cu", "batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr", "-I", CSRC]

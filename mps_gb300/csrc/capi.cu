@@ -4,6 +4,7 @@
 #include <sstream>
 
 #include "capi_internal.hpp"
+#include "batch.hpp"
 #include "linalg.hpp"
 
 namespace {
@@ -744,6 +745,123 @@ int mpsg_heff2_traffic(const mpsg_heff* op, double* copy_bytes, double* pack_byt
 
 int mpsg_heff2_free(mpsg_heff* op) {
   return guarded([&] { delete op; });
+}
+
+struct mpsg_heff_batch {
+  std::shared_ptr<mpsg::Context> owner;  // the batch's buffers hold it too
+  std::unique_ptr<mpsg::HeffBatch> b;
+};
+
+int mpsg_heff2_batch_create(mpsg_ctx* ctx, int32_t n, const mpsg_tensor* const* v_like,
+                            const mpsg_tensor* const* envl, const mpsg_tensor* const* envr,
+                            const mpsg_tensor* const* w1, const mpsg_tensor* const* w2,
+                            int32_t precision, int32_t use_graph, mpsg_heff_batch** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(out, "out");
+    if (n < 1) throw mpsg::Error(mpsg::kErrArgument, "a batch needs at least one operator");
+    for (auto* p : {(const void*)v_like, (const void*)envl, (const void*)envr, (const void*)w1,
+                    (const void*)w2})
+      need(p, "operand list");
+    std::vector<mpsg::TensorMeta> vm;
+    std::vector<const mpsg::DeviceTensor*> L, R, A, B;
+    for (int i = 0; i < n; ++i) {
+      for (const mpsg_tensor* t : {v_like[i], envl[i], envr[i], w1[i], w2[i]}) need(t, "operand");
+      vm.push_back(v_like[i]->t.meta);
+      L.push_back(&envl[i]->t);
+      R.push_back(&envr[i]->t);
+      A.push_back(&w1[i]->t);
+      B.push_back(&w2[i]->t);
+    }
+    auto h = std::make_unique<mpsg_heff_batch>();
+    h->owner = ctx->owner;
+    h->b = mpsg::heff_batch_create(&ctx->c, vm, L, R, A, B, precision, use_graph != 0);
+    *out = h.release();
+  });
+}
+
+int mpsg_heff2_batch_apply(mpsg_heff_batch* b, const mpsg_tensor* const* v, mpsg_tensor** out) {
+  return guarded([&] {
+    need(b, "b");
+    need(v, "v");
+    need(out, "out");
+    mpsg::HeffBatch& B = *b->b;
+    mpsg::Context* c = B.ctx;
+    for (int i = 0; i < B.n; ++i) {
+      need(v[i], "v[i]");
+      if (v[i]->t.ctx != c) throw mpsg::Error(mpsg::kErrArgument, "batch: tensor of another context");
+      if (!mpsg::same_meta(v[i]->t.meta, B.vmeta[i]))
+        throw mpsg::Error(mpsg::kErrSpaceMismatch, "batch: tensor of another structure");
+    }
+    for (int i = 0; i < B.n; ++i)
+      MPSG_CUDA(cudaMemcpyAsync(B.vin->ptr + B.voff[i], v[i]->t.data(),
+                                sizeof(double) * B.vmeta[i].total, cudaMemcpyDeviceToDevice,
+                                c->stream));
+    B.apply();
+    for (int i = 0; i < B.n; ++i) {
+      mpsg::DeviceTensor t = mpsg::new_tensor(c, B.vmeta[i], false);
+      MPSG_CUDA(cudaMemcpyAsync(t.data(), B.vout->ptr + B.voff[i],
+                                sizeof(double) * B.vmeta[i].total, cudaMemcpyDeviceToDevice,
+                                c->stream));
+      out[i] = wrap(std::move(t));
+    }
+  });
+}
+
+int mpsg_heff2_batch_eigsolve(mpsg_heff_batch* b, const mpsg_tensor* const* x0, int32_t krylovdim,
+                              int32_t maxiter, double tol, double* eigenvalues,
+                              mpsg_tensor** eigenvectors, double* normres, int32_t* numiter,
+                              int32_t* numops, int32_t* converged) {
+  return guarded([&] {
+    need(b, "b");
+    need(x0, "x0");
+    need(eigenvalues, "eigenvalues");
+    need(eigenvectors, "eigenvectors");
+    std::vector<const mpsg::DeviceTensor*> xs;
+    for (int i = 0; i < b->b->n; ++i) {
+      need(x0[i], "x0[i]");
+      xs.push_back(&x0[i]->t);
+    }
+    auto R = mpsg::eigsolve_heff2_batch(*b->b, xs, krylovdim, maxiter, tol);
+    for (int i = 0; i < b->b->n; ++i) {
+      eigenvalues[i] = R[i].value;
+      eigenvectors[i] = wrap(std::move(R[i].vec));
+      if (normres) normres[i] = R[i].normres;
+      if (numiter) numiter[i] = R[i].numiter;
+      if (numops) numops[i] = R[i].numops;
+      if (converged) converged[i] = R[i].converged ? 1 : 0;
+    }
+  });
+}
+
+int mpsg_heff2_batch_info(const mpsg_heff_batch* b, double* ref_flops, int64_t* graph_kernels,
+                          int64_t* applies, int32_t* tuning) {
+  return guarded([&] {
+    need(b, "b");
+    const mpsg::HeffBatch& B = *b->b;
+    if (ref_flops) *ref_flops = B.ref_flops;
+    if (graph_kernels) *graph_kernels = B.exec ? B.graph_kernels : 0;
+    if (applies) *applies = B.applies;
+    if (tuning) {
+      tuning[0] = B.t1.bn;
+      tuning[1] = B.t1.order;
+      tuning[2] = B.t2.bn;
+      tuning[3] = B.t2.order;
+    }
+  });
+}
+
+int mpsg_heff2_batch_free(mpsg_heff_batch* b) {
+  return guarded([&] { delete b; });
+}
+
+int mpsg_ctx_tuner(mpsg_ctx* ctx, int32_t enable, int64_t* runs, int64_t* hits) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    if (enable == 0 || enable == 1) ctx->c.autotune = enable != 0;
+    if (runs) *runs = ctx->c.tune_runs;
+    if (hits) *hits = ctx->c.tune_hits;
+  });
 }
 
 int mpsg_plan_heff2_check(const mpsg_tensor* v, const mpsg_tensor* envl, const mpsg_tensor* envr,

@@ -530,6 +530,87 @@ void check_heff_folded(const TensorMeta& v, const TensorMeta& envL, const Tensor
   if (!same_meta(F.c2->split.out, v)) throw Error(kErrSpaceMismatch, "folded H_eff changes v's structure");
 }
 
+HeffParts heff_parts(Context* ctx, const TensorMeta& vmeta, const DeviceTensor& envL,
+                     const DeviceTensor& envR, const DeviceTensor& W1, const DeviceTensor& W2,
+                     int precision) {
+  if (precision < 2 || precision > split::kMaxSlices)
+    throw Error(kErrUnsupported, "precision must be 0 (FP64) or 2..7 bf16 slices");
+  HeffParts H;
+  H.plw = get_contract_plan(ctx, envL.meta, kLW_A, W1.meta, kLW_B);
+  H.prw = get_contract_plan(ctx, W2.meta, kRW_A, envR.meta, kRW_B);
+  const TensorMeta& lwmeta = H.plw->host->split.out;
+  const TensorMeta& rwmeta = H.prw->host->split.out;
+  H.key = "H" + std::to_string(precision) + "|" + meta_key(vmeta) + "|" + meta_key(envL.meta) +
+          "|" + meta_key(envR.meta) + "|" + meta_key(W1.meta) + "|" + meta_key(W2.meta);
+  auto hit = ctx->heff_cache.find(H.key);
+  if (hit != ctx->heff_cache.end()) {  // take the idle plans of this structure
+    H.plans = hit->second;
+    ctx->heff_cache.erase(hit);
+    auto& lru = ctx->heff_lru;
+    lru.erase(std::find(lru.begin(), lru.end(), H.key));
+    ctx->heff_bytes -= H.plans->bytes;
+    return H;
+  }
+  auto P = std::make_shared<HeffPlans>();
+  P->c1 = private_contract_plan(ctx, lwmeta, kX_A, vmeta, kX_B);
+  P->c2 = private_contract_plan(ctx, P->c1->host->split.out, kO_A, rwmeta, kO_B);
+  const ContractPlan& h1 = *P->c1->host;
+  const ContractPlan& h2 = *P->c2->host;
+  std::vector<BlockMap> src_of_x, dst_of_x;
+  plan_split_permute_rec(h1.mm.out, h1.rlegs, h1.clegs, h1.perm, &src_of_x);
+  plan_symmatrix_rec(h1.split.out, h2.rowsA, h2.colsA, &dst_of_x);
+  P->x2a_host = compose_through(h1.split.out, src_of_x, dst_of_x);
+  P->x2a.upload(P->x2a_host, false, ctx->stream);
+  for (int side = 0; side < 2; ++side) {
+    const ContractPlan& f = side ? *H.prw->host : *H.plw->host;
+    std::vector<BlockMap> src, dst;
+    plan_split_permute_rec(f.mm.out, f.rlegs, f.clegs, f.perm, &src);
+    if (side)
+      plan_symmatrix_rec(f.split.out, h2.rowsB, h2.colsB, &dst);
+    else
+      plan_symmatrix_rec(f.split.out, h1.rowsA, h1.colsA, &dst);
+    (side ? P->rw2b : P->lw2a).upload(compose_through(f.split.out, src, dst), false, ctx->stream);
+  }
+  H.plans = P;
+  return H;
+}
+
+void heff_fold(Context* ctx, HeffParts& H, const DeviceTensor& envL, const DeviceTensor& envR,
+               const DeviceTensor& W1, const DeviceTensor& W2, double* dstA1, double* dstB2,
+               cudaEvent_t wait_left, cudaEvent_t wait_right) {
+  // the W folds (FP64): their fused GEMM outputs go straight into GEMM 1's A and GEMM 2's B
+  // operands through composed copies, so envLW and envRW are never materialised
+  if (wait_left) MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, wait_left, 0));
+  {
+    auto clw = contract_gemm(ctx, *H.plw, envL, W1, 0);
+    launch_copy(ctx, H.plans->lw2a, clw->ptr, dstA1);
+  }
+  if (wait_right) MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, wait_right, 0));
+  {
+    auto crw = contract_gemm(ctx, *H.prw, W2, envR, 0);
+    launch_copy(ctx, H.plans->rw2b, crw->ptr, dstB2);
+  }
+}
+
+void heff_plans_return(Context* ctx, const std::string& key, std::shared_ptr<HeffPlans> plans) {
+  if (!plans || key.empty() || !ctx) return;
+  // idle plans kept (device bytes): a share of 8 GiB per process
+  const size_t kBudget = cache_share(size_t(8) << 30);
+  if (ctx->heff_cache.count(key)) return;  // an idle copy exists already: drop this one
+  ctx->heff_cache[key] = plans;
+  ctx->heff_lru.push_back(key);
+  ctx->heff_bytes += plans->bytes;
+  while (ctx->heff_bytes > kBudget && !ctx->heff_lru.empty()) {
+    const std::string k = ctx->heff_lru.front();
+    ctx->heff_lru.erase(ctx->heff_lru.begin());
+    auto it = ctx->heff_cache.find(k);
+    if (it != ctx->heff_cache.end()) {
+      ctx->heff_bytes -= it->second->bytes;
+      ctx->heff_cache.erase(it);
+    }
+  }
+}
+
 std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const DeviceTensor& envL,
                                     const DeviceTensor& envR, const DeviceTensor& W1,
                                     const DeviceTensor& W2, int precision, cudaEvent_t wait_left,
@@ -546,71 +627,26 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
     op->W2 = W2;
     return op;
   }
-  if (precision < 2 || precision > split::kMaxSlices)
-    throw Error(kErrUnsupported, "precision must be 0 (FP64) or 2..7 bf16 slices");
-  // the W folds (FP64): their fused GEMM outputs go straight into GEMM 1's A and GEMM 2's B
-  // operands through composed copies, so envLW and envRW are never materialised
-  auto plw = get_contract_plan(ctx, envL.meta, kLW_A, W1.meta, kLW_B);
-  auto prw = get_contract_plan(ctx, W2.meta, kRW_A, envR.meta, kRW_B);
-  const TensorMeta& lwmeta = plw->host->split.out;
-  const TensorMeta& rwmeta = prw->host->split.out;
-  op->plan_key = "H" + std::to_string(precision) + "|" + meta_key(vmeta) + "|" +
-                 meta_key(envL.meta) + "|" + meta_key(envR.meta) + "|" + meta_key(W1.meta) +
-                 "|" + meta_key(W2.meta);
-  auto hit = ctx->heff_cache.find(op->plan_key);
-  if (hit != ctx->heff_cache.end()) {  // take the idle plans of this structure
-    op->plans = hit->second;
-    ctx->heff_cache.erase(hit);
-    auto& lru = ctx->heff_lru;
-    lru.erase(std::find(lru.begin(), lru.end(), op->plan_key));
-    ctx->heff_bytes -= op->plans->bytes;
-  } else {
-    auto P = std::make_shared<HeffPlans>();
-    P->c1 = private_contract_plan(ctx, lwmeta, kX_A, vmeta, kX_B);
-    P->c2 = private_contract_plan(ctx, P->c1->host->split.out, kO_A, rwmeta, kO_B);
-    const ContractPlan& h1 = *P->c1->host;
-    const ContractPlan& h2 = *P->c2->host;
-    std::vector<BlockMap> src_of_x, dst_of_x;
-    plan_split_permute_rec(h1.mm.out, h1.rlegs, h1.clegs, h1.perm, &src_of_x);
-    plan_symmatrix_rec(h1.split.out, h2.rowsA, h2.colsA, &dst_of_x);
-    P->x2a.upload(compose_through(h1.split.out, src_of_x, dst_of_x), false, ctx->stream);
-    for (int side = 0; side < 2; ++side) {
-      const ContractPlan& f = side ? *prw->host : *plw->host;
-      std::vector<BlockMap> src, dst;
-      plan_split_permute_rec(f.mm.out, f.rlegs, f.clegs, f.perm, &src);
-      if (side)
-        plan_symmatrix_rec(f.split.out, h2.rowsB, h2.colsB, &dst);
-      else
-        plan_symmatrix_rec(f.split.out, h1.rowsA, h1.colsA, &dst);
-      (side ? P->rw2b : P->lw2a).upload(compose_through(f.split.out, src, dst), false,
-                                        ctx->stream);
-    }
-    for (auto* c : {P->c1.get(), P->c2.get()}) {
-      auto& sp = c->mm.splitp[precision];
-      sp = std::make_shared<split::SplitPlan>();
-      sp->build(ctx, c->mm.host, precision);
-      P->bytes += (size_t)sp->S * (size_t)(sp->rowsA + sp->rowsB) * 128;
-    }
-    op->plans = P;
-  }
-  // constant operands: fuse once, slice once
+  HeffParts H = heff_parts(ctx, vmeta, envL, envR, W1, W2, precision);
+  op->plans = H.plans;
+  op->plan_key = H.key;
   DevContract& c1 = *op->plans->c1;
   DevContract& c2 = *op->plans->c2;
+  for (auto* c : {&c1, &c2}) {  // the split plans of this operator's own GEMMs (once per plans)
+    auto& sp = c->mm.splitp[precision];
+    if (sp) continue;
+    sp = std::make_shared<split::SplitPlan>();
+    sp->build(ctx, c->mm.host, precision, choose_tuning(ctx, c->mm.host, precision));
+    op->plans->bytes += (size_t)sp->S * (size_t)(sp->rowsA + sp->rowsB) * 128;
+  }
+  // constant operands: fuse once, slice once
   op->copy_bytes = 16.0 * (double)(c1.fb.elems + op->plans->x2a.elems + c2.split.elems);
   op->pack_bytes = (16.0 + 2.0 * precision) *
                    (double)(c1.host->fb.out.total + c2.host->fa.out.total);
-  if (wait_left) MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, wait_left, 0));
-  {
-    auto clw = contract_gemm(ctx, *plw, envL, W1, 0);
-    op->fusedA1 = alloc_buffer(ctx, c1.host->fa.out.total);
-    launch_copy(ctx, op->plans->lw2a, clw->ptr, op->fusedA1->ptr);
-  }
-  if (wait_right) MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, wait_right, 0));
-  {
-    auto crw = contract_gemm(ctx, *prw, W2, envR, 0);
-    op->fusedB2 = alloc_buffer(ctx, c2.host->fb.out.total);
-    launch_copy(ctx, op->plans->rw2b, crw->ptr, op->fusedB2->ptr);
-  }
+  op->fusedA1 = alloc_buffer(ctx, c1.host->fa.out.total);
+  op->fusedB2 = alloc_buffer(ctx, c2.host->fb.out.total);
+  heff_fold(ctx, H, envL, envR, W1, W2, op->fusedA1->ptr, op->fusedB2->ptr, wait_left,
+            wait_right);
   split::launch_split_gemm(ctx, *c1.mm.splitp[precision], op->fusedA1->ptr, nullptr, nullptr,
                            split::kPackA);
   split::launch_split_gemm(ctx, *c2.mm.splitp[precision], nullptr, op->fusedB2->ptr, nullptr,
@@ -622,24 +658,7 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
   return op;
 }
 
-HeffOp::~HeffOp() {
-  if (!plans || plan_key.empty() || !ctx) return;
-  // idle plans kept (device bytes): a share of 8 GiB per process
-  const size_t kBudget = cache_share(size_t(8) << 30);
-  if (ctx->heff_cache.count(plan_key)) return;  // an idle copy exists already: drop this one
-  ctx->heff_cache[plan_key] = plans;
-  ctx->heff_lru.push_back(plan_key);
-  ctx->heff_bytes += plans->bytes;
-  while (ctx->heff_bytes > kBudget && !ctx->heff_lru.empty()) {
-    const std::string k = ctx->heff_lru.front();
-    ctx->heff_lru.erase(ctx->heff_lru.begin());
-    auto it = ctx->heff_cache.find(k);
-    if (it != ctx->heff_cache.end()) {
-      ctx->heff_bytes -= it->second->bytes;
-      ctx->heff_cache.erase(it);
-    }
-  }
-}
+HeffOp::~HeffOp() { heff_plans_return(ctx, plan_key, plans); }
 
 DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v) {
   Context* ctx = op.ctx;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "runtime.hpp"
+#include "split.hpp"
 
 namespace mpsg {
 
@@ -60,6 +61,7 @@ double dot(Context* ctx, const DeviceTensor& a, const DeviceTensor& b);
 struct HeffPlans {
   std::shared_ptr<DevContract> c1, c2;
   DevCopyPlan x2a;                   // fused X of GEMM 1 -> fused A of GEMM 2 (X never built)
+  std::vector<CopyTask> x2a_host;    // its host task list (batched operators concatenate it)
   DevCopyPlan lw2a, rw2b;            // fold outputs -> GEMM 1's A / GEMM 2's B (composed)
   size_t bytes = 0;                  // device storage held, for the cache budget
   ~HeffPlans() {
@@ -100,6 +102,27 @@ FoldedHeffPlans plan_heff_folded(const TensorMeta& v, const TensorMeta& envL,
 // Host self-check of those plans (bounds, coverage, composition == two steps).
 void check_heff_folded(const TensorMeta& v, const TensorMeta& envL, const TensorMeta& envR,
                        const TensorMeta& W1, const TensorMeta& W2);
+// The structure-only parts of a W-folded H_eff at `precision` slices: its plans (taken from the
+// context's idle cache or built, without split-GEMM plans) and the two fold contractions.
+struct HeffParts {
+  std::shared_ptr<HeffPlans> plans;
+  std::string key;  // cache key of `plans`
+  std::shared_ptr<DevContract> plw, prw;
+};
+HeffParts heff_parts(Context* ctx, const TensorMeta& vmeta, const DeviceTensor& envL,
+                     const DeviceTensor& envR, const DeviceTensor& W1, const DeviceTensor& W2,
+                     int precision);
+// The W folds in FP64, written straight into GEMM 1's fused A (dstA1, c1 fa layout) and GEMM
+// 2's fused B (dstB2, c2 fb layout); each waits for its event first when one is given.
+void heff_fold(Context* ctx, HeffParts& H, const DeviceTensor& envL, const DeviceTensor& envR,
+               const DeviceTensor& W1, const DeviceTensor& W2, double* dstA1, double* dstB2,
+               cudaEvent_t wait_left = nullptr, cudaEvent_t wait_right = nullptr);
+// Hands idle plans back to the context's cache (LRU, a share of 8 GiB per process).
+void heff_plans_return(Context* ctx, const std::string& key, std::shared_ptr<HeffPlans> plans);
+// Split-GEMM kernel configuration for a task list at S slices: the tuner's cached choice for
+// this shape class, tuning it first when the context's autotuning is on (batch.cu), else the
+// defaults.
+split::Tuning choose_tuning(Context* ctx, const std::vector<GemmTask>& g, int S);
 // wait_left / wait_right: events the left / right W fold waits for (inputs still arriving)
 std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const DeviceTensor& envL,
                                     const DeviceTensor& envR, const DeviceTensor& W1,

@@ -190,6 +190,11 @@ struct Context : std::enable_shared_from_this<Context> {
   int64_t kernel_launches = 0;    // launches of this library's kernels
   bool debug_sync = false;        // MPSG_DEBUG_SYNC=1: synchronise and check after tensor-core GEMMs
   double gemm_flops = 0;          // algorithmic flops issued through block GEMMs
+  // split-GEMM tuner (batch.cu): when on, a new shape class of problem lists is timed over the
+  // kernel's N tiles and tile orders and the fastest (N tile, order) kept by class
+  bool autotune = false;
+  std::unordered_map<std::string, std::pair<int, int>> tune_cache;
+  int64_t tune_runs = 0, tune_hits = 0;
   void* solver = nullptr;         // cusolverDnHandle_t, created on first SVD
   void (*solver_destroy)(void*) = nullptr;
   // optional per-kernel-class event timing (see mpsg_ctx_set_timing)

@@ -365,15 +365,13 @@ class PhaseTimer:
         return t1
 
 
-def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stats=None,
-                   timing: PhaseTimer | None = None, **kw):
-    """``dmrg2sitesweep!`` (src/dmrg.jl:58-179): one left-to-right-to-left sweep on the GPU.
-    Returns the reference's energy list (3L-5 post-truncation energies; the right-to-left loop
-    pushes each energy twice, dmrg.jl:132,156). ``timing`` (a PhaseTimer) accumulates the wall
-    time of the eigensolves, truncations (svdtrunc), post-truncation energies and environment
-    updates."""
+def sweep_steps(mps: MPState, Ws, env, o: SweepOptions, timing: PhaseTimer | None = None):
+    """``dmrg2sitesweep!`` (src/dmrg.jl:58-179) as a generator: before each of the sweep's
+    eigensolves it yields ``(AA, l)`` (the two-site tensor and the 1-based bond; the operator is
+    that of env[l-1], env[l+2], Ws[l-1], Ws[l]) and takes the ground-state vector sent back.
+    Returns the energy list. ``dmrg2sitesweep`` answers each request with its own eigensolve;
+    a lock-step driver answers the requests of many chains with one batched eigensolve."""
     import time
-    o = opts or SweepOptions(**kw)
     tick = (lambda name, t0: timing(name, t0)) if timing else (lambda name, t0: t0)
     now = time.perf_counter
     lx = len(mps)
@@ -385,7 +383,7 @@ def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stat
     for l in range(1, lx - 1):
         _prefetch(env, l + 3)  # the right environment of the next bond
         AA = mg.contract(A, (1, 2, -1), mps.As[l], (-1, 3, 4), precision=0)
-        v = _eig(AA, env, Ws, l, o, stats)
+        v = yield AA, l
         t = tick("eigsolve", t)
         u, s, vt, AA, e, _ = _truncate_and_energy(v, AA, env, Ws, l, o, tick=timing)
         energies.append(e)
@@ -396,7 +394,7 @@ def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stat
         t = tick("environment", t)
     l = lx - 1
     AA = mg.contract(A, (1, 2, -1), mps.As[l], (-1, 3, 4), precision=0)
-    v = _eig(AA, env, Ws, l, o, stats)
+    v = yield AA, l
     t = tick("eigsolve", t)
     e = None
     for l in range(lx - 1, 1, -1):
@@ -410,7 +408,7 @@ def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stat
         A = mg.splitleg(mg.matmul(u, s, precision=0), 1, AA.space[0:2])
         t = tick("environment", t)
         AA = mg.contract(mps.As[l - 2], (1, 2, -1), A, (-1, 3, 4), precision=0)
-        v = _eig(AA, env, Ws, l - 1, o, stats)
+        v = yield AA, l - 1
         t = tick("eigsolve", t)
         energies.append(e)
     l = 1
@@ -422,6 +420,23 @@ def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stat
     mps.As[0] = mg.splitleg(mg.matmul(u, s, precision=0), 1, AA.space[0:2])
     tick("environment", t)
     return energies
+
+
+def dmrg2sitesweep(mps: MPState, Ws, env, opts: SweepOptions | None = None, stats=None,
+                   timing: PhaseTimer | None = None, **kw):
+    """``dmrg2sitesweep!`` (src/dmrg.jl:58-179): one left-to-right-to-left sweep on the GPU.
+    Returns the reference's energy list (3L-5 post-truncation energies; the right-to-left loop
+    pushes each energy twice, dmrg.jl:132,156). ``timing`` (a PhaseTimer) accumulates the wall
+    time of the eigensolves, truncations (svdtrunc), post-truncation energies and environment
+    updates."""
+    o = opts or SweepOptions(**kw)
+    gen = sweep_steps(mps, Ws, env, o, timing)
+    try:
+        AA, l = next(gen)
+        while True:
+            AA, l = gen.send(_eig(AA, env, Ws, l, o, stats))
+    except StopIteration as stop:
+        return stop.value
 
 
 HEFF_STEPS = (((-1, 2, 1), (-1, 3, 4, 5)), ((1, -1, -2, 4, 5), (-1, 2, 3, -2)),
@@ -486,4 +501,69 @@ def run_chains(specs, nsweeps: int, opts: SweepOptions, threads: int | None = No
 
     with ThreadPoolExecutor(max_workers=max(1, threads or len(specs))) as ex:
         list(ex.map(work, range(len(specs))))
+    return results
+
+
+def _chain_sweeps(mps, Ws, env, o, nsweeps):
+    es = None
+    for _ in range(nsweeps):
+        es = yield from sweep_steps(mps, Ws, env, o)
+    return es
+
+
+def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, ctx=None, seed: int = 7,
+                        graph: bool = True, stats=None, max_batch: int = 128):
+    """2-site DMRG on independent chains (L, Delta, maxdim) in lock step on ONE context: every
+    chain's sweep runs as a ``sweep_steps`` generator, and at each step the eigensolve requests
+    of all chains still sweeping are answered by one batched Lanczos (``HeffBatch``): one
+    grouped application per Krylov step for all chains (CUDA graph replay; split GEMMs with
+    tuned tiles), FP64 recurrences. Truncations and environment updates run chain by chain.
+    Same start states as ``run_chains`` (Philox seed + index). Returns the last
+    post-truncation energy of each chain; ``stats`` (a dict) collects batch counts, the chain
+    count per batch and the tuner's runs and hits."""
+    ctx = ctx or mg.get_context(0)
+    if opts.precision < 2:
+        raise ValueError("the lock-step driver batches the split-precision Krylov matvecs: "
+                         "precision >= 2")
+    chains, gens, pending = [], [], {}
+    for i, (L, delta, chi) in enumerate(specs):
+        Ws = xxz_u1mpo(L, delta, ctx=ctx)
+        mps = mps_from_host(binomial_mps_host(L, L // 2, chi, seed + i), ctx)
+        center_at(mps, 1, svd=opts.svd, normalize=True)
+        env = initialenv(mps, Ws)
+        o = SweepOptions(**{**opts.__dict__, "maxdim": chi})
+        chains.append((mps, Ws, env, o))
+        g = _chain_sweeps(mps, Ws, env, o, nsweeps)
+        gens.append(g)
+        pending[i] = next(g)
+    results = [None] * len(specs)
+    nbatches, sizes = 0, []
+    while pending:
+        ids = sorted(pending)
+        answers = {}
+        for k in range(0, len(ids), max_batch):
+            part = ids[k:k + max_batch]
+            ops, x0s = [], []
+            for i in part:
+                AA, l = pending[i]
+                _, Ws, env, _ = chains[i]
+                ops.append((AA, env[l - 1], env[l + 2], Ws[l - 1], Ws[l]))
+                x0s.append(AA)
+            B = mg.HeffBatch(ops, precision=opts.precision, graph=graph)
+            _, vecs, _ = B.eigsolve(x0s, krylovdim=opts.krylovdim, maxiter=opts.krylovmaxiter,
+                                    tol=opts.lanczostol)
+            del B
+            nbatches += 1
+            sizes.append(len(part))
+            answers.update(zip(part, vecs))
+        for i in ids:
+            try:
+                pending[i] = gens[i].send(answers[i])
+            except StopIteration as stop:
+                results[i] = stop.value[-1]
+                del pending[i]
+    if stats is not None:
+        runs, hits = mg.tuner(ctx)
+        stats.update({"batches": nbatches, "chains_per_batch": sizes, "tuner_runs": runs,
+                      "tuner_hits": hits})
     return results

@@ -27,7 +27,7 @@ __all__ = [
     "mpsupdateleft",
     "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision", "_svd_",
     "svdtrunc", "svd_complex", "dots", "lincomb", "truncatedsizes", "small_eigh",
-    "eigsolve_heff2", "EigInfo", "Heff2", "HostBuffer", "Copy", "download_async",
+    "eigsolve_heff2", "EigInfo", "Heff2", "HeffBatch", "tuner", "HostBuffer", "Copy", "download_async",
     "upload_async", "device_checks", "checked_library",
 ]
 
@@ -809,6 +809,82 @@ class EigInfo:
     def __repr__(self):
         return (f"EigInfo(normres={self.normres:.3e}, numiter={self.numiter}, "
                 f"numops={self.numops}, converged={self.converged})")
+
+
+def _handles(ts):
+    return (C.c_void_p * max(1, len(ts)))(*[t.handle for t in ts])
+
+
+class HeffBatch:
+    """The two-site H_eff of many independent chains prepared together (no counterpart in the
+    reference, which runs one chain per process): ``ops[i] = (v_like, envL, envR, W1, W2)`` of
+    chain i, any structures, one split precision S = 2..7. Every phase of an application is one
+    launch over all chains (the split GEMMs one persistent grouped launch each, tile shape and
+    order from the tuner), captured in a CUDA graph at its second use when ``graph``."""
+
+    def __init__(self, ops, precision=4, graph=True):
+        ops = list(ops)
+        if not ops:
+            raise MPSGError(_lib.ERR_ARGUMENT, "a batch needs at least one operator")
+        self.ctx = ops[0][0].ctx
+        self.n = len(ops)
+        cols = [_handles([o[k] for o in ops]) for k in range(5)]
+        h = C.c_void_p()
+        call("mpsg_heff2_batch_create", self.ctx.handle, self.n, *cols, int(precision),
+             int(bool(graph)), C.byref(h))
+        self._h = h
+        self._free = _lib.lib.mpsg_heff2_batch_free
+
+    def __call__(self, vs):
+        """[H_eff_i(v_i)] in one batched application."""
+        vs = list(vs)
+        if len(vs) != self.n:
+            raise MPSGError(_lib.ERR_ARGUMENT, "one tensor per chain")
+        out = (C.c_void_p * self.n)()
+        call("mpsg_heff2_batch_apply", self._h, _handles(vs), out)
+        return [SymTensor(C.c_void_p(h), self.ctx) for h in out]
+
+    def eigsolve(self, x0s, krylovdim=5, maxiter=8, tol=1e-7):
+        """``eigsolve_heff2`` of every chain, the Lanczos recurrences in lock step: returns
+        (eigenvalues, eigenvectors, infos)."""
+        x0s = list(x0s)
+        if len(x0s) != self.n:
+            raise MPSGError(_lib.ERR_ARGUMENT, "one start vector per chain")
+        n = self.n
+        ev = (C.c_double * n)()
+        vecs = (C.c_void_p * n)()
+        nr = (C.c_double * n)()
+        ni, no, cv = (C.c_int32 * n)(), (C.c_int32 * n)(), (C.c_int32 * n)()
+        call("mpsg_heff2_batch_eigsolve", self._h, _handles(x0s), int(krylovdim), int(maxiter),
+             float(tol), ev, vecs, nr, ni, no, cv)
+        return (list(ev), [SymTensor(C.c_void_p(h), self.ctx) for h in vecs],
+                [EigInfo(nr[i], ni[i], no[i], bool(cv[i])) for i in range(n)])
+
+    def info(self):
+        """dict: reference flops per application, kernels per graph replay (0 before the graph
+        exists), applications so far, tuned (N tile, order) of both GEMM stages."""
+        f, gk, ap = C.c_double(), C.c_int64(), C.c_int64()
+        t = (C.c_int32 * 4)()
+        call("mpsg_heff2_batch_info", self._h, C.byref(f), C.byref(gk), C.byref(ap), t)
+        return {"ref_flops": f.value, "graph_kernels": gk.value, "applies": ap.value,
+                "tuning": [(t[0], t[1]), (t[2], t[3])]}
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def tuner(ctx, enable=None):
+    """Split-GEMM tuner of a context: ``enable`` True / False switches tuning of single
+    prepared operators; returns (shape classes timed, choices served from the table)."""
+    r, h = C.c_int64(), C.c_int64()
+    call("mpsg_ctx_tuner", ctx.handle, -1 if enable is None else int(bool(enable)), C.byref(r),
+         C.byref(h))
+    return r.value, h.value
 
 
 def eigsolve_heff2(x0, envL, envR, W1, W2, krylovdim=5, maxiter=8, tol=1e-7, precision=None):
