@@ -74,6 +74,14 @@ def parse(argv=None):
                         "each, concurrently and one after the other")
     p.add_argument("--batched-concurrent-only", action="store_true",
                    help="--batched without the one-after-the-other comparison run")
+    p.add_argument("--lockstep", action="store_true",
+                   help="--batched: the chains in lock step on one context (one batched "
+                        "eigensolve per step: every Krylov application one grouped launch per "
+                        "phase for all chains, CUDA graph replay, tuned split-GEMM tiles), "
+                        "timed beside the concurrent and one-by-one runs")
+    p.add_argument("--fp64-check", type=int, default=0, metavar="K",
+                   help="--batched: also run the first K chains one by one as the FP64 drop-in "
+                        "and report |dE| of the batched energies against them")
     p.add_argument("--sweep-chi", type=int, default=None, help="maxdim of the sweep (default chi)")
     p.add_argument("--sweep-offload", type=int, default=0, metavar="W",
                    help="also run the mixed sweep with environments in a W-entry device window "
@@ -268,6 +276,10 @@ def run_reference(args):
 
 # ---------------------------------------------------------------------------------------------
 SWEEP_MIXED = dict(precision=4, energy_precision=7, env_precision=7, svd="gram")
+# Truncation tie band (both sweeps): singular values within 1e-9 of the largest count as equal
+# and the lowest sector keeps the state, so that SU(2) multiplets split by the maxdim cut are
+# split the same way whatever the rounding of the two factorisations
+SWEEP_TIEBAND = 1e-9
 SWEEP_FP64 = dict(precision=0, energy_precision=0, env_precision=0, svd="exact")
 
 
@@ -285,7 +297,8 @@ def sweep_bench(ctx, chi, lx=32, seed=7, phases=False, offload=0):
     m0 = gd.mps_from_host(gd.binomial_mps_host(lx, lx // 2, chi, seed), ctx)
     gd.center_at(m0, 1, svd="gram")
     env0 = gd.initialenv(m0, Ws)
-    kw = dict(maxdim=chi, tol=1e-10, lanczostol=1e-7, krylovdim=4, krylovmaxiter=8)
+    kw = dict(maxdim=chi, tol=1e-10, lanczostol=1e-7, krylovdim=4, krylovmaxiter=8,
+              tieband=SWEEP_TIEBAND)
     out = {}
     for name, cfg in (("fp64", SWEEP_FP64), ("mixed", SWEEP_MIXED)):
         mps = gd.MPState([mg.copy(A) for A in m0.As], center=1)
@@ -328,7 +341,8 @@ def sweep_bench(ctx, chi, lx=32, seed=7, phases=False, offload=0):
                 "GB_down": st.transfer.bytes_down / 1e9, "GB_up": st.transfer.bytes_up / 1e9}
     return {
         "workload": f"one 2-site DMRG sweep, Heisenberg chain L={lx} (J=1, OBC, Sz=0), "
-                    f"maxdim={chi}, cutoff 1e-10, Krylov dim 4, maxiter 8, tol 1e-7; initial "
+                    f"maxdim={chi}, cutoff 1e-10, tie band {SWEEP_TIEBAND:g}, Krylov dim 4, "
+                    f"maxiter 8, tol 1e-7; initial "
                     f"MPS: N(0,1) blocks (Philox seed {seed}), binomial bond profile ~{chi}",
         "fp64_s": t64, "mixed_s": tmx, "speedup_mixed_vs_fp64": t64 / tmx,
         "mixed_config": {k: v for k, v in SWEEP_MIXED.items()},
@@ -751,35 +765,64 @@ def run_small_chain(args):
 
 
 def run_batched(args):
-    """Many independent chains: one sweep of each of N seeded XXZ chains (mixed configuration),
-    driven concurrently (one context / CUDA stream and one host thread per chain) and one after
-    the other; wall time of each (setup included: random MPS, canonicalisation, environments)."""
+    """Many independent chains: one sweep of each of N seeded XXZ chains (mixed configuration).
+    Timed (wall, setup included: random MPS, canonicalisation, environments): in lock step on
+    one context with batched eigensolves (``--lockstep``), concurrently (one context / CUDA
+    stream and one host thread per chain) and one after the other. ``--fp64-check K`` runs the
+    first K chains as the FP64 drop-in and compares energies."""
+    import mps_gb300 as mg
     from mps_gb300 import dmrg as gd
     specs = gd.chain_ensemble(args.batched)
-    o = gd.SweepOptions(tol=1e-10, lanczostol=1e-7, krylovdim=4, krylovmaxiter=8, **SWEEP_MIXED)
-    import mps_gb300 as mg
-    mg.get_context(0).synchronize()
+    kw = dict(tol=1e-10, lanczostol=1e-7, krylovdim=4, krylovmaxiter=8, tieband=SWEEP_TIEBAND)
+    o = gd.SweepOptions(**kw, **SWEEP_MIXED)
+    ctx = mg.get_context(0)
+    ctx.synchronize()
+    res, stats, t_lock, launches = {}, {}, None, None
+    if args.lockstep:
+        k0, _ = ctx.counters()
+        t0 = time.perf_counter()
+        res["lockstep"] = gd.run_chains_lockstep(specs, 1, o, ctx=ctx, stats=stats)
+        ctx.synchronize()
+        t_lock = time.perf_counter() - t0
+        launches = ctx.counters()[0] - k0
     t0 = time.perf_counter()
-    e_conc = gd.run_chains(specs, 1, o, threads=len(specs))
+    res["concurrent"] = gd.run_chains(specs, 1, o, threads=len(specs))
     t_conc = time.perf_counter() - t0
-    e_seq, t_seq = None, None
+    t_seq = None
     if not args.batched_concurrent_only:
         t0 = time.perf_counter()
-        e_seq = gd.run_chains(specs, 1, o, threads=1)
+        res["one_by_one"] = gd.run_chains(specs, 1, o, threads=1)
         t_seq = time.perf_counter() - t0
+    fp64 = None
+    if args.fp64_check:
+        o64 = gd.SweepOptions(**kw, **SWEEP_FP64)
+        fp64 = gd.run_chains(specs[:args.fp64_check], 1, o64, threads=1)
+
+    def rel(a, b):
+        return max(abs(x - y) / abs(y) for x, y in zip(a, b))
+
+    main = "lockstep" if args.lockstep else "concurrent"
+    t_main = t_lock if args.lockstep else t_conc
     line = {
-        "metric": "independent DMRG chains, one sweep each: wall s", "value": t_conc, "unit": "s",
+        "metric": "independent DMRG chains, one sweep each: wall s", "value": t_main, "unit": "s",
         "higher_is_better": False, "n_gpus": 1, "data": "synthetic (seeded Philox)",
         "config": {"workload": f"{len(specs)} XXZ chains, L in [32,128], Delta in [0,1.5], maxdim "
                                "in {128,256,512,1024} (Philox seed 1911), one 2-site sweep each",
-                   "mixed": SWEEP_MIXED, "chains": [list(s) for s in specs]},
-        "concurrent_s": t_conc, "one_by_one_s": t_seq,
-        "speedup": t_seq / t_conc if t_seq else None,
-        "max_rel_dE_concurrent_vs_one_by_one": max(abs(a - b) / abs(b)
-                                                   for a, b in zip(e_conc, e_seq))
-        if e_seq else None,
-        "energies": e_conc,
+                   "mixed": SWEEP_MIXED, "sweep": kw, "chains": [list(s) for s in specs]},
+        "mode": main, "lockstep_s": t_lock, "concurrent_s": t_conc, "one_by_one_s": t_seq,
+        "speedup_vs_one_by_one": t_seq / t_main if t_seq else None,
+        "speedup_vs_concurrent": t_conc / t_lock if args.lockstep else None,
+        "max_rel_dE_vs_one_by_one": rel(res[main], res["one_by_one"]) if t_seq else None,
+        "energies": res[main],
     }
+    if args.lockstep:
+        sizes = stats.pop("chains_per_batch")
+        line["lockstep"] = {**stats, "kernel_launches": launches,
+                            "mean_chains_per_batch": sum(sizes) / max(1, len(sizes))}
+        line["max_rel_dE_lockstep_vs_concurrent"] = rel(res["lockstep"], res["concurrent"])
+    if fp64 is not None:
+        line["fp64_check"] = {"chains": args.fp64_check, "energies_fp64": fp64,
+                              "rel_dE": [abs(a - b) / abs(b) for a, b in zip(res[main], fp64)]}
     print(json.dumps(line), flush=True)
 
 
