@@ -38,15 +38,19 @@ void operand_extents(const std::vector<GemmTask>& g, int64_t& na, int64_t& nb, i
 }  // namespace
 
 std::string tune_shape_class(const std::vector<GemmTask>& g, int S) {
-  // problems by (M, N, K) in factor-4 buckets, counts in factor-2 buckets
-  std::map<std::tuple<int, int, int>, int64_t> h;
-  for (const GemmTask& t : g)
-    if (t.M > 0 && t.N > 0) h[{log2_ceil(t.M) / 2, log2_ceil(t.N) / 2, log2_ceil(t.K) / 2}]++;
-  std::string key = "S" + std::to_string(S);
-  for (const auto& e : h)
-    key += "|" + std::to_string(std::get<0>(e.first)) + "." + std::to_string(std::get<1>(e.first)) +
-           "." + std::to_string(std::get<2>(e.first)) + ":" + std::to_string(log2_ceil(e.second + 1));
-  return key;
+  // what the configuration choice depends on: the slice count, how many waves of 128 x 128
+  // output tiles the problems give a GB300 (factor-2 buckets) and how long their K loops are
+  // (tile-weighted mean K, factor-2 buckets)
+  double tiles = 0, ktiles = 0;
+  for (const GemmTask& t : g) {
+    if (t.M <= 0 || t.N <= 0) continue;
+    const double nt = (double)((t.M + 127) / 128) * (double)((t.N + 127) / 128);
+    tiles += nt;
+    ktiles += nt * (double)t.K;
+  }
+  const int waves = log2_ceil((int64_t)(1 + 4.0 * tiles / 152.0));
+  const int kb = log2_ceil((int64_t)(1 + (tiles > 0 ? ktiles / tiles : 0.0)));
+  return "S" + std::to_string(S) + "|w" + std::to_string(waves) + "|k" + std::to_string(kb);
 }
 
 split::Tuning tune_split(Context* ctx, const std::vector<GemmTask>& g, int S) {
@@ -73,7 +77,7 @@ split::Tuning tune_split(Context* ctx, const std::vector<GemmTask>& g, int S) {
       // the fast kernel has one tile shape: only the order is a choice
       if (sp.fast && t.bn != bns[0]) continue;
       split::launch_split_gemm(ctx, sp, A->ptr, B->ptr, C->ptr, split::kAll);  // warm-up
-      constexpr int kReps = 3;
+      constexpr int kReps = 2;
       MPSG_CUDA(cudaEventRecord(e0, ctx->stream));
       for (int r = 0; r < kReps; ++r)
         split::launch_split_gemm(ctx, sp, nullptr, nullptr, C->ptr, split::kRunGemm);

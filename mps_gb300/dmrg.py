@@ -536,8 +536,10 @@ def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, ctx=None, seed:
         g = _chain_sweeps(mps, Ws, env, o, nsweeps)
         gens.append(g)
         pending[i] = next(g)
+    import time
     results = [None] * len(specs)
     nbatches, sizes = 0, []
+    t_build = t_eig = t_rest = 0.0
     while pending:
         ids = sorted(pending)
         answers = {}
@@ -549,21 +551,32 @@ def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, ctx=None, seed:
                 _, Ws, env, _ = chains[i]
                 ops.append((AA, env[l - 1], env[l + 2], Ws[l - 1], Ws[l]))
                 x0s.append(AA)
+            t0 = time.perf_counter()
             B = mg.HeffBatch(ops, precision=opts.precision, graph=graph)
+            ctx.synchronize()
+            t1 = time.perf_counter()
             _, vecs, _ = B.eigsolve(x0s, krylovdim=opts.krylovdim, maxiter=opts.krylovmaxiter,
                                     tol=opts.lanczostol)
             del B
+            ctx.synchronize()
+            t2 = time.perf_counter()
+            t_build += t1 - t0
+            t_eig += t2 - t1
             nbatches += 1
             sizes.append(len(part))
             answers.update(zip(part, vecs))
+        t0 = time.perf_counter()
         for i in ids:
             try:
                 pending[i] = gens[i].send(answers[i])
             except StopIteration as stop:
                 results[i] = stop.value[-1]
                 del pending[i]
+        ctx.synchronize()
+        t_rest += time.perf_counter() - t0
     if stats is not None:
         runs, hits = mg.tuner(ctx)
         stats.update({"batches": nbatches, "chains_per_batch": sizes, "tuner_runs": runs,
-                      "tuner_hits": hits})
+                      "tuner_hits": hits, "batch_build_s": t_build, "batched_eigsolve_s": t_eig,
+                      "chain_steps_s": t_rest})
     return results
