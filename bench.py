@@ -79,6 +79,9 @@ def parse(argv=None):
                         "eigensolve per step: every Krylov application one grouped launch per "
                         "phase for all chains, CUDA graph replay, tuned split-GEMM tiles), "
                         "timed beside the concurrent and one-by-one runs")
+    p.add_argument("--dynamic", action="store_true",
+                   help="--lockstep: the batcher takes the requests waiting when it is free "
+                        "instead of waiting for every chain")
     p.add_argument("--fp64-check", type=int, default=0, metavar="K",
                    help="--batched: also run the first K chains one by one as the FP64 drop-in "
                         "and report |dE| of the batched energies against them")
@@ -781,7 +784,8 @@ def run_batched(args):
     if args.lockstep:
         k0, _ = ctx.counters()
         t0 = time.perf_counter()
-        res["lockstep"] = gd.run_chains_lockstep(specs, 1, o, ctx=ctx, stats=stats)
+        res["lockstep"] = gd.run_chains_lockstep(specs, 1, o, stats=stats,
+                                                 wait_all=not args.dynamic)
         ctx.synchronize()
         t_lock = time.perf_counter() - t0
         launches = ctx.counters()[0] - k0

@@ -285,7 +285,9 @@ int mpsg_heff2_free(mpsg_heff* op);
  * stages) is one launch over all chains, the split GEMMs one persistent grouped launch each
  * over every chain's sector problems. Kernel tile shape and tile order come from the tuner
  * (mpsg_ctx_tuner; on unless MPSG_AUTOTUNE=0). With use_graph != 0 the application is captured
- * in a CUDA graph at its second use and replayed after that. */
+ * in a CUDA graph at its second use and replayed after that. The work runs on ctx's stream;
+ * operands may belong to other contexts of the same device (one per chain) once their
+ * producers have finished (synchronise those contexts first). */
 typedef struct mpsg_heff_batch mpsg_heff_batch;
 int mpsg_heff2_batch_create(mpsg_ctx* ctx, int32_t n, const mpsg_tensor* const* v_like,
                             const mpsg_tensor* const* envl, const mpsg_tensor* const* envr,

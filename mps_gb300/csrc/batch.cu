@@ -179,7 +179,8 @@ std::unique_ptr<HeffBatch> heff_batch_create(Context* ctx, const std::vector<Ten
   parts.reserve(n);
   for (int i = 0; i < n; ++i) {
     for (const DeviceTensor* t : {envL[i], envR[i], W1[i], W2[i]})
-      if (!t || t->ctx != ctx) throw Error(kErrArgument, "batch: operand of another context");
+      if (!t || !t->ctx || t->ctx->device != ctx->device)
+        throw Error(kErrArgument, "batch: operand missing or on another device");
     parts.push_back(heff_parts(ctx, vmeta[i], *envL[i], *envR[i], *W1[i], *W2[i], precision));
     B->keys.push_back(parts.back().key);
     B->plans.push_back(parts.back().plans);
@@ -574,8 +575,8 @@ std::vector<EigResult> eigsolve_heff2_batch(HeffBatch& B, const std::vector<cons
     throw Error(kErrUnsupported, "a batched eigensolve takes at most 128 chains");
   if ((int)x0.size() != nch) throw Error(kErrArgument, "batch: one start vector per chain");
   for (int c = 0; c < nch; ++c) {
-    if (!x0[c] || x0[c]->ctx != ctx)
-      throw Error(kErrArgument, "batch: start vector of another context");
+    if (!x0[c] || !x0[c]->ctx || x0[c]->ctx->device != ctx->device)
+      throw Error(kErrArgument, "batch: start vector missing or on another device");
     if (!same_meta(x0[c]->meta, B.vmeta[c]))
       throw Error(kErrSpaceMismatch, "batch: start vector of another structure");
   }

@@ -14,7 +14,9 @@ namespace mpsg {
 // segment of shared device buffers, and the two split GEMMs run as one persistent grouped
 // launch each over the problems of all chains (tiles dealt largest K first across chains).
 // The application (vin -> vout, 5 copy / pack / GEMM stages) is captured once in a CUDA graph
-// and replayed.
+// and replayed. Operands and start vectors may belong to other contexts of the same device
+// (one per chain): their producers must have finished (the caller synchronises those contexts)
+// before they are passed in, and they must stay alive until the call returns.
 struct HeffBatch {
   Context* ctx = nullptr;
   int S = 0, n = 0;

@@ -789,7 +789,8 @@ int mpsg_heff2_batch_apply(mpsg_heff_batch* b, const mpsg_tensor* const* v, mpsg
     mpsg::Context* c = B.ctx;
     for (int i = 0; i < B.n; ++i) {
       need(v[i], "v[i]");
-      if (v[i]->t.ctx != c) throw mpsg::Error(mpsg::kErrArgument, "batch: tensor of another context");
+      if (!v[i]->t.ctx || v[i]->t.ctx->device != c->device)
+        throw mpsg::Error(mpsg::kErrArgument, "batch: tensor on another device");
       if (!mpsg::same_meta(v[i]->t.meta, B.vmeta[i]))
         throw mpsg::Error(mpsg::kErrSpaceMismatch, "batch: tensor of another structure");
     }

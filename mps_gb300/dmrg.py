@@ -511,72 +511,118 @@ def _chain_sweeps(mps, Ws, env, o, nsweeps):
     return es
 
 
-def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, ctx=None, seed: int = 7,
-                        graph: bool = True, stats=None, max_batch: int = 128):
-    """2-site DMRG on independent chains (L, Delta, maxdim) in lock step on ONE context: every
-    chain's sweep runs as a ``sweep_steps`` generator, and at each step the eigensolve requests
-    of all chains still sweeping are answered by one batched Lanczos (``HeffBatch``): one
-    grouped application per Krylov step for all chains (CUDA graph replay; split GEMMs with
-    tuned tiles), FP64 recurrences. Truncations and environment updates run chain by chain.
-    Same start states as ``run_chains`` (Philox seed + index). Returns the last
-    post-truncation energy of each chain; ``stats`` (a dict) collects batch counts, the chain
-    count per batch and the tuner's runs and hits."""
-    ctx = ctx or mg.get_context(0)
-    if opts.precision < 2:
-        raise ValueError("the lock-step driver batches the split-precision Krylov matvecs: "
-                         "precision >= 2")
-    chains, gens, pending = [], [], {}
-    for i, (L, delta, chi) in enumerate(specs):
-        Ws = xxz_u1mpo(L, delta, ctx=ctx)
-        mps = mps_from_host(binomial_mps_host(L, L // 2, chi, seed + i), ctx)
-        center_at(mps, 1, svd=opts.svd, normalize=True)
-        env = initialenv(mps, Ws)
-        o = SweepOptions(**{**opts.__dict__, "maxdim": chi})
-        chains.append((mps, Ws, env, o))
-        g = _chain_sweeps(mps, Ws, env, o, nsweeps)
-        gens.append(g)
-        pending[i] = next(g)
+def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, device: int = 0, seed: int = 7,
+                        graph: bool = True, stats=None, max_batch: int = 128,
+                        wait_all: bool = True):
+    """2-site DMRG on independent chains (L, Delta, maxdim) with batched eigensolves. Every
+    chain runs its sweeps on its own context and host thread (as ``run_chains``), as a
+    ``sweep_steps`` generator; its eigensolve requests go to one batcher, which answers all
+    requests waiting at that moment with ONE batched Lanczos on its own context (``HeffBatch``:
+    every Krylov application one grouped launch per phase for all those chains, replayed from a
+    CUDA graph, split GEMMs with tuned tiles; FP64 recurrences). With ``wait_all`` the batcher
+    waits until every chain still sweeping has a request (lock step); otherwise it takes what is
+    waiting. Same start states as ``run_chains`` (Philox seed + index). Returns the last
+    post-truncation energy of each chain; ``stats`` (a dict) collects batch counts, chains per
+    batch, batcher times and the tuner's runs and hits."""
+    import threading
     import time
-    results = [None] * len(specs)
-    nbatches, sizes = 0, []
-    t_build = t_eig = t_rest = 0.0
-    while pending:
-        ids = sorted(pending)
-        answers = {}
-        for k in range(0, len(ids), max_batch):
-            part = ids[k:k + max_batch]
-            ops, x0s = [], []
-            for i in part:
-                AA, l = pending[i]
-                _, Ws, env, _ = chains[i]
-                ops.append((AA, env[l - 1], env[l + 2], Ws[l - 1], Ws[l]))
-                x0s.append(AA)
-            t0 = time.perf_counter()
-            B = mg.HeffBatch(ops, precision=opts.precision, graph=graph)
-            ctx.synchronize()
-            t1 = time.perf_counter()
-            _, vecs, _ = B.eigsolve(x0s, krylovdim=opts.krylovdim, maxiter=opts.krylovmaxiter,
-                                    tol=opts.lanczostol)
-            del B
-            ctx.synchronize()
-            t2 = time.perf_counter()
-            t_build += t1 - t0
-            t_eig += t2 - t1
-            nbatches += 1
-            sizes.append(len(part))
-            answers.update(zip(part, vecs))
-        t0 = time.perf_counter()
-        for i in ids:
-            try:
-                pending[i] = gens[i].send(answers[i])
-            except StopIteration as stop:
-                results[i] = stop.value[-1]
-                del pending[i]
-        ctx.synchronize()
-        t_rest += time.perf_counter() - t0
+    if opts.precision < 2:
+        raise ValueError("batched eigensolves run the split-precision Krylov matvecs: "
+                         "precision >= 2")
+    n = len(specs)
+    bctx = mg.Context(device)
+    cv = threading.Condition()
+    waiting, answers = {}, {}
+    active = set(range(n))
+    results = [None] * n
+    failed = []
+    record = {"batches": 0, "chains_per_batch": [], "batch_build_s": 0.0,
+              "batched_eigsolve_s": 0.0}
+
+    def chain(i):
+        try:
+            L, delta, chi = specs[i]
+            ctx = mg.Context(device)
+            Ws = xxz_u1mpo(L, delta, ctx=ctx)
+            mps = mps_from_host(binomial_mps_host(L, L // 2, chi, seed + i), ctx)
+            center_at(mps, 1, svd=opts.svd, normalize=True)
+            env = initialenv(mps, Ws)
+            o = SweepOptions(**{**opts.__dict__, "maxdim": chi})
+            gen = _chain_sweeps(mps, Ws, env, o, nsweeps)
+            req = next(gen)
+            while True:
+                AA, l = req
+                ctx.synchronize()  # the batcher's stream reads these tensors
+                with cv:
+                    waiting[i] = (AA, env[l - 1], env[l + 2], Ws[l - 1], Ws[l])
+                    cv.notify_all()
+                    cv.wait_for(lambda: i in answers or failed)
+                    if failed:
+                        return
+                    v = answers.pop(i)
+                vec = mg.copy(v, ctx)
+                ctx.synchronize()  # before the batcher's vector is released
+                del v
+                try:
+                    req = gen.send(vec)
+                except StopIteration as stop:
+                    results[i] = stop.value[-1]
+                    return
+        except BaseException as e:  # noqa: BLE001 (re-raised in the caller)
+            with cv:
+                failed.append(e)
+                cv.notify_all()
+        finally:
+            with cv:
+                active.discard(i)
+                cv.notify_all()
+
+    def batcher():
+        try:
+            while True:
+                with cv:
+                    cv.wait_for(lambda: failed or not active or
+                                (waiting and (not wait_all or len(waiting) >= len(active))))
+                    if failed or (not active and not waiting):
+                        return
+                    batch = dict(waiting)
+                    waiting.clear()
+                ids = sorted(batch)
+                for k in range(0, len(ids), max_batch):
+                    part = ids[k:k + max_batch]
+                    t0 = time.perf_counter()
+                    B = mg.HeffBatch([batch[i] for i in part], precision=opts.precision,
+                                     graph=graph, ctx=bctx)
+                    bctx.synchronize()
+                    t1 = time.perf_counter()
+                    _, vecs, _ = B.eigsolve([batch[i][0] for i in part],
+                                            krylovdim=opts.krylovdim,
+                                            maxiter=opts.krylovmaxiter, tol=opts.lanczostol)
+                    del B
+                    bctx.synchronize()
+                    record["batch_build_s"] += t1 - t0
+                    record["batched_eigsolve_s"] += time.perf_counter() - t1
+                    record["batches"] += 1
+                    record["chains_per_batch"].append(len(part))
+                    with cv:
+                        answers.update(zip(part, vecs))
+                        cv.notify_all()
+        except BaseException as e:  # noqa: BLE001
+            with cv:
+                failed.append(e)
+                cv.notify_all()
+
+    threads = [threading.Thread(target=chain, args=(i,)) for i in range(n)]
+    tb = threading.Thread(target=batcher)
+    for t in threads:
+        t.start()
+    tb.start()
+    for t in threads:
+        t.join()
+    tb.join()
+    if failed:
+        raise failed[0]
     if stats is not None:
-        runs, hits = mg.tuner(ctx)
-        stats.update({"batches": nbatches, "chains_per_batch": sizes, "tuner_runs": runs,
-                      "tuner_hits": hits, "batch_build_s": t_build, "batched_eigsolve_s": t_eig,
-                      "chain_steps_s": t_rest})
+        runs, hits = mg.tuner(bctx)
+        stats.update({**record, "tuner_runs": runs, "tuner_hits": hits})
     return results

@@ -512,10 +512,13 @@ def dual(x):
     return SymTensor(h, x.ctx)
 
 
-def copy(A: SymTensor) -> SymTensor:
+def copy(A: SymTensor, ctx=None) -> SymTensor:
+    """A copy of A, on ``ctx`` (another context of the same device) when given: the copy is
+    ordered on that context's stream, so A's producer must have finished."""
+    ctx = ctx or A.ctx
     h = C.c_void_p()
-    call("mpsg_tensor_copy", A.ctx.handle, A.handle, C.byref(h))
-    return SymTensor(h, A.ctx)
+    call("mpsg_tensor_copy", ctx.handle, A.handle, C.byref(h))
+    return SymTensor(h, ctx)
 
 
 def similar(A: SymTensor) -> SymTensor:
@@ -822,11 +825,13 @@ class HeffBatch:
     launch over all chains (the split GEMMs one persistent grouped launch each, tile shape and
     order from the tuner), captured in a CUDA graph at its second use when ``graph``."""
 
-    def __init__(self, ops, precision=4, graph=True):
+    def __init__(self, ops, precision=4, graph=True, ctx=None):
         ops = list(ops)
         if not ops:
             raise MPSGError(_lib.ERR_ARGUMENT, "a batch needs at least one operator")
-        self.ctx = ops[0][0].ctx
+        # the batch's work runs on ``ctx``; operands may come from other contexts of the device
+        # once their producers have finished
+        self.ctx = ctx or ops[0][0].ctx
         self.n = len(ops)
         cols = [_handles([o[k] for o in ops]) for k in range(5)]
         h = C.c_void_p()

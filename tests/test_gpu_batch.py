@@ -101,11 +101,14 @@ def test_lockstep_chains_match_one_by_one():
     specs = [(12, 0.4, 16), (16, 1.1, 24), (10, 0.0, 8), (14, 0.7, 32)]
     o = gd.SweepOptions(tol=1e-10, lanczostol=1e-9, krylovdim=5, krylovmaxiter=6, precision=4,
                         energy_precision=7, env_precision=7, svd="exact")
-    ctx = mg.Context(0)
     stats = {}
-    e_lock = gd.run_chains_lockstep(specs, 2, o, ctx=ctx, stats=stats)
+    e_lock = gd.run_chains_lockstep(specs, 2, o, stats=stats)
     e_one = gd.run_chains(specs, 2, o, threads=1)
     for a, b in zip(e_lock, e_one):
         assert abs(a - b) <= 1e-10 * abs(b), (a, b)
     assert stats["batches"] >= 2 * (2 * 16 - 3)  # the longest chain: 2L - 3 eigensolves a sweep
     assert max(stats["chains_per_batch"]) == len(specs)
+    # dynamic batching (whatever is waiting) gives the same energies
+    e_dyn = gd.run_chains_lockstep(specs, 2, o, wait_all=False)
+    for a, b in zip(e_dyn, e_one):
+        assert abs(a - b) <= 1e-10 * abs(b), (a, b)
