@@ -610,20 +610,15 @@ std::vector<EigResult> eigsolve_heff2_batch(HeffBatch& B, const std::vector<cons
   ChainGeom* d_geo = nullptr;
   MPSG_CUDA(cudaMallocAsync((void**)&d_geo, sizeof(ChainGeom) * nch, st));
   MPSG_CUDA(cudaMemcpyAsync(d_geo, geo.data(), sizeof(ChainGeom) * nch, cudaMemcpyHostToDevice, st));
-  double* h_out = nullptr;  // pinned: norms and eigen outputs read back by the host
-  MPSG_CUDA(cudaMallocHost((void**)&h_out, sizeof(double) * 3 * nch));
+  double* h_out = ctx->h_pinned + 64;  // pinned: norms and eigen outputs read by the host
+  static_assert(Context::kPinnedDoubles >= 64 + 3 * kMaxChains, "pinned scratch too small");
   struct Guard {
     ChainGeom* g;
-    double* h;
     cudaStream_t s;
     ~Guard() {
       if (g) cudaFreeAsync(g, s);
-      if (h) {
-        cudaStreamSynchronize(s);
-        cudaFreeHost(h);
-      }
     }
-  } guard{d_geo, h_out, st};
+  } guard{d_geo, st};
   double* V = Vb->ptr;
   double* w = B.vout->ptr;
   const dim3 vgrid((unsigned)G, (unsigned)nch);

@@ -221,8 +221,18 @@ struct BlockSVD {
   int64_t M, N, k;
   std::shared_ptr<Buffer> U, S, V;  // U: M x k, S: k, V: N x k (all column-major)
   std::shared_ptr<Buffer> work, aux, wbuf;  // temporaries, kept until the lanes are joined
+  std::shared_ptr<Buffer> ref;              // second-level Gram workspace (density matrix)
   int lwork = 0;
+  int64_t refined = 0;                      // eigenvectors recomputed by the second level
 };
+
+// Second level of the density-matrix factorisation: Gram eigenvalues below kRefine times the
+// largest of the block (singular values below about 3e-6 of the block's largest) have
+// eigenvectors fixed only to eps * lambda_max / gap by the first eigen-decomposition, which at
+// a DMRG truncation cut mixes kept and discarded directions. Their subspace is decomposed
+// again through its own Gram matrix, whose entries are of the size of those eigenvalues, so the
+// second decomposition resolves them to eps relative to the largest of them.
+constexpr double kRefine = 1e-11;
 
 // Exact thin SVD of one column-major M x N block with cuSOLVER's QR-iteration SVD (gesvd, the
 // method of the reference's fallback, src/symtools.jl:14-19). gesvd wants M >= N, so a wide
@@ -313,7 +323,13 @@ void prepare_gram(Context* ctx, cusolverDnHandle_t h, BlockSVD& B, bool left) {
   B.aux = alloc_buffer(ctx, n);
   MPSG_SOLVER(cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
                                           (int)n, B.work->ptr, (int)n, B.aux->ptr, &B.lwork));
+  int lwork2 = 0;  // the second level decomposes at most k x k
+  MPSG_SOLVER(cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                          (int)k, B.work->ptr, (int)k, B.aux->ptr, &lwork2));
+  B.lwork = std::max(B.lwork, lwork2);
   B.wbuf = alloc_buffer(ctx, std::max(B.lwork, 1));
+  const int64_t rows = left ? N : M;  // rows of the other factor
+  B.ref = alloc_buffer(ctx, rows * k + 2 * k * k + n * k + 2 * k);
 }
 
 void run_gram(Context* ctx, cudaStream_t st, cusolverDnHandle_t h, cublasHandle_t bl,
@@ -332,13 +348,46 @@ void run_gram(Context* ctx, cudaStream_t st, cusolverDnHandle_t h, cublasHandle_
   double* X = left ? B.U->ptr : B.V->ptr;  // orthonormal factor
   double* Y = left ? B.V->ptr : B.U->ptr;  // the other one
   top_eigpairs_kernel<<<grid_for(n * k), 256, 0, st>>>(X, B.S->ptr, G, B.aux->ptr, n, k);
+  const int64_t rows = left ? N : M;
+  // second level (kRefine): the eigenvalues decide how many trailing columns of X to redo
+  std::vector<double> w(n);
+  int info = 0;
+  MPSG_CUDA(cudaMemcpyAsync(w.data(), B.aux->ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  MPSG_CUDA(cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MPSG_CUDA(cudaStreamSynchronize(st));
+  int64_t p = 0;
+  if (info == 0 && n > 0 && w[n - 1] > 0)
+    for (int64_t i = 0; i < k; ++i)
+      if (w[n - 1 - i] < kRefine * w[n - 1]) ++p;
+  if (p >= 2) {
+    double* Xs = X + n * (k - p);  // the trailing p columns (smallest eigenvalues of the top k)
+    double* Ys = B.ref->ptr;       // rows x p
+    double* Gs = Ys + rows * k;    // p x p
+    double* Rs = Gs + k * k;       // p x p, descending
+    double* Xt = Rs + k * k;       // n x p
+    double* ws = Xt + n * k;       // p eigenvalues, p square roots (unused)
+    if (left)  // Ys = A^T Xs
+      MPSG_BLAS(cublasDgemm(bl, CUBLAS_OP_T, CUBLAS_OP_N, (int)N, (int)p, (int)M, &one, A, (int)M,
+                            Xs, (int)M, &zero, Ys, (int)N));
+    else  // Ys = A Xs
+      MPSG_BLAS(cublasDgemm(bl, CUBLAS_OP_N, CUBLAS_OP_N, (int)M, (int)p, (int)N, &one, A, (int)M,
+                            Xs, (int)N, &zero, Ys, (int)M));
+    MPSG_BLAS(cublasDsyrk(bl, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, (int)p, (int)rows, &one, Ys,
+                          (int)rows, &zero, Gs, (int)p));
+    MPSG_SOLVER(cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)p, Gs,
+                                 (int)p, ws, B.wbuf->ptr, B.lwork, dinfo));
+    top_eigpairs_kernel<<<grid_for(p * p), 256, 0, st>>>(Rs, ws + k, Gs, ws, p, p);
+    MPSG_BLAS(cublasDgemm(bl, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, (int)p, (int)p, &one, Xs, (int)n,
+                          Rs, (int)p, &zero, Xt, (int)n));
+    MPSG_CUDA(cudaMemcpyAsync(Xs, Xt, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, st));
+    B.refined = p;
+  }
   if (left)  // V (N x k) = A^T U
     MPSG_BLAS(cublasDgemm(bl, CUBLAS_OP_T, CUBLAS_OP_N, (int)N, (int)k, (int)M, &one, A, (int)M,
                           X, (int)M, &zero, Y, (int)N));
   else  // U (M x k) = A V
     MPSG_BLAS(cublasDgemm(bl, CUBLAS_OP_N, CUBLAS_OP_N, (int)M, (int)k, (int)N, &one, A, (int)M,
                           X, (int)N, &zero, Y, (int)M));
-  const int64_t rows = left ? N : M;
   col_norms_kernel<<<(unsigned)std::min<int64_t>((k + 7) / 8, 1184), 256, 0, st>>>(Y, B.S->ptr,
                                                                                  rows, k);
   running_min_kernel<<<1, 1, 0, st>>>(B.S->ptr, k);

@@ -39,7 +39,7 @@ void context_init(Context* ctx, int device) {
   MPSG_CUDA(cudaMalloc(&ctx->d_partials, sizeof(double) * (ctx->num_sms * 4 + 64)));
   MPSG_CUDA(cudaMalloc(&ctx->d_copy_err, sizeof(int)));
   MPSG_CUDA(cudaMemset(ctx->d_copy_err, 0, sizeof(int)));
-  MPSG_CUDA(cudaMallocHost(&ctx->h_pinned, sizeof(double) * 64));
+  MPSG_CUDA(cudaMallocHost(&ctx->h_pinned, sizeof(double) * Context::kPinnedDoubles));
   const char* dbg = std::getenv("MPSG_DEBUG_SYNC");
   ctx->debug_sync = dbg && dbg[0] == '1';
 }

@@ -176,7 +176,9 @@ struct Context : std::enable_shared_from_this<Context> {
   cudaStream_t stream = nullptr;
   double* d_partials = nullptr;   // reduction partials (one per CTA of a reduction launch)
   int* d_copy_err = nullptr;      // set by the TMA-staged copy kernel when a bounded wait expires
-  double* h_pinned = nullptr;     // small pinned host scratch for scalar results
+  // small pinned host scratch: [0, 64) scalar results, [64, 64 + 3 * 128) the batched Lanczos
+  static constexpr int kPinnedDoubles = 64 + 3 * 128;
+  double* h_pinned = nullptr;
   PlanCache<DevContract> contract_cache;
   std::unordered_map<std::string, std::shared_ptr<DevReleg>> releg_cache;
   PlanCache<DevGemmPlan> matmul_cache;
