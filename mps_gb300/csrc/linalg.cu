@@ -6,6 +6,7 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <exception>
 #include <functional>
@@ -31,7 +32,14 @@ namespace mpsg {
 
 namespace {
 
-constexpr int kLanes = 4;
+constexpr int kLanes = 8;  // solver lanes created per context; MPSG_SOLVER_LANES of them used
+
+// Lanes a call spreads its blocks over: MPSG_SOLVER_LANES (1..8), default 4.
+int active_lanes() {
+  const char* e = std::getenv("MPSG_SOLVER_LANES");
+  const int n = e ? std::atoi(e) : 4;
+  return std::max(1, std::min(kLanes, n));
+}
 
 // Side streams with their own cuSOLVER and cuBLAS handles. The per-sector factorisations of one
 // call are independent, so they run concurrently on these lanes, forked from the context stream
@@ -155,10 +163,11 @@ void run_on_lanes(Context* ctx, SolverLanes& L, size_t nb, const std::function<d
   std::stable_sort(order.begin(), order.end(),
                    [&](size_t x, size_t y) { return cost(x) > cost(y); });
   std::vector<size_t> list[kLanes];
-  double load[kLanes] = {0, 0, 0, 0};
+  double load[kLanes] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int nl = active_lanes();
   for (size_t b : order) {
     int lane = 0;
-    for (int i = 1; i < kLanes; ++i)
+    for (int i = 1; i < nl; ++i)
       if (load[i] < load[lane]) lane = i;
     load[lane] += cost(b);
     list[lane].push_back(b);
@@ -226,13 +235,17 @@ struct BlockSVD {
   int64_t refined = 0;                      // eigenvectors recomputed by the second level
 };
 
-// Second level of the density-matrix factorisation: Gram eigenvalues below kRefine times the
+// Second level of the density-matrix factorisation: Gram eigenvalues below 1e-11 times the
 // largest of the block (singular values below about 3e-6 of the block's largest) have
 // eigenvectors fixed only to eps * lambda_max / gap by the first eigen-decomposition, which at
 // a DMRG truncation cut mixes kept and discarded directions. Their subspace is decomposed
 // again through its own Gram matrix, whose entries are of the size of those eigenvalues, so the
 // second decomposition resolves them to eps relative to the largest of them.
-constexpr double kRefine = 1e-11;
+constexpr double kRefineDefault = 1e-11;
+double refine_threshold() {  // MPSG_GRAM_REFINE overrides it (0: no second level)
+  const char* e = std::getenv("MPSG_GRAM_REFINE");
+  return e ? std::atof(e) : kRefineDefault;
+}
 
 // Exact thin SVD of one column-major M x N block with cuSOLVER's QR-iteration SVD (gesvd, the
 // method of the reference's fallback, src/symtools.jl:14-19). gesvd wants M >= N, so a wide
@@ -349,16 +362,17 @@ void run_gram(Context* ctx, cudaStream_t st, cusolverDnHandle_t h, cublasHandle_
   double* Y = left ? B.V->ptr : B.U->ptr;  // the other one
   top_eigpairs_kernel<<<grid_for(n * k), 256, 0, st>>>(X, B.S->ptr, G, B.aux->ptr, n, k);
   const int64_t rows = left ? N : M;
-  // second level (kRefine): the eigenvalues decide how many trailing columns of X to redo
+  // second level: the eigenvalues decide how many trailing columns of X to redo
   std::vector<double> w(n);
   int info = 0;
   MPSG_CUDA(cudaMemcpyAsync(w.data(), B.aux->ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
   MPSG_CUDA(cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
   MPSG_CUDA(cudaStreamSynchronize(st));
   int64_t p = 0;
-  if (info == 0 && n > 0 && w[n - 1] > 0)
+  const double thr = refine_threshold();
+  if (info == 0 && n > 0 && w[n - 1] > 0 && thr > 0)
     for (int64_t i = 0; i < k; ++i)
-      if (w[n - 1 - i] < kRefine * w[n - 1]) ++p;
+      if (w[n - 1 - i] < thr * w[n - 1]) ++p;
   if (p >= 2) {
     double* Xs = X + n * (k - p);  // the trailing p columns (smallest eigenvalues of the top k)
     double* Ys = B.ref->ptr;       // rows x p
