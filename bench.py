@@ -278,7 +278,9 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------------------------
-SWEEP_MIXED = dict(precision=4, energy_precision=7, env_precision=7, svd="gram")
+# Krylov matvecs at 5 slices: with 4 (relative error 2e-8 per matvec) the Lanczos vectors of
+# the first sweep's unconverged solves move the post-truncation energies by up to 5e-9
+SWEEP_MIXED = dict(precision=5, energy_precision=7, env_precision=7, svd="gram")
 # Truncation tie band (both sweeps): singular values within 1e-9 of the largest count as equal
 # and the lowest sector keeps the state, so that SU(2) multiplets split by the maxdim cut are
 # split the same way whatever the rounding of the two factorisations

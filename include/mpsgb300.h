@@ -312,6 +312,11 @@ int mpsg_heff2_batch_free(mpsg_heff_batch* b);
  * on / off (-1 leaves it); runs = shape classes timed so far, hits = choices served from the
  * context's table. */
 int mpsg_ctx_tuner(mpsg_ctx* ctx, int32_t enable, int64_t* runs, int64_t* hits);
+/* Fixes the split-GEMM configuration of plans built from now on in this context: N tile bn (64,
+ * 128, or 0 = the kernel's default for the slice count; 128 falls back to the default where it
+ * does not fit) and tile order (0 = decreasing K, 1 = problem by problem); bn < 0 returns to the
+ * tuner / defaults. For measurements and tests. */
+int mpsg_ctx_set_split_tuning(mpsg_ctx* ctx, int32_t bn, int32_t order);
 /* Host self-check of the tensor-core H_eff plans for these structures (any tensors, also
  * structure-only ones): every copy and GEMM window in bounds, every output element written
  * once, and the composed intermediate copy equal to the two-step copy. */

@@ -102,6 +102,12 @@ split::Tuning tune_split(Context* ctx, const std::vector<GemmTask>& g, int S) {
 }
 
 split::Tuning choose_tuning(Context* ctx, const std::vector<GemmTask>& g, int S) {
+  if (ctx->forced_bn >= 0) {  // a configuration fixed by the caller
+    split::Tuning t;
+    t.bn = (ctx->forced_bn == 64 || ctx->forced_bn == split::exact_bn(S)) ? ctx->forced_bn : 0;
+    t.order = ctx->forced_order;
+    return t;
+  }
   if (!ctx->autotune || g.empty()) return split::Tuning();
   const std::string key = tune_shape_class(g, S);
   auto it = ctx->tune_cache.find(key);

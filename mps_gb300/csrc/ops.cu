@@ -237,7 +237,7 @@ static void run_gemm(Context* ctx, DevGemmPlan& g, const double* A, const double
   auto& sp = g.splitp[precision];
   if (!sp) {
     sp = std::make_shared<split::SplitPlan>();
-    sp->build(ctx, g.host, precision);
+    sp->build(ctx, g.host, precision, choose_tuning(ctx, g.host, precision));
     // the new scratch counts against the plan caches' budgets (the caller holds `g`)
     ctx->contract_cache.trim();
     ctx->matmul_cache.trim();

@@ -197,6 +197,7 @@ struct Context : std::enable_shared_from_this<Context> {
   bool autotune = false;
   std::unordered_map<std::string, std::pair<int, int>> tune_cache;
   int64_t tune_runs = 0, tune_hits = 0;
+  int forced_bn = -1, forced_order = -1;  // mpsg_ctx_set_split_tuning: fixed configuration
   void* solver = nullptr;         // cusolverDnHandle_t, created on first SVD
   void (*solver_destroy)(void*) = nullptr;
   // optional per-kernel-class event timing (see mpsg_ctx_set_timing)

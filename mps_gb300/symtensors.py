@@ -27,7 +27,7 @@ __all__ = [
     "mpsupdateleft",
     "mpsupdateright", "SpaceMismatch", "MPSGError", "set_default_precision", "_svd_",
     "svdtrunc", "svd_complex", "dots", "lincomb", "truncatedsizes", "small_eigh",
-    "eigsolve_heff2", "EigInfo", "Heff2", "HeffBatch", "tuner", "HostBuffer", "Copy", "download_async",
+    "eigsolve_heff2", "EigInfo", "Heff2", "HeffBatch", "tuner", "set_split_tuning", "HostBuffer", "Copy", "download_async",
     "upload_async", "device_checks", "checked_library",
 ]
 
@@ -890,6 +890,13 @@ def tuner(ctx, enable=None):
     call("mpsg_ctx_tuner", ctx.handle, -1 if enable is None else int(bool(enable)), C.byref(r),
          C.byref(h))
     return r.value, h.value
+
+
+def set_split_tuning(ctx, bn=None, order=0):
+    """Fix the split-GEMM configuration of plans built from now on in ``ctx``: N tile ``bn``
+    (64, 128 or 0 = default; None returns to the tuner / defaults) and tile ``order`` (0 =
+    decreasing K, 1 = problem by problem)."""
+    call("mpsg_ctx_set_split_tuning", ctx.handle, -1 if bn is None else int(bn), int(order))
 
 
 def eigsolve_heff2(x0, envL, envR, W1, W2, krylovdim=5, maxiter=8, tol=1e-7, precision=None):

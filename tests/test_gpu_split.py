@@ -165,3 +165,22 @@ def test_applymps2site_from_host_buffers(S):
         np.testing.assert_array_equal(d.to_flat(), h)
     with pytest.raises(mg.MPSGError):
         mg.applymps2site_host(*dev, host_in, np.zeros(3), precision=S)
+
+
+@pytest.mark.parametrize("S", [4, 5, 6, 7])
+@pytest.mark.parametrize("bn,order", [(64, 0), (64, 1), (128, 0), (0, 1)])
+def test_split_configurations_agree(S, bn, order):
+    """Every N tile and tile order the tuner may pick gives the default configuration's result:
+    the exact groups are order-independent integer sums, so only the shared accumulator of the
+    two smallest groups may round differently (far below the slicing bound)."""
+    rng = np.random.default_rng(100 + S)
+    A, B = pair(rng, [(0, 300), (1, 129), (2, 7)], [(0, 1500), (1, 65), (2, 1)],
+                [(0, 200), (1, 300), (2, 3)])
+    want = st.matmul(A, B)
+    ref = mg.matmul(to_device(A), to_device(B), precision=S)
+    ctx = mg.Context(0)
+    mg.set_split_tuning(ctx, bn, order)
+    got = mg.matmul(to_device(A, ctx), to_device(B, ctx), precision=S)
+    for s in want.blocks:
+        assert relerr(got.blocks[s], want.blocks[s]) < TOL[S], s
+        assert relerr(got.blocks[s], ref.blocks[s]) < 1e-3 * TOL[S], s
