@@ -293,6 +293,17 @@ int mpsg_heff2_batch_create(mpsg_ctx* ctx, int32_t n, const mpsg_tensor* const* 
                             const mpsg_tensor* const* envl, const mpsg_tensor* const* envr,
                             const mpsg_tensor* const* w1, const mpsg_tensor* const* w2,
                             int32_t precision, int32_t use_graph, mpsg_heff_batch** out);
+/* One chain's share of a batch, prepared on that chain's own context (plans and the FP64 W
+ * folds; no split-precision packing of its own): usable only in mpsg_heff2_batch_from. */
+int mpsg_heff2_prepare(mpsg_ctx* ctx, const mpsg_tensor* v_like, const mpsg_tensor* envl,
+                       const mpsg_tensor* envr, const mpsg_tensor* w1, const mpsg_tensor* w2,
+                       int32_t precision, mpsg_heff** out);
+/* The batch of n prepared operators (any contexts of ctx's device, all preparations finished,
+ * e.g. their contexts synchronised): their host work is already done, so assembling the batch
+ * on ctx is concatenation, one copy of the constant operands and one packing. The operators
+ * may be freed once this returns. */
+int mpsg_heff2_batch_from(mpsg_ctx* ctx, int32_t n, const mpsg_heff* const* ops,
+                          int32_t use_graph, mpsg_heff_batch** out);
 /* out[i] = H_eff_i(v[i]) for every chain, in one batched application. */
 int mpsg_heff2_batch_apply(mpsg_heff_batch* b, const mpsg_tensor* const* v, mpsg_tensor** out);
 /* mpsg_eigsolve_heff2 for every chain from x0[i] (at most 128 chains), the Lanczos recurrences

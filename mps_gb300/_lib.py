@@ -113,6 +113,8 @@ SIGNATURES = {
     "mpsg_plan_heff2_check": [P, P, P, P, P],
     "mpsg_heff2_batch_create": [P, I32, PP, PP, PP, PP, PP, I32, I32, PP],
     "mpsg_heff2_batch_apply": [P, PP, PP],
+    "mpsg_heff2_prepare": [P, P, P, P, P, P, I32, PP],
+    "mpsg_heff2_batch_from": [P, I32, PP, I32, PP],
     "mpsg_heff2_batch_eigsolve": [P, PP, I32, I32, F64, PF64, PP, PF64, PI32, PI32, PI32],
     "mpsg_heff2_batch_info": [P, PF64, PI64, PI64, PI32],
     "mpsg_heff2_batch_free": [P],

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <tuple>
 
@@ -162,46 +163,38 @@ void append_shifted(std::vector<GemmTask>& out, const std::vector<GemmTask>& in,
 
 }  // namespace
 
-std::unique_ptr<HeffBatch> heff_batch_create(Context* ctx, const std::vector<TensorMeta>& vmeta,
-                                             const std::vector<const DeviceTensor*>& envL,
-                                             const std::vector<const DeviceTensor*>& envR,
-                                             const std::vector<const DeviceTensor*>& W1,
-                                             const std::vector<const DeviceTensor*>& W2,
-                                             int precision, bool use_graph) {
-  const int n = (int)vmeta.size();
-  if (n < 1) throw Error(kErrArgument, "a batch needs at least one operator");
-  if (envL.size() != (size_t)n || envR.size() != (size_t)n || W1.size() != (size_t)n ||
-      W2.size() != (size_t)n)
-    throw Error(kErrArgument, "batch: operand lists of different lengths");
-  if (precision < 2 || precision > split::kMaxSlices)
-    throw Error(kErrUnsupported, "a batch runs the split-precision path: precision 2..7");
-  auto B = std::make_unique<HeffBatch>();
+namespace {
+
+// What the batch needs of one chain: its structure-only plans (host task lists) and how its
+// FP64 fused constant operands get into the batch's buffers.
+struct ChainPart {
+  TensorMeta vmeta;
+  std::shared_ptr<HeffPlans> plans;
+  double ref_flops = 0;
+  const double* A1 = nullptr;  // fused constant operands prepared elsewhere (copied in), or
+  const double* B2 = nullptr;  // null: folded straight into the batch's buffers by `fold`
+};
+
+std::unique_ptr<HeffBatch> build_batch(
+    Context* ctx, std::unique_ptr<HeffBatch> B, const std::vector<ChainPart>& ch, int precision,
+    const std::function<void(int, double*, double*)>& fold) {
+  const int n = (int)ch.size();
   B->ctx = ctx;
   B->S = precision;
   B->n = n;
-  B->use_graph = use_graph;
-  B->vmeta = vmeta;
-  std::vector<HeffParts> parts;
-  parts.reserve(n);
-  for (int i = 0; i < n; ++i) {
-    for (const DeviceTensor* t : {envL[i], envR[i], W1[i], W2[i]})
-      if (!t || !t->ctx || t->ctx->device != ctx->device)
-        throw Error(kErrArgument, "batch: operand missing or on another device");
-    parts.push_back(heff_parts(ctx, vmeta[i], *envL[i], *envR[i], *W1[i], *W2[i], precision));
-    B->keys.push_back(parts.back().key);
-    B->plans.push_back(parts.back().plans);
-    B->ref_flops += applymps2site_flops(ctx, vmeta[i], envL[i]->meta, envR[i]->meta,
-                                        W1[i]->meta, W2[i]->meta);
+  for (const ChainPart& c : ch) {
+    B->vmeta.push_back(c.vmeta);
+    B->ref_flops += c.ref_flops;
   }
   // segments: chain i's data in every shared buffer, 32-element aligned
   std::vector<int64_t> oA1(n), oB1(n), oC1(n), oA2(n), oB2(n), oC2(n);
   int64_t nA1 = 0, nB1 = 0, nC1 = 0, nA2 = 0, nB2 = 0, nC2 = 0;
   B->voff.resize(n);
   for (int i = 0; i < n; ++i) {
-    const ContractPlan& h1 = *B->plans[i]->c1->host;
-    const ContractPlan& h2 = *B->plans[i]->c2->host;
+    const ContractPlan& h1 = *ch[i].plans->c1->host;
+    const ContractPlan& h2 = *ch[i].plans->c2->host;
     B->voff[i] = B->vtot;
-    B->vtot += align32(vmeta[i].total);
+    B->vtot += align32(ch[i].vmeta.total);
     oA1[i] = nA1, nA1 += align32(h1.fa.out.total);
     oB1[i] = nB1, nB1 += align32(h1.fb.out.total);
     oC1[i] = nC1, nC1 += align32(h1.mm.out.total);
@@ -219,15 +212,24 @@ std::unique_ptr<HeffBatch> heff_batch_create(Context* ctx, const std::vector<Ten
   B->C2 = alloc_buffer(ctx, std::max<int64_t>(nC2, 1));
   auto A1 = alloc_buffer(ctx, std::max<int64_t>(nA1, 1));
   auto B2 = alloc_buffer(ctx, std::max<int64_t>(nB2, 1));
-  // the W folds of every chain, straight into the shared constant operands
-  for (int i = 0; i < n; ++i)
-    heff_fold(ctx, parts[i], *envL[i], *envR[i], *W1[i], *W2[i], A1->ptr + oA1[i],
-              B2->ptr + oB2[i]);
+  // every chain's constant operands into the shared buffers
+  for (int i = 0; i < n; ++i) {
+    const ContractPlan& h1 = *ch[i].plans->c1->host;
+    const ContractPlan& h2 = *ch[i].plans->c2->host;
+    if (ch[i].A1) {
+      MPSG_CUDA(cudaMemcpyAsync(A1->ptr + oA1[i], ch[i].A1, sizeof(double) * h1.fa.out.total,
+                                cudaMemcpyDeviceToDevice, ctx->stream));
+      MPSG_CUDA(cudaMemcpyAsync(B2->ptr + oB2[i], ch[i].B2, sizeof(double) * h2.fb.out.total,
+                                cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+      fold(i, A1->ptr + oA1[i], B2->ptr + oB2[i]);
+    }
+  }
   // one problem list per GEMM over all chains
   std::vector<GemmTask> g1, g2;
   for (int i = 0; i < n; ++i) {
-    append_shifted(g1, B->plans[i]->c1->mm.host, oA1[i], oB1[i], oC1[i]);
-    append_shifted(g2, B->plans[i]->c2->mm.host, oA2[i], oB2[i], oC2[i]);
+    append_shifted(g1, ch[i].plans->c1->mm.host, oA1[i], oB1[i], oC1[i]);
+    append_shifted(g2, ch[i].plans->c2->mm.host, oA2[i], oB2[i], oC2[i]);
   }
   const char* at = std::getenv("MPSG_AUTOTUNE");
   const bool was = ctx->autotune;
@@ -249,16 +251,16 @@ std::unique_ptr<HeffBatch> heff_batch_create(Context* ctx, const std::vector<Ten
   // one copy list per copy stage over all chains
   std::vector<CopyTask> tin, tx2a, tout;
   for (int i = 0; i < n; ++i) {
-    const HeffPlans& P = *B->plans[i];
+    const HeffPlans& P = *ch[i].plans;
     const ContractPlan& h1 = *P.c1->host;
     const ContractPlan& h2 = *P.c2->host;
     if (h1.fb.identity)
-      tin.push_back(contiguous_task(vmeta[i].total, B->voff[i], oB1[i]));
+      tin.push_back(contiguous_task(ch[i].vmeta.total, B->voff[i], oB1[i]));
     else
       append_shifted(tin, h1.fb.tasks, B->voff[i], oB1[i]);
     append_shifted(tx2a, P.x2a_host, oC1[i], oA2[i]);
     if (h2.split.identity)
-      tout.push_back(contiguous_task(vmeta[i].total, oC2[i], B->voff[i]));
+      tout.push_back(contiguous_task(ch[i].vmeta.total, oC2[i], B->voff[i]));
     else
       append_shifted(tout, h2.split.tasks, oC2[i], B->voff[i]);
   }
@@ -273,6 +275,68 @@ std::unique_ptr<HeffBatch> heff_batch_create(Context* ctx, const std::vector<Ten
   B->cx2a.upload(tx2a, false, ctx->stream);
   B->cout.upload(tout, false, ctx->stream);
   return B;
+}
+
+}  // namespace
+
+std::unique_ptr<HeffBatch> heff_batch_create(Context* ctx, const std::vector<TensorMeta>& vmeta,
+                                             const std::vector<const DeviceTensor*>& envL,
+                                             const std::vector<const DeviceTensor*>& envR,
+                                             const std::vector<const DeviceTensor*>& W1,
+                                             const std::vector<const DeviceTensor*>& W2,
+                                             int precision, bool use_graph) {
+  const int n = (int)vmeta.size();
+  if (n < 1) throw Error(kErrArgument, "a batch needs at least one operator");
+  if (envL.size() != (size_t)n || envR.size() != (size_t)n || W1.size() != (size_t)n ||
+      W2.size() != (size_t)n)
+    throw Error(kErrArgument, "batch: operand lists of different lengths");
+  if (precision < 2 || precision > split::kMaxSlices)
+    throw Error(kErrUnsupported, "a batch runs the split-precision path: precision 2..7");
+  auto B = std::make_unique<HeffBatch>();
+  B->use_graph = use_graph;
+  std::vector<HeffParts> parts;
+  std::vector<ChainPart> ch(n);
+  parts.reserve(n);
+  for (int i = 0; i < n; ++i) {
+    for (const DeviceTensor* t : {envL[i], envR[i], W1[i], W2[i]})
+      if (!t || !t->ctx || t->ctx->device != ctx->device)
+        throw Error(kErrArgument, "batch: operand missing or on another device");
+    parts.push_back(heff_parts(ctx, vmeta[i], *envL[i], *envR[i], *W1[i], *W2[i], precision));
+    B->keys.push_back(parts.back().key);
+    B->plans.push_back(parts.back().plans);  // handed back to this context's cache at the end
+    ch[i].vmeta = vmeta[i];
+    ch[i].plans = parts.back().plans;
+    ch[i].ref_flops = applymps2site_flops(ctx, vmeta[i], envL[i]->meta, envR[i]->meta,
+                                          W1[i]->meta, W2[i]->meta);
+  }
+  return build_batch(ctx, std::move(B), ch, precision, [&](int i, double* a1, double* b2) {
+    heff_fold(ctx, parts[i], *envL[i], *envR[i], *W1[i], *W2[i], a1, b2);
+  });
+}
+
+std::unique_ptr<HeffBatch> heff_batch_from_ops(Context* ctx,
+                                               const std::vector<const HeffOp*>& ops,
+                                               bool use_graph) {
+  const int n = (int)ops.size();
+  if (n < 1) throw Error(kErrArgument, "a batch needs at least one operator");
+  std::vector<ChainPart> ch(n);
+  int S = 0;
+  for (int i = 0; i < n; ++i) {
+    const HeffOp* op = ops[i];
+    if (!op || !op->batch_only || !op->plans || !op->fusedA1 || !op->fusedB2)
+      throw Error(kErrArgument, "batch: operator not prepared for a batch");
+    if (op->ctx->device != ctx->device) throw Error(kErrArgument, "batch: operator on another device");
+    if (i == 0) S = op->precision;
+    if (op->precision != S) throw Error(kErrArgument, "batch: operators of different precision");
+    ch[i].vmeta = op->vmeta;
+    ch[i].plans = op->plans;  // read here only: the operator's context keeps its plans
+    ch[i].ref_flops = op->ref_flops;
+    ch[i].A1 = op->fusedA1->ptr;
+    ch[i].B2 = op->fusedB2->ptr;
+  }
+  auto B = std::make_unique<HeffBatch>();
+  B->use_graph = use_graph;
+  return build_batch(ctx, std::move(B), ch, S, nullptr);
 }
 
 void HeffBatch::run_launches() {

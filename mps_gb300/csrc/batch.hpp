@@ -47,6 +47,12 @@ std::unique_ptr<HeffBatch> heff_batch_create(Context* ctx, const std::vector<Ten
                                              const std::vector<const DeviceTensor*>& W2,
                                              int precision, bool use_graph);
 
+// The same batch from operators prepared by heff_prepare on the chains' own contexts (same
+// device, same precision; their preparation must have finished): the batch copies their fused
+// constant operands and reads their host task lists, and keeps no reference to them.
+std::unique_ptr<HeffBatch> heff_batch_from_ops(Context* ctx, const std::vector<const HeffOp*>& ops,
+                                               bool use_graph);
+
 // Lowest eigenpair of every chain's H_eff from its start vector, by the thick-restart Lanczos
 // of eigsolve_heff2 run for all chains in lock step: one batched application per Krylov step
 // (a graph replay), and the recurrence (reorthogonalisation dots, vector updates, the projected

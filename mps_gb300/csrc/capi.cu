@@ -780,6 +780,40 @@ int mpsg_heff2_batch_create(mpsg_ctx* ctx, int32_t n, const mpsg_tensor* const* 
   });
 }
 
+int mpsg_heff2_prepare(mpsg_ctx* ctx, const mpsg_tensor* v_like, const mpsg_tensor* envl,
+                       const mpsg_tensor* envr, const mpsg_tensor* w1, const mpsg_tensor* w2,
+                       int32_t precision, mpsg_heff** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    for (const void* p : {(const void*)v_like, (const void*)envl, (const void*)envr,
+                          (const void*)w1, (const void*)w2, (const void*)out})
+      need(p, "argument");
+    auto h = std::make_unique<mpsg_heff>();
+    h->op = mpsg::heff_prepare(&ctx->c, v_like->t.meta, envl->t, envr->t, w1->t, w2->t,
+                               precision);
+    *out = h.release();
+  });
+}
+
+int mpsg_heff2_batch_from(mpsg_ctx* ctx, int32_t n, const mpsg_heff* const* ops,
+                          int32_t use_graph, mpsg_heff_batch** out) {
+  return guarded([&] {
+    need(ctx, "ctx");
+    need(ops, "ops");
+    need(out, "out");
+    if (n < 1) throw mpsg::Error(mpsg::kErrArgument, "a batch needs at least one operator");
+    std::vector<const mpsg::HeffOp*> v;
+    for (int i = 0; i < n; ++i) {
+      need(ops[i], "ops[i]");
+      v.push_back(ops[i]->op.get());
+    }
+    auto h = std::make_unique<mpsg_heff_batch>();
+    h->owner = ctx->owner;
+    h->b = mpsg::heff_batch_from_ops(&ctx->c, v, use_graph != 0);
+    *out = h.release();
+  });
+}
+
 int mpsg_heff2_batch_apply(mpsg_heff_batch* b, const mpsg_tensor* const* v, mpsg_tensor** out) {
   return guarded([&] {
     need(b, "b");

@@ -658,6 +658,25 @@ std::shared_ptr<HeffOp> heff_create(Context* ctx, const TensorMeta& vmeta, const
   return op;
 }
 
+std::shared_ptr<HeffOp> heff_prepare(Context* ctx, const TensorMeta& vmeta,
+                                     const DeviceTensor& envL, const DeviceTensor& envR,
+                                     const DeviceTensor& W1, const DeviceTensor& W2, int precision) {
+  if (precision < 2) throw Error(kErrUnsupported, "a batch runs the split-precision path: precision 2..7");
+  auto op = std::make_shared<HeffOp>();
+  op->ctx = ctx;
+  op->precision = precision;
+  op->vmeta = vmeta;
+  op->batch_only = true;
+  op->ref_flops = applymps2site_flops(ctx, vmeta, envL.meta, envR.meta, W1.meta, W2.meta);
+  HeffParts H = heff_parts(ctx, vmeta, envL, envR, W1, W2, precision);
+  op->plans = H.plans;
+  op->plan_key = H.key;
+  op->fusedA1 = alloc_buffer(ctx, op->plans->c1->host->fa.out.total);
+  op->fusedB2 = alloc_buffer(ctx, op->plans->c2->host->fb.out.total);
+  heff_fold(ctx, H, envL, envR, W1, W2, op->fusedA1->ptr, op->fusedB2->ptr);
+  return op;
+}
+
 HeffOp::~HeffOp() { heff_plans_return(ctx, plan_key, plans); }
 
 DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v) {
@@ -665,6 +684,7 @@ DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v) {
   if (!same_meta(v.meta, op.vmeta))
     throw Error(kErrSpaceMismatch, "H_eff applied to a tensor of another structure");
   if (op.precision == 0) return applymps2site(ctx, v, op.envL, op.envR, op.W1, op.W2, 0);
+  if (op.batch_only) throw Error(kErrUnsupported, "operator prepared for a batch only");
   const int S = op.precision;
   // X = envLW . v
   DevContract& c1 = *op.plans->c1;

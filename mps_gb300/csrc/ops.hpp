@@ -80,6 +80,9 @@ struct HeffOp {
   std::shared_ptr<HeffPlans> plans;  // precision >= 2
   std::string plan_key;
   std::shared_ptr<Buffer> fusedA1, fusedB2;
+  // prepared for a batch (heff_prepare): the FP64 fused constant operands kept, no split plans
+  // of its own; it cannot be applied alone
+  bool batch_only = false;
   double ref_flops = 0;  // algorithmic flops of the reference contraction order
   // algorithmic bytes per application (precision >= 2): block-permute copies (8 read + 8 written
   // per element) and operand packing (exponent pass 8 read, slice pass 8 read + 2 S written)
@@ -137,6 +140,11 @@ DeviceTensor applymps2site_host(Context* ctx, const DeviceTensor& v, const Devic
                                 const DeviceTensor& W2, const double* const host_in[5],
                                 int precision, double* host_out);
 DeviceTensor heff_apply(HeffOp& op, const DeviceTensor& v);
+// The part of a batched H_eff that belongs to one chain, done on that chain's context: plans,
+// and the W folds into FP64 fused operands kept in the operator (batch_only).
+std::shared_ptr<HeffOp> heff_prepare(Context* ctx, const TensorMeta& vmeta,
+                                     const DeviceTensor& envL, const DeviceTensor& envR,
+                                     const DeviceTensor& W1, const DeviceTensor& W2, int precision);
 
 // One host<->device copy on the context's copy stream, started after the work queued so far on
 // the context stream. It holds the tensor's device buffer, so the tensor may be released at once;

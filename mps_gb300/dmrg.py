@@ -516,8 +516,9 @@ def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, device: int = 0
                         wait_all: bool = True):
     """2-site DMRG on independent chains (L, Delta, maxdim) with batched eigensolves. Every
     chain runs its sweeps on its own context and host thread (as ``run_chains``), as a
-    ``sweep_steps`` generator; its eigensolve requests go to one batcher, which answers all
-    requests waiting at that moment with ONE batched Lanczos on its own context (``HeffBatch``:
+    ``sweep_steps`` generator, and prepares its share of each eigensolve there (host planning
+    and W folds, ``Heff2.prepare``); one batcher answers all requests waiting at that moment
+    with ONE batched Lanczos on its own context (``HeffBatch.from_prepared``:
     every Krylov application one grouped launch per phase for all those chains, replayed from a
     CUDA graph, split GEMMs with tuned tiles; FP64 recurrences). With ``wait_all`` the batcher
     waits until every chain still sweeping has a request (lock step); otherwise it takes what is
@@ -533,6 +534,7 @@ def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, device: int = 0
     bctx = mg.Context(device)
     cv = threading.Condition()
     waiting, answers = {}, {}
+    release = []  # the batcher's vectors, dropped by the batcher between its own launches
     active = set(range(n))
     results = [None] * n
     failed = []
@@ -552,16 +554,22 @@ def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, device: int = 0
             req = next(gen)
             while True:
                 AA, l = req
+                # this chain's share of the batch (host planning and W folds) on its own context
+                op = mg.Heff2.prepare(AA, env[l - 1], env[l + 2], Ws[l - 1], Ws[l],
+                                      precision=opts.precision)
                 ctx.synchronize()  # the batcher's stream reads these tensors
                 with cv:
-                    waiting[i] = (AA, env[l - 1], env[l + 2], Ws[l - 1], Ws[l])
+                    waiting[i] = (op, AA)
                     cv.notify_all()
                     cv.wait_for(lambda: i in answers or failed)
                     if failed:
                         return
                     v = answers.pop(i)
+                del op
                 vec = mg.copy(v, ctx)
-                ctx.synchronize()  # before the batcher's vector is released
+                ctx.synchronize()
+                with cv:  # freed on the batcher's stream: only the batcher may release it
+                    release.append(v)
                 del v
                 try:
                     req = gen.send(vec)
@@ -587,15 +595,16 @@ def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, device: int = 0
                         return
                     batch = dict(waiting)
                     waiting.clear()
+                    release.clear()
                 ids = sorted(batch)
                 for k in range(0, len(ids), max_batch):
                     part = ids[k:k + max_batch]
                     t0 = time.perf_counter()
-                    B = mg.HeffBatch([batch[i] for i in part], precision=opts.precision,
-                                     graph=graph, ctx=bctx)
-                    bctx.synchronize()
+                    B = mg.HeffBatch.from_prepared([batch[i][0] for i in part], bctx,
+                                                   graph=graph)
+                    bctx.synchronize()  # the chains' operators may go once this is done
                     t1 = time.perf_counter()
-                    _, vecs, _ = B.eigsolve([batch[i][0] for i in part],
+                    _, vecs, _ = B.eigsolve([batch[i][1] for i in part],
                                             krylovdim=opts.krylovdim,
                                             maxiter=opts.krylovmaxiter, tol=opts.lanczostol)
                     del B

@@ -653,6 +653,19 @@ class Heff2:
         self.ctx = v_like.ctx
         self._free = _lib.lib.mpsg_heff2_free
 
+    @classmethod
+    def prepare(cls, v_like, envL, envR, W1, W2, precision=4):
+        """One chain's share of a ``HeffBatch`` prepared on that chain's context (plans and the
+        FP64 W folds): usable only in ``HeffBatch.from_prepared``."""
+        self = cls.__new__(cls)
+        h = C.c_void_p()
+        call("mpsg_heff2_prepare", v_like.ctx.handle, v_like.handle, envL.handle, envR.handle,
+             W1.handle, W2.handle, int(precision), C.byref(h))
+        self._h = h
+        self.ctx = v_like.ctx
+        self._free = _lib.lib.mpsg_heff2_free
+        return self
+
     def __call__(self, v) -> SymTensor:
         h = C.c_void_p()
         call("mpsg_heff2_apply", self.ctx.handle, self._h, v.handle, C.byref(h))
@@ -839,6 +852,24 @@ class HeffBatch:
              int(bool(graph)), C.byref(h))
         self._h = h
         self._free = _lib.lib.mpsg_heff2_batch_free
+
+    @classmethod
+    def from_prepared(cls, ops, ctx, graph=True):
+        """The batch of operators from ``Heff2.prepare`` (on any contexts of ``ctx``'s device,
+        their contexts synchronised), assembled and run on ``ctx``; the operators may be
+        released once this returns."""
+        ops = list(ops)
+        if not ops:
+            raise MPSGError(_lib.ERR_ARGUMENT, "a batch needs at least one operator")
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.n = len(ops)
+        h = C.c_void_p()
+        call("mpsg_heff2_batch_from", ctx.handle, self.n,
+             (C.c_void_p * self.n)(*[o._h for o in ops]), int(bool(graph)), C.byref(h))
+        self._h = h
+        self._free = _lib.lib.mpsg_heff2_batch_free
+        return self
 
     def __call__(self, vs):
         """[H_eff_i(v_i)] in one batched application."""

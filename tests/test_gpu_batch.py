@@ -51,6 +51,29 @@ def test_batch_apply_equals_single_operators(graph):
     assert runs + hits >= 2  # both GEMM stages went through the tuner
 
 
+def test_batch_from_operators_prepared_on_other_contexts():
+    """Each chain prepares its share on its own context; the batch is assembled and applied on a
+    third context (the chains' operators released right after assembly)."""
+    shapes = SHAPES[:3]
+    ctxs = [mg.Context(0) for _ in shapes]
+    ops = [_ops(c, [shp])[0] for c, shp in zip(ctxs, shapes)]
+    prepared = [mg.Heff2.prepare(*op, precision=4) for op in ops]
+    with pytest.raises(mg.MPSGError):
+        prepared[0](ops[0][0])  # a prepared share cannot be applied alone
+    for c in ctxs:
+        c.synchronize()
+    bctx = mg.Context(0)
+    B = mg.HeffBatch.from_prepared(prepared, bctx)
+    bctx.synchronize()
+    del prepared
+    for rep in range(3):
+        got = B([op[0] for op in ops])
+        bctx.synchronize()
+        for op, g, shp in zip(ops, got, shapes):
+            single = mg.Heff2(*op, precision=4)(op[0]).to_flat()
+            assert relerr(g.to_flat(), single) < 1e-12, (rep, shp)
+
+
 def test_batch_apply_on_new_inputs():
     """The graph reads the batch's input buffer: new vectors give new results."""
     ctx = mg.Context(0)
