@@ -667,8 +667,9 @@ def run_gradient(args):
 def run_cylinder(args):
     """2-site DMRG on the J1 Heisenberg cylinder (width 6, length 24, periodic around the
     circumference, column-major sites; MPO from the lattice generator, 20-26 channels) at
-    maxdim chi from a random binomial-profile MPS: wall time of each mixed sweep (Krylov 4
-    slices, energy/environments 7 slices, density-matrix truncation) and the energies."""
+    maxdim chi from a random binomial-profile MPS: wall time of each mixed sweep (the sweep
+    bench's mixed configuration) and the energies; a line per sweep goes to stderr as it ends.
+    ``--compare-fp64`` repeats the last sweep as the FP64 drop-in from the same state."""
     import mps_gb300 as mg
     from mps_gb300 import dmrg as gd
     from mps_gb300 import lattice as lt
@@ -685,8 +686,10 @@ def run_cylinder(args):
     ctx.synchronize()
     t_init = time.perf_counter() - t0
     times, energies, matvecs = [], [], []
-    kw = dict(maxdim=chi, tol=1e-10, lanczostol=1e-7, krylovdim=4, krylovmaxiter=8)
+    kw = dict(maxdim=chi, tol=1e-10, lanczostol=1e-7, krylovdim=4, krylovmaxiter=8,
+              tieband=SWEEP_TIEBAND)
     compare = None
+    print(json.dumps({"init_s": t_init}), file=sys.stderr, flush=True)
     for k in range(args.sweeps):
         saved = None
         if args.compare_fp64 and k == args.sweeps - 1:  # the state the last sweep starts from
@@ -699,6 +702,8 @@ def run_cylinder(args):
         times.append(time.perf_counter() - t0)
         energies.append(es[-1])
         matvecs.append(sum(i.numops for i in stats))
+        print(json.dumps({"sweep": k + 1, "s": times[-1], "energy": es[-1],
+                          "energy_per_site": es[-1] / n}), file=sys.stderr, flush=True)
         if saved is not None:
             m64 = gd.MPState(saved[0], center=1)
             e64_env = saved[1]
@@ -715,6 +720,9 @@ def run_cylinder(args):
                        "dE_final": de[-1], "dE_max_over_sweep": max(de),
                        "dE_rel_max_over_sweep": max(de) / abs(e64[-1]),
                        "energies_compared": len(de), "fp64_config": SWEEP_FP64}
+            print(json.dumps({"fp64_sweep_s": t64, **{k_: v_ for k_, v_ in compare.items()
+                                                      if k_ != "fp64_config"}}),
+                  file=sys.stderr, flush=True)
             del m64, e64_env
     line = {
         "metric": "DMRG sweep s, J1 Heisenberg 6x24 cylinder", "value": times[-1], "unit": "s",
