@@ -97,6 +97,8 @@ def parse(argv=None):
                         "Delta derivative of a two-point function by central differences")
     p.add_argument("--tdvp-lx", type=int, default=32)
     p.add_argument("--tdvp-steps", type=int, default=10)
+    p.add_argument("--tdvp-no-fd", action="store_true",
+                   help="--tdvp: skip the finite-difference evolutions")
     p.add_argument("--tdvp-precision", type=int, default=0,
                    help="block-GEMM arithmetic of the TDVP contractions (0 = FP64, S = slices)")
     return p.parse_args(argv)
@@ -862,8 +864,10 @@ def run_tdvp(args):
     an XXZ chain (Delta = 0.5) from a seeded random U(1) MPS with a binomial bond profile of
     about chi states, on complex block-sparse tensors (two real parts, GPU contractions,
     per-sector complex SVD gauge moves). Reports seconds per sweep, norm and energy drift, and
-    C(t) = <Sz_i Sz_{i+1}>(t) (i = L/2) with dC/dDelta by central differences (h = 1e-5): three
-    evolutions under H(Delta), H(Delta +- h) from the same state."""
+    C(t) = <Sz_i Sz_{i+1}>(t) (i = L/2) with dC/dDelta twice: by forward-mode tangents through
+    the sweeps (one evolution carrying derivatives, ``mps_gb300.tdvp_grad``) and by central
+    differences (h = 1e-5: evolutions under H(Delta +- h) from the same state; off with
+    --tdvp-no-fd)."""
     import numpy as np
     import mps_gb300 as mg
     from mps_gb300 import ctensor as ct
@@ -902,8 +906,31 @@ def run_tdvp(args):
         return out
 
     r0 = evolve(delta, True)
-    rp = evolve(delta + h, False)
-    rm = evolve(delta - h, False)
+    print(json.dumps({"forward_s": sum(r0["sweep_s"]), "C": r0["C"]}), file=sys.stderr,
+          flush=True)
+    # the derivative by tangents through the same sweeps
+    from mps_gb300 import tdvp_grad as tg
+    mps = gd.mps_from_host(host, ctx)
+    gd.center_at(mps, 1)
+    mg.rmul(mps.As[0], 1.0 / mg.norm(mps.As[0]))
+    Ws = gd.xxz_u1mpo(lx, delta, ctx=ctx)
+    dWs = [ops.lincomb([(1.0, a), (-1.0, b)])
+           for a, b in zip(gd.xxz_u1mpo(lx, 1.0, ctx=ctx), gd.xxz_u1mpo(lx, 0.0, ctx=ctx))]
+    As = [ct.CTensor(A) for A in mps.As]
+    tstats = tg.TangentStats()
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    c_t, dc_t = tg.evolve_with_tangent(ops, As, Ws, dWs, dt, steps, {i: sz, i + 1: sz},
+                                       stats=tstats)
+    ctx.synchronize()
+    tangent_s = time.perf_counter() - t0
+    print(json.dumps({"tangent_s": tangent_s, "dC": dc_t.real}), file=sys.stderr, flush=True)
+    del As, mps
+    fd = None
+    if not args.tdvp_no_fd:
+        rp = evolve(delta + h, False)
+        rm = evolve(delta - h, False)
+        fd = (rp["C"] - rm["C"]) / (2 * h)
     line = {
         "metric": "1-site TDVP sweep s (complex U(1) MPS)", "value": float(np.median(r0["sweep_s"])),
         "unit": "s", "higher_is_better": False, "n_gpus": 1,
@@ -913,7 +940,12 @@ def run_tdvp(args):
                                "Krylov tol 1e-12, dim <= 30",
                    "dtype": "complex f64" + (f" via {args.tdvp_precision} bf16 slices"
                                              if args.tdvp_precision else "")},
-        "t": 2 * dt * steps, "C_t": r0["C"], "dC_dDelta_fd": (rp["C"] - rm["C"]) / (2 * h),
+        "t": 2 * dt * steps, "C_t": r0["C"],
+        "dC_dDelta_tangent": dc_t.real, "dC_dDelta_fd": fd,
+        "rel_diff_tangent_vs_fd": abs(dc_t.real - fd) / abs(fd) if fd else None,
+        "C_t_tangent_run": c_t.real, "tangent_evolution_s": tangent_s,
+        "forward_evolution_s": sum(r0["sweep_s"]),
+        "tangent_matvecs": tstats.matvecs, "tangent_unconverged": tstats.unconverged,
         "norm_drift": r0["norm_drift"], "energy_drift": r0["energy_drift"],
         "matvecs_per_sweep": r0["matvecs"] / steps, "unconverged_exponentials": r0["unconverged"],
         "sweep_s": r0["sweep_s"],

@@ -1,0 +1,369 @@
+"""Derivatives of TDVP-evolved observables with respect to a Hamiltonian coupling.
+
+The reference evolves MPS with the time-dependent variational principle (src/tdvp.jl:12-89);
+config 5 asks for d<Sz_i Sz_j>(t)/dDelta after 1-site TDVP. A single scalar parameter is a
+forward-mode (tangent) derivative: every quantity of the sweep in ``mps_gb300.tdvp`` carries
+its derivative with respect to the coupling, propagated through each step by the chain rule,
+so one tangent sweep costs a fixed multiple of a plain sweep and stores nothing beyond the
+current state and environments (no tape, no recomputation). The result is the exact
+derivative of the discrete algorithm's output (up to the Krylov tolerances).
+
+Steps and their tangents (``d`` = derivative with respect to the coupling, W the MPO, dW its
+derivative, H_eff built from the environments L, R and W):
+
+* Krylov exponential x' = exp(t F) x with F Hermitian and dF its derivative (the H_eff built with
+  one of dL, dR, dW in place of L, R, W). The derivative of exp(t F) x in the direction dF is the
+  top block of exp(t M) [dx; x] for the block-triangular M = [[F, dF], [0, F]]; M is not
+  Hermitian, so ``exponentiate_tangent`` runs Arnoldi with full reorthogonalisation on pairs of
+  tensors and exponentiates the small Hessenberg matrix on the host, with the error estimate
+  and step halving of ``ctensor.exponentiate``. The value x' itself comes from the plain
+  Lanczos exponential, so the forward state is the one ``tdvp1sitesweep`` computes.
+* Gauge move M = Q lam (per-sector SVD, Q = u isometric, lam = s v): the tangent with
+  Q^H dQ = 0, i.e. dQ = (1 - Q Q^H) dM v^H s^-1 and dlam = Q^H dM (right-to-left: M = lam Q,
+  dlam = dM Q^H, dQ = s^-1 u^H dM (1 - Q^H Q)). Any other choice differs by a gauge
+  transformation of the MPS, which TDVP carries covariantly and no observable sees.
+* Environments: the four-term product rule over (environment, ket, MPO, bra) of
+  ``_mpsupdateleft`` / ``_mpsupdateright`` (src/apply.jl:17-58).
+* Observables: <psi|O|psi> / <psi|psi> by transfer matrices with their tangents.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .ctensor import (CTensor, Ops, cdual, ccontract, cdots, cfuselegs, clincomb,
+                      cmatmul_real, cmatmul_real_right, cnorm, cscale, cspace, csplitleg, csvd,
+                      cdownload, creal, exponentiate)
+from .tdvp import TURNING, _transfer, apply0, apply1
+
+
+# ---------------------------------------------------------------------------------------------
+# small helpers: None stands for a zero tangent
+# ---------------------------------------------------------------------------------------------
+def _sum(ops: Ops, terms):
+    """sum of (coefficient, CTensor or None) terms; None when every term is None."""
+    terms = [(z, X) for z, X in terms if X is not None]
+    if not terms:
+        return None
+    if len(terms) == 1 and terms[0][0] == 1.0:
+        return terms[0][1]
+    return clincomb(ops, terms)
+
+
+def _diag_inverse(ops: Ops, s):
+    """The inverse of the SVD's real diagonal s as a map back: legs (dual(s_2), dual(s_1)),
+    block (c2, c1) = diag(1 / s_(c1, c2)) (zero where s is zero: a pseudo-inverse), so that
+    X * s^-1 contracts with a leg s_2 and s^-1 * Y with a leg s_1. Blocks of s are the diagonals
+    (1-d) or dense square blocks."""
+    blocks = {}
+    for key, b in s.blocks.items():
+        b = np.asarray(b, dtype=np.float64)
+        d = b if b.ndim == 1 else np.diagonal(b)
+        inv = np.where(d != 0.0, 1.0 / np.where(d != 0.0, d, 1.0), 0.0)
+        blocks[(key[1], key[0])] = np.diag(inv)
+    V1, V2 = ops.space(s)
+    return ops.from_blocks(s.charge, (ops.dual_space(V2), ops.dual_space(V1)), blocks)
+
+
+def _mm(ops, X, Y):
+    """Matrix product X * Y of complex rank-2 tensors (last leg of X with first of Y)."""
+    return ccontract(ops, X, (1, -1), Y, (-1, 2))
+
+
+def _dag_mm(ops, X, Y):
+    """X^H * Y (first legs contracted, X conjugated)."""
+    return ccontract(ops, cdual(ops, X), (-1, 1), Y, (-1, 2))
+
+
+def _mm_dag(ops, X, Y):
+    """X * Y^H (last legs contracted, Y conjugated)."""
+    return ccontract(ops, X, (1, -1), cdual(ops, Y), (2, -1))
+
+
+def updateleft4(ops: Ops, env, Aket, W, Abra):
+    """``_mpsupdateleft`` (src/apply.jl:49-58) with separate ket and bra site tensors."""
+    t = ccontract(ops, env, (-1, 3, 4), Aket, (-1, 2, 1))
+    t = ccontract(ops, t, (1, -1, -2, 4), W, (-2, 2, 3, -1))
+    return ccontract(ops, t, (1, -1, 2, -2), cdual(ops, Abra), (-2, -1, 3))
+
+
+def updateright4(ops: Ops, env, Aket, W, Abra):
+    """``_mpsupdateright`` (src/apply.jl:17-25) with separate ket and bra site tensors."""
+    t = ccontract(ops, env, (-1, 3, 4), Aket, (1, 2, -1))
+    t = ccontract(ops, t, (1, -1, -2, 4), W, (3, 2, -2, -1))
+    return ccontract(ops, t, (1, -1, 2, -2), cdual(ops, Abra), (3, -1, -2))
+
+
+def _env_tangent(ops, upd, env, denv, A, dA, W, dW):
+    """Product rule of an environment update over (environment, ket, MPO, bra)."""
+    return _sum(ops, [
+        (1.0, None if denv is None else upd(ops, denv, A, W, A)),
+        (1.0, None if dA is None else upd(ops, env, dA, W, A)),
+        (1.0, None if dW is None else upd(ops, env, A, dW, A)),
+        (1.0, None if dA is None else upd(ops, env, A, W, dA))])
+
+
+# ---------------------------------------------------------------------------------------------
+# the derivative of a Krylov exponential
+# ---------------------------------------------------------------------------------------------
+def _pair_dots(ops, V, w):
+    a = cdots(ops, [v[0] for v in V], w[0])
+    b = cdots(ops, [v[1] for v in V], w[1])
+    return [x + y for x, y in zip(a, b)]
+
+
+def _pair_comb(ops, terms):
+    return (clincomb(ops, [(z, p[0]) for z, p in terms]),
+            clincomb(ops, [(z, p[1]) for z, p in terms]))
+
+
+def _pair_norm(ops, p):
+    return float(np.hypot(cnorm(ops, p[0]), cnorm(ops, p[1])))
+
+
+def exponentiate_tangent(ops: Ops, f, df, t, x, dx, krylovdim: int = 30, tol: float = 1e-12,
+                         maxiter: int = 100):
+    """d/dp [exp(t F(p)) x(p)] = the top block of exp(t M) [dx; x], M = [[F, dF], [0, F]]
+    (f applies F, df applies dF, dx may be None for a constant x): Arnoldi with classical
+    Gram-Schmidt applied twice on pairs of complex tensors, exp of the Hessenberg matrix on the
+    host (scipy), a-posteriori error h_{m+1,m} |e_m^T exp(tau t H_m) e_1| |[dx; x]| per step
+    and step halving when the basis cannot reach tol. Returns (tangent, numops, converged)."""
+    from scipy.linalg import expm
+    if dx is None:
+        dx = cscale(ops, x, 0.0)
+    v = (dx, x)
+    scale = _pair_norm(ops, v)
+    if scale == 0.0:
+        return dx, 0, True
+    v = _pair_comb(ops, [(1.0 / scale, v)])
+
+    def M(p):
+        fx, fy = f(p[0]), f(p[1])
+        return (clincomb(ops, [(1.0, fx), (1.0, df(p[1]))]), fy)
+
+    left = 1.0
+    numops = steps = 0
+    converged = True
+    y = v
+    while left > 0.0 and steps < maxiter:
+        steps += 1
+        V = [v]
+        H = np.zeros((krylovdim + 1, krylovdim), dtype=complex)
+        step = None
+        c = None
+        for j in range(krylovdim):
+            w = M(V[j])
+            numops += 1
+            for _ in range(2):
+                coef = _pair_dots(ops, V, w)
+                H[:j + 1, j] += coef
+                w = _pair_comb(ops, [(1.0, w)] + [(-cu, u) for cu, u in zip(coef, V)])
+            b = _pair_norm(ops, w)
+            m = j + 1
+            tau = left
+            E = expm(tau * t * H[:m, :m])
+            c = E[:, 0]
+            err = b * abs(c[m - 1]) * scale
+            if err <= tol or b <= 1e-14 * max(1.0, abs(H[j, j])):
+                step = tau
+                break
+            if m == krylovdim:
+                while err > tol and tau > 1e-6 * left:
+                    tau *= 0.5
+                    c = expm(tau * t * H[:m, :m])[:, 0]
+                    err = b * abs(c[m - 1]) * scale
+                if err > tol:
+                    converged = False
+                step = tau
+                break
+            H[j + 1, j] = b
+            V.append(_pair_comb(ops, [(1.0 / b, w)]))
+        y = _pair_comb(ops, [(complex(c[i]) * scale, V[i]) for i in range(len(c))])
+        left = left - step if step < left else 0.0
+        scale = _pair_norm(ops, y)
+        v = _pair_comb(ops, [(1.0 / scale, y)])
+    if left > 0.0:
+        converged = False
+    return y[0], numops, converged
+
+
+class TangentStats:
+    def __init__(self):
+        self.exponentials = 0
+        self.matvecs = 0
+        self.unconverged = 0
+
+    def add(self, numops, converged):
+        self.exponentials += 1
+        self.matvecs += numops
+        self.unconverged += 0 if converged else 1
+
+
+def _expo_pair(ops, f, df, t, x, dx, krylovdim, tol, stats):
+    """(exp(t F) x by the plain Lanczos exponential, its tangent)."""
+    y, info = exponentiate(ops, f, t, x, krylovdim=krylovdim, tol=tol)
+    dy, nops, ok = exponentiate_tangent(ops, f, df, t, x, dx, krylovdim=krylovdim, tol=tol)
+    if stats is not None:
+        stats.add(info.numops + nops, info.converged and ok)
+    return y, dy
+
+
+def _h1_tangent(ops, L, dL, R, dR, W, dW):
+    """x -> dH_eff x for the 1-site H_eff (src/apply.jl:70-78)."""
+    def df(x):
+        return _sum(ops, [(1.0, None if dL is None else apply1(ops, x, dL, R, W)),
+                          (1.0, None if dR is None else apply1(ops, x, L, dR, W)),
+                          (1.0, None if dW is None else apply1(ops, x, L, R, dW))]) or \
+            cscale(ops, x, 0.0)
+    return df
+
+
+def _h0_tangent(ops, L, dL, R, dR):
+    """x -> dH_eff x for the 0-site H_eff (src/apply.jl:2-7)."""
+    def df(x):
+        return _sum(ops, [(1.0, None if dL is None else apply0(ops, x, dL, R)),
+                          (1.0, None if dR is None else apply0(ops, x, L, dR))]) or \
+            cscale(ops, x, 0.0)
+    return df
+
+
+# ---------------------------------------------------------------------------------------------
+# environments, sweeps, observables
+# ---------------------------------------------------------------------------------------------
+def initialenv_tangent(ops: Ops, As, dAs, Ws, dWs, env):
+    """Tangents of the environments built by ``tdvp.initialenv`` (right environments from the
+    right end; the boundary ones are constant)."""
+    lx = len(As)
+    denv = [None] * (lx + 2)
+    for l in range(lx, 0, -1):
+        denv[l] = _env_tangent(ops, updateright4, env[l + 1], denv[l + 1], As[l - 1],
+                               dAs[l - 1], Ws[l - 1], dWs[l - 1])
+    return denv
+
+
+def tdvp1sitesweep_tangent(ops: Ops, dt: float, As, dAs, Ws, dWs, env, denv,
+                           turning: str = "reference", krylovdim: int = 30, tol: float = 1e-12,
+                           stats: TangentStats | None = None):
+    """``tdvp.tdvp1sitesweep`` (src/tdvp.jl:12-89) with every site tensor and environment
+    carrying its derivative with respect to the coupling (``dAs``, ``denv``: lists of CTensor
+    or None; ``dWs``: the MPO's derivative, real tensors or None). All four lists are updated
+    in place; the state is the plain sweep's."""
+    if turning not in TURNING:
+        raise ValueError(f"turning must be one of {TURNING}")
+    lx = len(As)
+    As[:] = [creal(A) for A in As]
+    A, dA = As[0], dAs[0]
+    for l in range(1, lx):
+        L, R = env[l - 1], env[l + 1]
+        A, dA = _expo_pair(ops, lambda v: apply1(ops, v, L, R, Ws[l - 1]),
+                           _h1_tangent(ops, L, denv[l - 1], R, denv[l + 1], Ws[l - 1],
+                                       dWs[l - 1]), -1j * dt, A, dA, krylovdim, tol, stats)
+        M = cfuselegs(ops, A, 1, 2)
+        u, s, v = csvd(ops, M)  # as _pushright!, src/symmps.jl:176-183
+        sp = cspace(ops, A)[0:2]
+        Q = csplitleg(ops, u, 1, sp)
+        lam = cmatmul_real(ops, s, v)
+        dQ = dlam = None
+        if dA is not None:
+            dM = cfuselegs(ops, dA, 1, 2)
+            Y = cmatmul_real_right(ops, _mm_dag(ops, dM, v), _diag_inverse(ops, s))
+            dQf = clincomb(ops, [(1.0, Y), (-1.0, _mm(ops, u, _dag_mm(ops, u, Y)))])
+            dQ = csplitleg(ops, dQf, 1, sp)
+            dlam = _dag_mm(ops, u, dM)
+        As[l - 1], dAs[l - 1] = Q, dQ
+        env[l] = updateleft4(ops, env[l - 1], Q, Ws[l - 1], Q)
+        denv[l] = _env_tangent(ops, updateleft4, env[l - 1], denv[l - 1], Q, dQ, Ws[l - 1],
+                               dWs[l - 1])
+        L0, R0 = env[l], env[l + 1]
+        lam, dlam = _expo_pair(ops, lambda x: apply0(ops, x, L0, R0),
+                               _h0_tangent(ops, L0, denv[l], R0, denv[l + 1]), 1j * dt, lam,
+                               dlam, krylovdim, tol, stats)
+        A = ccontract(ops, lam, (1, -1), As[l], (-1, 2, 3))
+        dA = _sum(ops, [(1.0, None if dlam is None else ccontract(ops, dlam, (1, -1), As[l],
+                                                                   (-1, 2, 3))),
+                        (1.0, None if dAs[l] is None else ccontract(ops, lam, (1, -1), dAs[l],
+                                                                     (-1, 2, 3)))])
+    t_turn = 2.0 * dt if turning == "symmetric" else dt
+    L, R = env[lx - 1], env[lx + 1]
+    A, dA = _expo_pair(ops, lambda v: apply1(ops, v, L, R, Ws[lx - 1]),
+                       _h1_tangent(ops, L, denv[lx - 1], R, denv[lx + 1], Ws[lx - 1],
+                                   dWs[lx - 1]), -1j * t_turn, A, dA, krylovdim, tol, stats)
+    for l in range(lx - 1, 0, -1):
+        M = cfuselegs(ops, A, 2, 2)
+        u, s, v = csvd(ops, M)  # as _pushleft!, src/symmps.jl:167-174
+        sp = cspace(ops, A)[1:3]
+        Q = csplitleg(ops, v, 2, sp)
+        lam = cmatmul_real_right(ops, u, s)
+        dQ = dlam = None
+        if dA is not None:
+            dM = cfuselegs(ops, dA, 2, 2)
+            dlam = _mm_dag(ops, dM, v)
+            Y = cmatmul_real(ops, _diag_inverse(ops, s), _dag_mm(ops, u, dM))
+            dQf = clincomb(ops, [(1.0, Y), (-1.0, _mm(ops, _mm_dag(ops, Y, v), v))])
+            dQ = csplitleg(ops, dQf, 2, sp)
+        As[l], dAs[l] = Q, dQ
+        env[l + 1] = updateright4(ops, env[l + 2], Q, Ws[l], Q)
+        denv[l + 1] = _env_tangent(ops, updateright4, env[l + 2], denv[l + 2], Q, dQ, Ws[l],
+                                   dWs[l])
+        L0, R0 = env[l], env[l + 1]
+        lam, dlam = _expo_pair(ops, lambda x: apply0(ops, x, L0, R0),
+                               _h0_tangent(ops, L0, denv[l], R0, denv[l + 1]), 1j * dt, lam,
+                               dlam, krylovdim, tol, stats)
+        A = ccontract(ops, As[l - 1], (1, 2, -1), lam, (-1, 3))
+        dA = _sum(ops, [(1.0, None if dlam is None else ccontract(ops, As[l - 1], (1, 2, -1),
+                                                                   dlam, (-1, 3))),
+                        (1.0, None if dAs[l - 1] is None else ccontract(ops, dAs[l - 1],
+                                                                         (1, 2, -1), lam,
+                                                                         (-1, 3)))])
+        L, R = env[l - 1], env[l + 1]
+        A, dA = _expo_pair(ops, lambda x: apply1(ops, x, L, R, Ws[l - 1]),
+                           _h1_tangent(ops, L, denv[l - 1], R, denv[l + 1], Ws[l - 1],
+                                       dWs[l - 1]), -1j * dt, A, dA, krylovdim, tol, stats)
+    As[0], dAs[0] = A, dA
+    return As, dAs, env, denv
+
+
+def _transfer_bra_ket(ops: Ops, L, Abra, Aket, op=None):
+    """L <- L . conj(Abra) [. op] . Aket (``tdvp._transfer`` with separate bra and ket)."""
+    t = ccontract(ops, L, (-1, 1), cdual(ops, Abra), (-1, 2, 3))
+    if op is not None:
+        t = ccontract(ops, t, (1, -1, 3), op, (-1, 2))
+    return ccontract(ops, t, (-1, -2, 1), Aket, (-1, -2, 2))
+
+
+def expectation_tangent(ops: Ops, As, dAs, site_ops: dict):
+    """(<psi|O|psi> / <psi|psi>, its derivative) for O = prod_x site_ops[x] (1-based sites)."""
+    V0 = cspace(ops, As[0])[0]
+    L0 = CTensor(ops.fill(1.0, 0, (V0, ops.dual_space(V0))))
+    L, N, dL, dN = L0, L0, None, None
+    for x, (A, dA) in enumerate(zip(As, dAs), start=1):
+        op = site_ops.get(x)
+        nL = _transfer(ops, L, A, op)
+        nN = _transfer(ops, N, A)
+        dL = _sum(ops, [(1.0, None if dL is None else _transfer(ops, dL, A, op)),
+                        (1.0, None if dA is None else _transfer_bra_ket(ops, L, A, dA, op)),
+                        (1.0, None if dA is None else _transfer_bra_ket(ops, L, dA, A, op))])
+        dN = _sum(ops, [(1.0, None if dN is None else _transfer(ops, dN, A)),
+                        (1.0, None if dA is None else _transfer_bra_ket(ops, N, A, dA)),
+                        (1.0, None if dA is None else _transfer_bra_ket(ops, N, dA, A))])
+        L, N = nL, nN
+    total = lambda T: 0.0 if T is None else complex(cdownload(ops, T).sum())
+    num, den = total(L), total(N)
+    dnum, dden = total(dL), total(dN)
+    return num / den, (dnum * den - num * dden) / den ** 2
+
+
+def evolve_with_tangent(ops: Ops, As, Ws, dWs, dt: float, sweeps: int, site_ops: dict,
+                        turning: str = "symmetric", krylovdim: int = 30, tol: float = 1e-12,
+                        stats: TangentStats | None = None):
+    """Evolve the center-1 MPS ``As`` (list of CTensor, modified in place) by ``sweeps`` 1-site
+    TDVP sweeps of dt under the MPO Ws, carrying tangents with respect to the coupling whose
+    MPO derivative is dWs (the initial state does not depend on it). Returns (<O>(t),
+    d<O>(t)/dp) for O = prod site_ops."""
+    from .tdvp import initialenv
+    env = initialenv(ops, As, Ws)
+    dAs = [None] * len(As)
+    denv = initialenv_tangent(ops, As, dAs, Ws, dWs, env)
+    for _ in range(sweeps):
+        tdvp1sitesweep_tangent(ops, dt, As, dAs, Ws, dWs, env, denv, turning=turning,
+                               krylovdim=krylovdim, tol=tol, stats=stats)
+    return expectation_tangent(ops, As, dAs, site_ops)

@@ -1,0 +1,122 @@
+"""Coupling derivatives of TDVP-evolved correlators (forward-mode tangents through the 1-site
+sweep, ``mps_gb300.tdvp_grad``) on the CPU, with the oracle's real operations: against central
+finite differences (h = 1e-5) of the same evolution on a truncated chain, and against the exact
+derivative of exp(-iHt) (Frechet derivative of the dense matrix exponential) where 1-site TDVP
+with the symmetric turning point is the exact evolution (full bond dimension)."""
+import numpy as np
+import pytest
+
+from helpers import dense_site, oracle_ops, rand_tensor
+from mps_gb300 import ctensor as ct
+from mps_gb300 import tdvp as td
+from mps_gb300 import tdvp_grad as tg
+from oracle import mps as om
+from oracle import symtensors as st
+from oracle import tdvp as ot
+from oracle.symtensors import U1Space, dual_space
+
+LX, M, DELTA, DT = 8, 4, 0.5, 0.05
+
+
+def random_state(lx, m, chimax, seed):
+    rng = np.random.default_rng(seed)
+    d = U1Space((0, 1), (1, 1))
+    Vl = U1Space((0, 1))
+    As = []
+    for site in range(1, lx + 1):
+        Vr = U1Space(*om.binomial_bond_dims(lx, site, m, chimax))
+        As.append(rand_tensor(0, (Vl, d, dual_space(Vr)), rng))
+        Vl = Vr
+    mps = om.center_at(om.MPState(As, 0), 1)
+    mps.As[0] = st.scaled(mps.As[0], 1.0 / st.norm(mps.As[0]))
+    return mps
+
+
+def mpo_and_derivative(ops, lx, delta):
+    Ws = om.xxz_u1mpo(lx, delta)
+    W1, W0 = om.xxz_u1mpo(lx, 1.0), om.xxz_u1mpo(lx, 0.0)
+    return Ws, [ops.lincomb([(1.0, a), (-1.0, b)]) for a, b in zip(W1, W0)]
+
+
+def correlator(ops, mps, delta, sweeps, sites, turning="symmetric"):
+    Ws = om.xxz_u1mpo(LX, delta)
+    As = [ct.CTensor(A) for A in mps.As]
+    env = td.initialenv(ops, As, Ws)
+    for _ in range(sweeps):
+        td.tdvp1sitesweep(ops, DT, As, Ws, env, turning=turning)
+    sz = td.site_operator(ops, mps.As[0].space[1], {0: -0.5, 1: 0.5})
+    return td.expectation(ops, As, {i: sz for i in sites}).real, As
+
+
+@pytest.mark.parametrize("turning", ["symmetric", "reference"])
+def test_tangent_matches_central_differences_on_a_truncated_chain(turning):
+    ops = oracle_ops()
+    mps = random_state(LX, M, 4, seed=11)
+    sites = (3, 6)
+    Ws, dWs = mpo_and_derivative(ops, LX, DELTA)
+    As = [ct.CTensor(A) for A in mps.As]
+    sz = td.site_operator(ops, mps.As[0].space[1], {0: -0.5, 1: 0.5})
+    c, dc = tg.evolve_with_tangent(ops, As, Ws, dWs, DT, 2, {i: sz for i in sites},
+                                   turning=turning)
+    c0, As0 = correlator(ops, mps, DELTA, 2, sites, turning)
+    # the state carried by the tangent sweep is the plain sweep's
+    for A, B in zip(As, As0):
+        assert np.abs(dense_site(ops, A) - dense_site(ops, B)).max() < 1e-12
+    assert abs(c.real - c0) < 1e-12
+    h = 1e-5
+    fd = (correlator(ops, mps, DELTA + h, 2, sites, turning)[0] -
+          correlator(ops, mps, DELTA - h, 2, sites, turning)[0]) / (2 * h)
+    assert abs(dc.real - fd) <= 1e-6 * abs(fd)
+    assert abs(dc.imag) < 1e-12
+
+
+def test_tangent_equals_the_exact_derivative_at_full_bond_dimension():
+    ops = oracle_ops()
+    from scipy.linalg import expm_frechet
+    mps = random_state(LX, M, 1 << 20, seed=5)
+    sites = (2, 5)
+    sweeps = 3
+    Ws, dWs = mpo_and_derivative(ops, LX, DELTA)
+    As = [ct.CTensor(A) for A in mps.As]
+    psi0 = ot.state_vector([dense_site(ops, A) for A in As])
+    sz = td.site_operator(ops, mps.As[0].space[1], {0: -0.5, 1: 0.5})
+    c, dc = tg.evolve_with_tangent(ops, As, Ws, dWs, DT, sweeps, {i: sz for i in sites})
+    t = 2 * DT * sweeps  # a symmetric sweep is the exact evolution by 2 dt
+    H = om.xxz_hamiltonian(LX, DELTA)
+    dH = om.xxz_hamiltonian(LX, 1.0) - om.xxz_hamiltonian(LX, 0.0)
+    U, dU = expm_frechet(-1j * t * H, -1j * t * dH)
+    psi, dpsi = U @ psi0, dU @ psi0
+    O = np.ones(psi.size)
+    idx = np.arange(psi.size)
+    for i in sites:  # Sz_i diagonal in the computational basis (site i = bit LX - i)
+        O = O * (((idx >> (LX - i)) & 1) - 0.5)
+    want_c = np.vdot(psi, O * psi).real
+    want_dc = 2.0 * np.vdot(psi, O * dpsi).real
+    assert abs(c.real - want_c) < 1e-10
+    assert abs(dc.real - want_dc) < 1e-8 * max(1.0, abs(want_dc))
+
+
+def test_tangent_of_the_exponential_on_its_own():
+    """d/dp exp(t (F + p G)) x at p = 0 against the Frechet derivative of the dense matrix."""
+    from scipy.linalg import expm_frechet
+    ops = oracle_ops()
+    rng = np.random.default_rng(4)
+    V = U1Space((0, 5), (1, 6), (2, 4))
+    fb, gb = {}, {}
+    for c, n in V.sectors:
+        a, b = rng.standard_normal((n, n)), rng.standard_normal((n, n))
+        fb[(c, c)], gb[(c, c)] = a + a.T, b + b.T
+    F = st.from_blocks(0, (dual_space(V), V), fb)
+    G = st.from_blocks(0, (dual_space(V), V), gb)
+    W = (dual_space(U1Space((0, 1))), V)
+    x = ct.CTensor(rand_tensor(0, W, rng), rand_tensor(0, W, rng))
+    f = lambda v: ct.ccontract(ops, v, (1, -1), F, (-1, 2))
+    g = lambda v: ct.ccontract(ops, v, (1, -1), G, (-1, 2))
+    t = -0.3j
+    dy, nops, ok = tg.exponentiate_tangent(ops, f, g, t, x, None, krylovdim=8, tol=1e-12)
+    assert ok
+    Fd, Gd = st.array(F), st.array(G)
+    xd = dense_site(ops, x)[0]
+    _, L = expm_frechet(t * Fd, t * Gd)
+    want = xd @ L  # row vector times the (right-acting) operator
+    assert np.linalg.norm(dense_site(ops, dy)[0] - want) < 1e-11 * np.linalg.norm(want)
