@@ -97,6 +97,10 @@ def parse(argv=None):
                         "Delta derivative of a two-point function by central differences")
     p.add_argument("--tdvp-lx", type=int, default=32)
     p.add_argument("--tdvp-steps", type=int, default=10)
+    p.add_argument("--dense-gemm", type=int, default=0, metavar="N",
+                   help="instead: the split-precision GEMM on one dense N x N x N block "
+                        "(--precision slices, default the headline's), kernel time by CUDA "
+                        "events, algorithmic and executed TFLOP/s against the measured peak")
     p.add_argument("--tdvp-no-fd", action="store_true",
                    help="--tdvp: skip the finite-difference evolutions")
     p.add_argument("--tdvp-precision", type=int, default=0,
@@ -953,6 +957,40 @@ def run_tdvp(args):
     print(json.dumps(line), flush=True)
 
 
+def run_dense_gemm(args):
+    """The split-precision grouped GEMM on a single dense N x N x N problem (one sector): the
+    per-tile pipeline without the ragged work distribution of the sector GEMMs."""
+    import numpy as np
+    import mps_gb300 as mg
+    n = args.dense_gemm
+    S = DEFAULT_SLICES if args.precision is None else args.precision
+    ctx = mg.get_context(0)
+    V = mg.VectorSpace([(0, n)])
+    rng = np.random.default_rng(3)
+    A = mg.from_flat(0, (V, mg.dual(V)), rng.standard_normal(n * n), ctx)
+    B = mg.from_flat(0, (V, mg.dual(V)), rng.standard_normal(n * n), ctx)
+    for _ in range(args.warmup):
+        mg.matmul(A, B, precision=S)
+    ctx.synchronize()
+    ctx.set_timing(True)
+    for _ in range(args.steps):
+        mg.matmul(A, B, precision=S)
+    ctx.synchronize()
+    ms, nl, fl = ctx.kernel_time("gemm_split")
+    ctx.set_timing(False)
+    peaks = measured_peaks()
+    peak = peaks["bf16_tflops"] if peaks else 1900.0
+    tf = fl / (ms / 1e3) / 1e12
+    pairs = S * (S + 1) // 2
+    line = {"metric": "split-precision GEMM on a dense block: algorithmic TFLOP/s", "value": tf,
+            "unit": "TFLOP/s", "higher_is_better": True, "n_gpus": 1,
+            "data": "synthetic (N(0,1) blocks)",
+            "config": {"workload": f"dense {n}^3 block GEMM, {S} bf16 slices"},
+            "ms_per_gemm": ms / max(nl, 1), "launches": nl, "executed_tflops": tf * pairs,
+            "executed_frac_of_measured_bf16_peak": tf * pairs / peak, "peak": peak}
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
@@ -967,5 +1005,7 @@ if __name__ == "__main__":
         run_small_chain(a)
     elif a.tdvp:
         run_tdvp(a)
+    elif a.dense_gemm:
+        run_dense_gemm(a)
     else:
         run_ours(a)
