@@ -325,9 +325,10 @@ int mpsg_heff2_batch_free(mpsg_heff_batch* b);
 int mpsg_ctx_tuner(mpsg_ctx* ctx, int32_t enable, int64_t* runs, int64_t* hits);
 /* Fixes the split-GEMM configuration of plans built from now on in this context: N tile bn (64,
  * 128, or 0 = the kernel's default for the slice count; 128 falls back to the default where it
- * does not fit) and tile order (0 = decreasing K, 1 = problem by problem); bn < 0 returns to the
- * tuner / defaults. For measurements and tests. */
-int mpsg_ctx_set_split_tuning(mpsg_ctx* ctx, int32_t bn, int32_t order);
+ * does not fit), tile order (0 = decreasing K, 1 = problem by problem) and split-K (1: the
+ * longest tiles halved along K while there are fewer than two waves of tiles; exact mode);
+ * bn < 0 returns to the tuner / defaults. For measurements and tests. */
+int mpsg_ctx_set_split_tuning(mpsg_ctx* ctx, int32_t bn, int32_t order, int32_t splitk);
 /* Host self-check of the tensor-core H_eff plans for these structures (any tensors, also
  * structure-only ones): every copy and GEMM window in bounds, every output element written
  * once, and the composed intermediate copy equal to the two-step copy. */

@@ -119,7 +119,7 @@ SIGNATURES = {
     "mpsg_heff2_batch_info": [P, PF64, PI64, PI64, PI32],
     "mpsg_heff2_batch_free": [P],
     "mpsg_ctx_tuner": [P, I32, PI64, PI64],
-    "mpsg_ctx_set_split_tuning": [P, I32, I32],
+    "mpsg_ctx_set_split_tuning": [P, I32, I32, I32],
     "mpsg_meta_create": [I32, I32, PI32, PI32, PI64, PI32, PP],
     "mpsg_plan_permutelegs": [P, PI32, PP],
     "mpsg_plan_fuselegs": [P, I32, I32, I32, PP],

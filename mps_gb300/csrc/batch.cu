@@ -59,7 +59,8 @@ split::Tuning tune_split(Context* ctx, const std::vector<GemmTask>& g, int S) {
   std::vector<int> bns = {split::exact_bn(S)};
   if (split::exact_bn(S) != 64) bns.push_back(64);
   for (int bn : bns)
-    for (int order : {split::kOrderK, split::kOrderProblem}) cands.push_back({bn, order});
+    for (int order : {split::kOrderK, split::kOrderProblem})
+      for (int sk : {0, 1}) cands.push_back({bn, order, sk});
   int64_t na, nb, nc;
   operand_extents(g, na, nb, nc);
   // operand values do not change the kernels' work: ones
@@ -75,8 +76,10 @@ split::Tuning tune_split(Context* ctx, const std::vector<GemmTask>& g, int S) {
     for (const split::Tuning& t : cands) {
       split::SplitPlan sp;
       sp.build(ctx, g, S, t);
-      // the fast kernel has one tile shape: only the order is a choice
-      if (sp.fast && t.bn != bns[0]) continue;
+      // the fast kernel has one tile shape and no split-K: only the order is a choice; a
+      // split-K candidate that splits nothing is the candidate without it
+      if (sp.fast && (t.bn != bns[0] || t.splitk)) continue;
+      if (t.splitk && sp.nsplit == 0) continue;
       split::launch_split_gemm(ctx, sp, A->ptr, B->ptr, C->ptr, split::kAll);  // warm-up
       constexpr int kReps = 2;
       MPSG_CUDA(cudaEventRecord(e0, ctx->stream));
@@ -107,6 +110,7 @@ split::Tuning choose_tuning(Context* ctx, const std::vector<GemmTask>& g, int S)
     split::Tuning t;
     t.bn = (ctx->forced_bn == 64 || ctx->forced_bn == split::exact_bn(S)) ? ctx->forced_bn : 0;
     t.order = ctx->forced_order;
+    t.splitk = ctx->forced_splitk;
     return t;
   }
   if (!ctx->autotune || g.empty()) return split::Tuning();
@@ -115,12 +119,13 @@ split::Tuning choose_tuning(Context* ctx, const std::vector<GemmTask>& g, int S)
   if (it != ctx->tune_cache.end()) {
     ctx->tune_hits++;
     split::Tuning t;
-    t.bn = it->second.first;
-    t.order = it->second.second;
+    t.bn = it->second[0];
+    t.order = it->second[1];
+    t.splitk = it->second[2];
     return t;
   }
   const split::Tuning t = tune_split(ctx, g, S);
-  ctx->tune_cache[key] = {t.bn, t.order};
+  ctx->tune_cache[key] = {t.bn, t.order, t.splitk};
   return t;
 }
 

@@ -899,18 +899,21 @@ int mpsg_ctx_tuner(mpsg_ctx* ctx, int32_t enable, int64_t* runs, int64_t* hits) 
   });
 }
 
-int mpsg_ctx_set_split_tuning(mpsg_ctx* ctx, int32_t bn, int32_t order) {
+int mpsg_ctx_set_split_tuning(mpsg_ctx* ctx, int32_t bn, int32_t order, int32_t splitk) {
   return guarded([&] {
     need(ctx, "ctx");
     if (bn < 0) {
       ctx->c.forced_bn = ctx->c.forced_order = -1;
+      ctx->c.forced_splitk = 0;
       return;
     }
     if (bn != 0 && bn != 64 && bn != 128)
       throw mpsg::Error(mpsg::kErrArgument, "split GEMM N tile must be 0, 64 or 128");
     if (order != 0 && order != 1) throw mpsg::Error(mpsg::kErrArgument, "tile order must be 0 or 1");
+    if (splitk != 0 && splitk != 1) throw mpsg::Error(mpsg::kErrArgument, "split-K must be 0 or 1");
     ctx->c.forced_bn = bn;
     ctx->c.forced_order = order;
+    ctx->c.forced_splitk = splitk;
   });
 }
 

@@ -571,7 +571,9 @@ __global__ void __launch_bounds__(kExactThreads, 1) split_gemm_kernel(
         const int nks = probs[tr.x].nks;
         const int64_t baseA = (probs[tr.x].tA + (int64_t)tr.y * nks) * BM;
         const int64_t baseB = (probs[tr.x].tB + (int64_t)tr.z * nks) * CF::kBN;
-        for (int ks = 0; ks < nks * CF::kPerRow; ++ks) {
+        // K steps [kb, ke) of 64 columns (the whole K unless split-K halved this tile)
+        const int kb = tr.w & 0xffff, ke = (int)((unsigned)tr.w >> 16);
+        for (int ks = kb * CF::kPerRow; ks < ke * CF::kPerRow; ++ks) {
           if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) break;
           uint8_t* sA = smem + stage * CF::kStageBytes;
           uint8_t* sB = sA + S * CF::kABytes;
@@ -601,8 +603,10 @@ __global__ void __launch_bounds__(kExactThreads, 1) split_gemm_kernel(
       for (int64_t i = 0; !*abort_flag; ++i) {
         const int64_t pos = sched_pos(i, gridDim.x, blockIdx.x);
         if (pos >= ntiles) break;
-        const int nsteps = probs[tiles[pos].x].nks * CF::kPerRow;
-        for (int c0 = 0; c0 < nsteps && !*abort_flag; c0 += CF::kChunkSteps) {
+        const int tw = tiles[pos].w;
+        const int nsteps = (int)((unsigned)tw >> 16) * CF::kPerRow;
+        for (int c0 = (tw & 0xffff) * CF::kPerRow; c0 < nsteps && !*abort_flag;
+             c0 += CF::kChunkSteps) {
           const int buf = (int)(use % CF::kBufs);
           const uint32_t bph = (uint32_t)((use / CF::kBufs) & 1);
           if (!mbar_wait(&tempty[buf], bph ^ 1, abort_flag, err, 2)) break;
@@ -670,7 +674,9 @@ __global__ void __launch_bounds__(kExactThreads, 1) split_gemm_kernel(
         lo[j] = 0.f;
       }
       bool ok = true;
-      for (int c0 = 0; c0 < P.nks * CF::kPerRow; c0 += CF::kChunkSteps) {
+      const int kb = tr.w & 0xffff, ke = (int)((unsigned)tr.w >> 16);
+      const bool part = kb != 0 || ke != P.nks;  // one of two split-K halves
+      for (int c0 = kb * CF::kPerRow; c0 < ke * CF::kPerRow; c0 += CF::kChunkSteps) {
         const int buf = (int)(use % CF::kBufs);
         const uint32_t bph = (uint32_t)((use / CF::kBufs) & 1);
         if (!mbar_wait(&tfull[buf], bph, abort_flag, err, 5)) {
@@ -707,7 +713,10 @@ __global__ void __launch_bounds__(kExactThreads, 1) split_gemm_kernel(
             const int Cc = CB[P.rB + col];
             // a zero row or column (no exponent) contributes exact zeros
             const int E = (Rr == kNoExponent || Cc == kNoExponent) ? 0 : Rr + Cc;
-            Cp[col * P.ldc] = ds_to_f64(hi[j], lo[j], E);
+            if (part)  // zeroed output, exactly two partial sums: order-independent
+              atomicAdd(Cp + col * P.ldc, ds_to_f64(hi[j], lo[j], E));
+            else
+              Cp[col * P.ldc] = ds_to_f64(hi[j], lo[j], E);
           }
         }
       }
@@ -1044,13 +1053,40 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_, Tuni
   ntiles = tile_prefix.back();
   // output tiles problem by problem (N tile, then M tile), for the snake schedule by decreasing
   // K (ties keep that order) unless the tuning asks for the problem order
+  // w = K steps [kb, ke) of the tile: kb | ke << 16 (split-K halves cover part of K)
   std::vector<int4> tl;
   tl.reserve(ntiles);
-  for (int p = 0; p < nprob; ++p)
+  for (int p = 0; p < nprob; ++p) {
+    if (probs[p].nks > 0x7fff) throw Error(kErrUnsupported, "split GEMM: K too long");
     for (int ni = 0; ni < probs[p].nt; ++ni)
-      for (int mi = 0; mi < probs[p].mt; ++mi) tl.push_back(make_int4(p, mi, ni, probs[p].nks));
+      for (int mi = 0; mi < probs[p].mt; ++mi)
+        tl.push_back(make_int4(p, mi, ni, probs[p].nks << 16));
+  }
+  auto work = [](const int4& t) { return (int)((unsigned)t.w >> 16) - (t.w & 0xffff); };
+  nsplit = 0;
+  std::vector<char> zero_prob(nprob, 0);
+  if (tune.splitk && !fast) {
+    // halve the longest tiles at a chunk boundary while there are fewer than two waves
+    const int c64 = chunk / 64;
+    const int64_t target = 2 * (int64_t)ctx->num_sms;
+    std::stable_sort(tl.begin(), tl.end(),
+                     [&](const int4& a, const int4& b) { return work(a) > work(b); });
+    const size_t n0 = tl.size();
+    for (size_t i = 0; i < n0 && (int64_t)tl.size() < target; ++i) {
+      int4& t = tl[i];
+      const int nks = probs[t.x].nks;
+      const int mid = ((nks / c64) / 2) * c64;
+      if (mid <= 0 || mid >= nks) continue;  // shorter than two chunks: not split
+      tl.push_back(make_int4(t.x, t.y, t.z, mid | (nks << 16)));
+      t.w = mid << 16;
+      zero_prob[t.x] = 1;
+      ++nsplit;
+    }
+  }
+  ntiles = (int64_t)tl.size();
   if (order == kOrderK)
-    std::stable_sort(tl.begin(), tl.end(), [](const int4& a, const int4& b) { return a.w > b.w; });
+    std::stable_sort(tl.begin(), tl.end(),
+                     [&](const int4& a, const int4& b) { return work(a) > work(b); });
   tilesA = tA;
   tilesB = tB;
   rowsA = tA * BM;
@@ -1076,6 +1112,11 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_, Tuni
   up((void**)&d_probs, probs.data(), sizeof(Problem) * nprob);
   up((void**)&d_tile_prefix, tile_prefix.data(), sizeof(int64_t) * (nprob + 1));
   up((void**)&d_tiles, tl.data(), sizeof(int4) * tl.size());
+  std::vector<int> zl;
+  for (int p = 0; p < nprob; ++p)
+    if (zero_prob[p]) zl.push_back(p);
+  nzero = (int)zl.size();
+  if (nzero) up((void**)&d_zero, zl.data(), sizeof(int) * zl.size());
   up((void**)&d_packA_prefix, packA_prefix.data(), sizeof(int64_t) * (nprob + 1));
   up((void**)&d_packB_prefix, packB_prefix.data(), sizeof(int64_t) * (nprob + 1));
   up((void**)&d_rowA_prefix, rowA_prefix.data(), sizeof(int64_t) * (nprob + 1));
@@ -1099,7 +1140,8 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_, Tuni
 
 void SplitPlan::release() {
   void* ptrs[] = {d_probs, d_tile_prefix, d_packA_prefix, d_packB_prefix, d_rowA_prefix,
-                  d_rowB_prefix, d_RA, d_CB, d_EA, d_EB, d_packA, d_packB, d_err, d_tiles};
+                  d_rowB_prefix, d_RA, d_CB, d_EA, d_EB, d_packA, d_packB, d_err, d_tiles,
+                  d_zero};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, stream);
   d_probs = nullptr;
@@ -1109,7 +1151,21 @@ void SplitPlan::release() {
   d_EA = d_EB = nullptr;
   d_packA = d_packB = nullptr;
   d_err = nullptr;
+  d_zero = nullptr;
+  nzero = 0;
+  nsplit = 0;
   nprob = 0;
+}
+
+// Zeroes the output blocks of the problems listed in `list` (those with split-K tiles, whose
+// halves add into the output); one CTA per problem.
+__global__ void zero_outputs_kernel(const Problem* __restrict__ probs, const int* __restrict__ list,
+                                    double* __restrict__ C) {
+  const Problem P = probs[list[blockIdx.x]];
+  for (int64_t e = threadIdx.x; e < P.M * P.N; e += blockDim.x) {
+    const int64_t j = e / P.M, i = e - j * P.M;
+    C[P.offC + i + j * P.ldc] = 0.0;
+  }
 }
 
 // The exact kernel at N tile BN (the fast kernel when the plan is in fast mode).
@@ -1125,6 +1181,11 @@ static void launch_gemm_t(Context* ctx, SplitPlan& sp, double* C) {
   else
     set_smem_limit_once(ctx, exact_set, split_gemm_kernel<S, BN>, (int)CF::kSmemBytes);
   const int grid = (int)std::min<int64_t>(sp.ntiles, (int64_t)ctx->num_sms);
+  if (sp.nzero) {
+    zero_outputs_kernel<<<sp.nzero, 256, 0, ctx->stream>>>(sp.d_probs, sp.d_zero, C);
+    MPSG_CUDA(cudaGetLastError());
+    ctx->kernel_launches++;
+  }
   KernelTimer timer(ctx, kKindGemmSplit, sp.flops);
   if (sp.fast) {
     if (S > 3) throw Error(kErrUnsupported, "fast split mode needs S <= 3");

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <atomic>
 #include <list>
 #include <memory>
@@ -195,9 +196,9 @@ struct Context : std::enable_shared_from_this<Context> {
   // split-GEMM tuner (batch.cu): when on, a new shape class of problem lists is timed over the
   // kernel's N tiles and tile orders and the fastest (N tile, order) kept by class
   bool autotune = false;
-  std::unordered_map<std::string, std::pair<int, int>> tune_cache;
+  std::unordered_map<std::string, std::array<int, 3>> tune_cache;  // (N tile, order, split-K)
   int64_t tune_runs = 0, tune_hits = 0;
-  int forced_bn = -1, forced_order = -1;  // mpsg_ctx_set_split_tuning: fixed configuration
+  int forced_bn = -1, forced_order = -1, forced_splitk = 0;  // mpsg_ctx_set_split_tuning
   void* solver = nullptr;         // cusolverDnHandle_t, created on first SVD
   void (*solver_destroy)(void*) = nullptr;
   // optional per-kernel-class event timing (see mpsg_ctx_set_timing)

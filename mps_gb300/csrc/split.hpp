@@ -37,9 +37,14 @@ constexpr int exact_bn(int S) { return exact_accs(S) * 128 <= 512 ? 128 : 64; }
 // balances ragged sectors; kOrderProblem: problem by problem, N tile by N tile, which keeps the
 // CTAs of one wave on the same operands).
 enum { kOrderK = 0, kOrderProblem = 1 };
+// splitk: cut the output tiles with the longest K loops into two halves at a chunk boundary
+// while that leaves fewer than two waves of tiles on the GPU (exact mode only). Each half adds
+// its FP64 partial result into the zeroed output with one atomic add; with exactly two terms
+// the sum does not depend on their order, so results stay deterministic.
 struct Tuning {
   int bn = 0;
   int order = kOrderK;
+  int splitk = 0;
 };
 
 // One sector GEMM as the split kernels see it (column-major A: M x K, B: K x N, C: M x N).
@@ -59,6 +64,9 @@ struct SplitPlan {
   bool fast = false;   // one FP32 accumulator, 128 x 256 tiles (S <= 3); else exact chunked mode
   int bn = 64;         // rows of a packed B tile = N of an output tile
   int order = kOrderK; // output tile order (Tuning)
+  int64_t nsplit = 0;  // tiles cut in two by split-K
+  int nzero = 0;       // problems whose output is zeroed before the GEMM (split tiles)
+  int* d_zero = nullptr;
   int chunk = 0;       // K columns per exact chunk (whole K in fast mode)
   int seg = 0;         // K columns per exponent-pass work item
   int nprob = 0;

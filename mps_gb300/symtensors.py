@@ -923,11 +923,13 @@ def tuner(ctx, enable=None):
     return r.value, h.value
 
 
-def set_split_tuning(ctx, bn=None, order=0):
+def set_split_tuning(ctx, bn=None, order=0, splitk=0):
     """Fix the split-GEMM configuration of plans built from now on in ``ctx``: N tile ``bn``
-    (64, 128 or 0 = default; None returns to the tuner / defaults) and tile ``order`` (0 =
-    decreasing K, 1 = problem by problem)."""
-    call("mpsg_ctx_set_split_tuning", ctx.handle, -1 if bn is None else int(bn), int(order))
+    (64, 128 or 0 = default; None returns to the tuner / defaults), tile ``order`` (0 =
+    decreasing K, 1 = problem by problem) and ``splitk`` (1: the longest tiles halved along K
+    while there are fewer than two waves)."""
+    call("mpsg_ctx_set_split_tuning", ctx.handle, -1 if bn is None else int(bn), int(order),
+         int(splitk))
 
 
 def eigsolve_heff2(x0, envL, envR, W1, W2, krylovdim=5, maxiter=8, tol=1e-7, precision=None):

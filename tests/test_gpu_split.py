@@ -168,19 +168,25 @@ def test_applymps2site_from_host_buffers(S):
 
 
 @pytest.mark.parametrize("S", [4, 5, 6, 7])
-@pytest.mark.parametrize("bn,order", [(64, 0), (64, 1), (128, 0), (0, 1)])
-def test_split_configurations_agree(S, bn, order):
-    """Every N tile and tile order the tuner may pick gives the default configuration's result:
-    the exact groups are order-independent integer sums, so only the shared accumulator of the
-    two smallest groups may round differently (far below the slicing bound)."""
+@pytest.mark.parametrize("bn,order,splitk", [(64, 0, 0), (64, 1, 0), (128, 0, 0), (0, 1, 0),
+                                             (0, 0, 1), (64, 1, 1)])
+def test_split_configurations_agree(S, bn, order, splitk):
+    """Every N tile, tile order and split-K choice the tuner may pick gives the default
+    configuration's result: the exact groups are order-independent integer sums, the shared
+    accumulator of the two smallest groups may round differently (far below the slicing bound),
+    and split-K halves add two FP64 partial sums. A split result is the same on every run."""
     rng = np.random.default_rng(100 + S)
-    A, B = pair(rng, [(0, 300), (1, 129), (2, 7)], [(0, 1500), (1, 65), (2, 1)],
+    # K = 2600 in the largest sector: at least two exact chunks, so split-K halves its tiles
+    A, B = pair(rng, [(0, 300), (1, 129), (2, 7)], [(0, 2600), (1, 65), (2, 1)],
                 [(0, 200), (1, 300), (2, 3)])
     want = st.matmul(A, B)
     ref = mg.matmul(to_device(A), to_device(B), precision=S)
     ctx = mg.Context(0)
-    mg.set_split_tuning(ctx, bn, order)
-    got = mg.matmul(to_device(A, ctx), to_device(B, ctx), precision=S)
+    mg.set_split_tuning(ctx, bn, order, splitk)
+    Ad, Bd = to_device(A, ctx), to_device(B, ctx)
+    got = mg.matmul(Ad, Bd, precision=S)
+    again = mg.matmul(Ad, Bd, precision=S)
     for s in want.blocks:
         assert relerr(got.blocks[s], want.blocks[s]) < TOL[S], s
         assert relerr(got.blocks[s], ref.blocks[s]) < 1e-3 * TOL[S], s
+        assert np.array_equal(got.blocks[s], again.blocks[s]), s
