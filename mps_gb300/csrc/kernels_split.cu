@@ -1063,26 +1063,10 @@ void SplitPlan::build(Context* ctx, const std::vector<GemmTask>& g, int S_, Tuni
         tl.push_back(make_int4(p, mi, ni, probs[p].nks << 16));
   }
   auto work = [](const int4& t) { return (int)((unsigned)t.w >> 16) - (t.w & 0xffff); };
-  nsplit = 0;
   std::vector<char> zero_prob(nprob, 0);
-  if (tune.splitk && !fast) {
-    // halve the longest tiles at a chunk boundary while there are fewer than two waves
-    const int c64 = chunk / 64;
-    const int64_t target = 2 * (int64_t)ctx->num_sms;
-    std::stable_sort(tl.begin(), tl.end(),
-                     [&](const int4& a, const int4& b) { return work(a) > work(b); });
-    const size_t n0 = tl.size();
-    for (size_t i = 0; i < n0 && (int64_t)tl.size() < target; ++i) {
-      int4& t = tl[i];
-      const int nks = probs[t.x].nks;
-      const int mid = ((nks / c64) / 2) * c64;
-      if (mid <= 0 || mid >= nks) continue;  // shorter than two chunks: not split
-      tl.push_back(make_int4(t.x, t.y, t.z, mid | (nks << 16)));
-      t.w = mid << 16;
-      zero_prob[t.x] = 1;
-      ++nsplit;
-    }
-  }
+  nsplit = (tune.splitk && !fast)
+               ? split_k_tiles(tl, probs, chunk / 64, 2 * (int64_t)ctx->num_sms, zero_prob)
+               : 0;
   ntiles = (int64_t)tl.size();
   if (order == kOrderK)
     std::stable_sort(tl.begin(), tl.end(),

@@ -2,6 +2,10 @@
 #pragma once
 
 #include <cuda.h>
+#include <vector_types.h>
+
+#include <algorithm>
+#include <vector>
 
 #include "runtime.hpp"
 
@@ -90,6 +94,31 @@ struct SplitPlan {
 };
 
 int chunk_for(int S);
+
+// Split-K of a tile list (host): tiles are (problem, M tile, N tile, kb | ke << 16) with K steps
+// [kb, ke) of 64 columns. The tiles with the longest K loops (stable order) are halved at a
+// multiple of c64 K steps (one exact chunk) while the list has fewer than `target` tiles; each
+// halved tile's problem is marked in `zero_prob` (its output is zeroed, the halves add into
+// it). Returns the number of tiles halved. Pure host code (checked on the CPU).
+inline int64_t split_k_tiles(std::vector<int4>& tl, const std::vector<Problem>& probs, int c64,
+                             int64_t target, std::vector<char>& zero_prob) {
+  auto work = [](const int4& t) { return (int)((unsigned)t.w >> 16) - (t.w & 0xffff); };
+  std::stable_sort(tl.begin(), tl.end(),
+                   [&](const int4& a, const int4& b) { return work(a) > work(b); });
+  int64_t n = 0;
+  const size_t n0 = tl.size();
+  for (size_t i = 0; i < n0 && (int64_t)tl.size() < target; ++i) {
+    const int4 t = tl[i];  // a copy: push_back below may move the list
+    const int nks = probs[t.x].nks;
+    const int mid = c64 > 0 ? ((nks / c64) / 2) * c64 : 0;
+    if (mid <= 0 || mid >= nks || work(t) != nks) continue;  // short, or already a half
+    tl[i].w = mid << 16;
+    tl.push_back(make_int4(t.x, t.y, t.z, mid | (nks << 16)));
+    zero_prob[t.x] = 1;
+    ++n;
+  }
+  return n;
+}
 // what: bit 0 = pack A, bit 1 = pack B, bit 2 = run the GEMM (an operand packed by an earlier
 // call stays valid in the plan's scratch until the plan is packed again).
 enum { kPackA = 1, kPackB = 2, kRunGemm = 4, kAll = 7 };
