@@ -1142,11 +1142,12 @@ void SplitPlan::release() {
 }
 
 // Zeroes the output blocks of the problems listed in `list` (those with split-K tiles, whose
-// halves add into the output); one CTA per problem.
+// halves add into the output); blockIdx.y selects the problem, blockIdx.x strides over it.
 __global__ void zero_outputs_kernel(const Problem* __restrict__ probs, const int* __restrict__ list,
                                     double* __restrict__ C) {
-  const Problem P = probs[list[blockIdx.x]];
-  for (int64_t e = threadIdx.x; e < P.M * P.N; e += blockDim.x) {
+  const Problem P = probs[list[blockIdx.y]];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P.M * P.N;
+       e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = e / P.M, i = e - j * P.M;
     C[P.offC + i + j * P.ldc] = 0.0;
   }
@@ -1166,7 +1167,8 @@ static void launch_gemm_t(Context* ctx, SplitPlan& sp, double* C) {
     set_smem_limit_once(ctx, exact_set, split_gemm_kernel<S, BN>, (int)CF::kSmemBytes);
   const int grid = (int)std::min<int64_t>(sp.ntiles, (int64_t)ctx->num_sms);
   if (sp.nzero) {
-    zero_outputs_kernel<<<sp.nzero, 256, 0, ctx->stream>>>(sp.d_probs, sp.d_zero, C);
+    zero_outputs_kernel<<<dim3(64, (unsigned)sp.nzero), 256, 0, ctx->stream>>>(sp.d_probs,
+                                                                              sp.d_zero, C);
     MPSG_CUDA(cudaGetLastError());
     ctx->kernel_launches++;
   }

@@ -188,5 +188,6 @@ def test_split_configurations_agree(S, bn, order, splitk):
     again = mg.matmul(Ad, Bd, precision=S)
     for s in want.blocks:
         assert relerr(got.blocks[s], want.blocks[s]) < TOL[S], s
-        assert relerr(got.blocks[s], ref.blocks[s]) < 1e-3 * TOL[S], s
+        # the double-single accumulation of each half limits agreement to about 2^-48
+        assert relerr(got.blocks[s], ref.blocks[s]) < max(1e-3 * TOL[S], 2e-14), s
         assert np.array_equal(got.blocks[s], again.blocks[s]), s
