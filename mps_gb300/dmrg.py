@@ -522,7 +522,8 @@ def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, device: int = 0
     every Krylov application one grouped launch per phase for all those chains, replayed from a
     CUDA graph, split GEMMs with tuned tiles; FP64 recurrences). With ``wait_all`` the batcher
     waits until every chain still sweeping has a request (lock step); otherwise it takes what is
-    waiting. Same start states as ``run_chains`` (Philox seed + index). Returns the last
+    waiting (then without graph capture: the other chains' threads keep working meanwhile).
+    Same start states as ``run_chains`` (Philox seed + index). Returns the last
     post-truncation energy of each chain; ``stats`` (a dict) collects batch counts, chains per
     batch, batcher times and the tuner's runs and hits."""
     import threading
@@ -600,8 +601,10 @@ def run_chains_lockstep(specs, nsweeps: int, opts: SweepOptions, device: int = 0
                 for k in range(0, len(ids), max_batch):
                     part = ids[k:k + max_batch]
                     t0 = time.perf_counter()
+                    # dynamic batches run uncaptured: the other chains' threads keep issuing
+                    # their own work (first launches load kernels) while a capture would run
                     B = mg.HeffBatch.from_prepared([batch[i][0] for i in part], bctx,
-                                                   graph=graph)
+                                                   graph=graph and wait_all)
                     bctx.synchronize()  # the chains' operators may go once this is done
                     t1 = time.perf_counter()
                     _, vecs, _ = B.eigsolve([batch[i][1] for i in part],
