@@ -367,3 +367,312 @@ def evolve_with_tangent(ops: Ops, As, Ws, dWs, dt: float, sweeps: int, site_ops:
         tdvp1sitesweep_tangent(ops, dt, As, dAs, Ws, dWs, env, denv, turning=turning,
                                krylovdim=krylovdim, tol=tol, stats=stats)
     return expectation_tangent(ops, As, dAs, site_ops)
+
+
+# ---------------------------------------------------------------------------------------------
+# reverse mode: adjoints of the sweep, environments recomputed from per-sweep checkpoints
+# ---------------------------------------------------------------------------------------------
+_FRESH = 1000  # offset of the negative labels that pair legs in an adjoint contraction
+
+
+def _cscale_any(ops, X, z):
+    return clincomb(ops, [(complex(z), X)])
+
+
+def _contract_vjp_one(ops, ix, Y, iy, dC):
+    """Cotangent of X in C = ccontract(X, ix, Y, iy) for the cotangent dC (dL = Re<dC, dC_>):
+    dX = dC contracted with conj(Y) (``cdual``: conjugated, dual spaces) on the legs C took
+    from Y; a full contraction (C a number) gives dX = dC * conj(Y) in X's leg order."""
+    if not any(lab > 0 for lab in ix + iy):
+        if tuple(ix) != tuple(iy):
+            raise ValueError("full contraction adjoint needs matching leg order")
+        return _cscale_any(ops, cdual(ops, Y), dC)
+    nC = sum(1 for lab in ix + iy if lab > 0)
+    idx_dc = []
+    for p in range(1, nC + 1):
+        idx_dc.append(ix.index(p) + 1 if p in ix else -(_FRESH + p))
+    idx_y = [-(_FRESH + lab) if lab > 0 else ix.index(lab) + 1 for lab in iy]
+    return ccontract(ops, dC, tuple(idx_dc), cdual(ops, Y), tuple(idx_y))
+
+
+class _Tape:
+    """Records the sweep's primitive operations with their adjoints; ``backward`` propagates
+    cotangents (dL = Re <x_bar, dx>) from seeds to every recorded input, matched by identity."""
+
+    def __init__(self, ops):
+        self.ops = ops
+        self.rec = []
+
+    def contract(self, A, ia, B, ib):
+        ia, ib = tuple(int(x) for x in ia), tuple(int(x) for x in ib)
+        C = ccontract(self.ops, A, ia, B, ib)
+        ops = self.ops
+        self.rec.append(((A, B), (C,), lambda g: (_contract_vjp_one(ops, ia, B, ib, g[0]),
+                                                   _contract_vjp_one(ops, ib, A, ia, g[0]))))
+        return C
+
+    def dual(self, A):
+        D = cdual(self.ops, A)
+        ops = self.ops
+        self.rec.append(((A,), (D,), lambda g: (cdual(ops, g[0]),)))
+        return D
+
+    def fuse(self, A, l, n):
+        M = cfuselegs(self.ops, A, l, n)
+        sp = cspace(self.ops, A)[l - 1:l - 1 + n]
+        ops = self.ops
+        self.rec.append(((A,), (M,), lambda g: (csplitleg(ops, g[0], l, sp),)))
+        return M
+
+    def split(self, M, l, sp):
+        A = csplitleg(self.ops, M, l, sp)
+        ops, n = self.ops, len(sp)
+        self.rec.append(((M,), (A,), lambda g: (cfuselegs(ops, g[0], l, n),)))
+        return A
+
+    def custom(self, inputs, outputs, vjp):
+        self.rec.append((tuple(inputs), tuple(outputs), vjp))
+
+    def backward(self, seeds):
+        ops = self.ops
+        grads = {}
+
+        def acc(x, g):
+            if g is None or x is None:
+                return
+            k = id(x)
+            grads[k] = g if k not in grads else clincomb(ops, [(1.0, grads[k]), (1.0, g)])
+
+        for x, g in seeds:
+            acc(x, g)
+        for inputs, outputs, vjp in reversed(self.rec):
+            gs = [grads.get(id(o)) for o in outputs]
+            if all(g is None for g in gs):
+                continue
+            for i, o in enumerate(outputs):  # an output's cotangent is consumed here
+                if gs[i] is None:
+                    gs[i] = cscale(ops, o, 0.0)
+            for x, g in zip(inputs, vjp(gs)):
+                acc(x, g)
+        return lambda x: grads.get(id(x))
+
+
+def _gauss_legendre(q):
+    x, w = np.polynomial.legendre.leggauss(q)
+    return 0.5 * (x + 1.0), 0.5 * w
+
+
+def _apply_tape(ops, kind, v, L, R, W):
+    """The 1-site (kind 1) or 0-site (kind 0) H_eff of ``tdvp`` on a private tape."""
+    tp = _Tape(ops)
+    if kind == 1:  # apply1
+        t = tp.contract(L, (-1, 2, 1), v, (-1, 3, 4))
+        t = tp.contract(t, (1, -1, -2, 4), W, (-1, 2, 3, -2))
+        out = tp.contract(t, (1, 2, -1, -2), R, (-2, -1, 3))
+    else:  # apply0
+        t = tp.contract(L, (-1, 2, 1), v, (-1, 3))
+        out = tp.contract(t, (1, -1, -2), R, (-2, -1, 2))
+    return tp, out
+
+
+def _expo_vjp(ops, kind, L, R, W, tau, x, ybar, krylovdim, tol, quad):
+    """Adjoint of y = exp(tau F) x, F the Hermitian H_eff built from (L, R, W):
+    x_bar = exp(conj(tau) F) y_bar, and for the operands of F the gradient of
+    Re tau int_0^1 <exp(s conj(tau) F) y_bar, dF exp((1-s) tau F) x> ds by Gauss-Legendre
+    quadrature (``quad`` nodes), each node one adjoint of the H_eff's contractions."""
+    if kind == 1:
+        f = lambda v: apply1(ops, v, L, R, W)
+    else:
+        f = lambda v: apply0(ops, v, L, R)
+    xbar, _ = exponentiate(ops, f, np.conj(tau), ybar, krylovdim=krylovdim, tol=tol)
+    s_nodes, weights = _gauss_legendre(quad)
+    gL = gR = gW = None
+    for s, w in zip(s_nodes, weights):
+        u, _ = exponentiate(ops, f, s * np.conj(tau), ybar, krylovdim=krylovdim, tol=tol)
+        v, _ = exponentiate(ops, f, (1.0 - s) * tau, x, krylovdim=krylovdim, tol=tol)
+        tp, out = _apply_tape(ops, kind, v, L, R, W)
+        grad = tp.backward([(out, cscale(ops, u, w * np.conj(tau)))])
+        gL = _sum(ops, [(1.0, gL), (1.0, grad(L))])
+        gR = _sum(ops, [(1.0, gR), (1.0, grad(R))])
+        if kind == 1:
+            gW = _sum(ops, [(1.0, gW), (1.0, grad(W))])
+    return xbar, gL, gR, gW
+
+
+def _same_shape_inverse(ops, s):
+    """s^-1 with s's own legs and sectors (block (c1, c2) = diag(1 / s_(c1, c2)))."""
+    blocks = {}
+    for key, b in s.blocks.items():
+        b = np.asarray(b, dtype=np.float64)
+        d = b if b.ndim == 1 else np.diagonal(b)
+        blocks[key] = np.diag(np.where(d != 0.0, 1.0 / np.where(d != 0.0, d, 1.0), 0.0))
+    return ops.from_blocks(s.charge, ops.space(s), blocks)
+
+
+def _sweep_taped(ops, tp, dt, As, Ws, env, turning, krylovdim, tol, quad, stats):
+    """``tdvp.tdvp1sitesweep`` on a tape (same operations, same state); As and env in place."""
+    lx = len(As)
+    As[:] = [creal(A) for A in As]
+
+    def expo(kind, l_env, r_env, W, tau, x):
+        L, R = env[l_env], env[r_env]
+        f = (lambda v: apply1(ops, v, L, R, W)) if kind == 1 else (lambda v: apply0(ops, v, L, R))
+        y, info = exponentiate(ops, f, tau, x, krylovdim=krylovdim, tol=tol)
+        if stats is not None:
+            stats.add(info.numops, info.converged)
+        ins = (x, L, R) + ((W,) if kind == 1 else ())
+
+        def vjp(g, kind=kind, L=L, R=R, W=W, tau=tau, x=x):
+            xb, gL, gR, gW = _expo_vjp(ops, kind, L, R, W, tau, x, g[0], krylovdim, tol, quad)
+            return (xb, gL, gR) + ((gW,) if kind == 1 else ())
+        tp.custom(ins, (y,), vjp)
+        return y
+
+    def gauge(A, left):
+        M = tp.fuse(A, 1, 2) if left else tp.fuse(A, 2, 2)
+        u, s, v = csvd(ops, M)
+        sinv = _same_shape_inverse(ops, s)
+        if left:
+            Qf, lam = u, cmatmul_real(ops, s, v)
+
+            def vjp(g, u=u, v=v, sinv=sinv):
+                Qb, lb = g
+                Y = _mm(ops, Qb, cmatmul_real(ops, sinv, v))
+                Y = clincomb(ops, [(1.0, Y), (-1.0, _mm(ops, u, _dag_mm(ops, u, Y)))])
+                return (clincomb(ops, [(1.0, Y), (1.0, _mm(ops, u, lb))]),)
+        else:
+            Qf, lam = v, cmatmul_real_right(ops, u, s)
+
+            def vjp(g, u=u, v=v, sinv=sinv):
+                Qb, lb = g
+                Z = _mm(ops, cmatmul_real_right(ops, u, sinv), Qb)
+                Z = clincomb(ops, [(1.0, Z), (-1.0, _mm(ops, _mm_dag(ops, Z, v), v))])
+                return (clincomb(ops, [(1.0, Z), (1.0, _mm(ops, lb, v))]),)
+        tp.custom((M,), (Qf, lam), vjp)
+        return Qf, lam
+
+    def upd_left(e, Q, W):
+        t = tp.contract(e, (-1, 3, 4), Q, (-1, 2, 1))
+        t = tp.contract(t, (1, -1, -2, 4), W, (-2, 2, 3, -1))
+        return tp.contract(t, (1, -1, 2, -2), tp.dual(Q), (-2, -1, 3))
+
+    def upd_right(e, Q, W):
+        t = tp.contract(e, (-1, 3, 4), Q, (1, 2, -1))
+        t = tp.contract(t, (1, -1, -2, 4), W, (3, 2, -2, -1))
+        return tp.contract(t, (1, -1, 2, -2), tp.dual(Q), (3, -1, -2))
+
+    A = As[0]
+    for l in range(1, lx):
+        A = expo(1, l - 1, l + 1, Ws[l - 1], -1j * dt, A)
+        Qf, lam = gauge(A, True)
+        Q = tp.split(Qf, 1, cspace(ops, A)[0:2])
+        As[l - 1] = Q
+        env[l] = upd_left(env[l - 1], Q, Ws[l - 1])
+        lam = expo(0, l, l + 1, None, 1j * dt, lam)
+        A = tp.contract(lam, (1, -1), As[l], (-1, 2, 3))
+    t_turn = 2.0 * dt if turning == "symmetric" else dt
+    A = expo(1, lx - 1, lx + 1, Ws[lx - 1], -1j * t_turn, A)
+    for l in range(lx - 1, 0, -1):
+        Qf, lam = gauge(A, False)
+        Q = tp.split(Qf, 2, cspace(ops, A)[1:3])
+        As[l] = Q
+        env[l + 1] = upd_right(env[l + 2], Q, Ws[l])
+        lam = expo(0, l, l + 1, None, 1j * dt, lam)
+        A = tp.contract(As[l - 1], (1, 2, -1), lam, (-1, 3))
+        A = expo(1, l - 1, l + 1, Ws[l - 1], -1j * dt, A)
+    As[0] = A
+    return As, env
+
+
+def _initialenv_taped(ops, tp, As, Ws):
+    """``tdvp.initialenv`` on a tape (the right environments as functions of As and Ws)."""
+    lx = len(As)
+    env = [None] * (lx + 2)
+    lVa = cspace(ops, As[0])[0]
+    rVa = ops.dual_space(cspace(ops, As[-1])[2])
+    lVw = ops.space(Ws[0])[0]
+    rVw = ops.dual_space(ops.space(Ws[-1])[2])
+    env[0] = CTensor(ops.fill(1.0, 0, (ops.dual_space(lVa), ops.dual_space(lVw), lVa)))
+    env[lx + 1] = CTensor(ops.fill(1.0, 0, (rVa, rVw, ops.dual_space(rVa))))
+    for l in range(lx, 0, -1):
+        t = tp.contract(env[l + 1], (-1, 3, 4), As[l - 1], (1, 2, -1))
+        t = tp.contract(t, (1, -1, -2, 4), Ws[l - 1], (3, 2, -2, -1))
+        env[l] = tp.contract(t, (1, -1, 2, -2), tp.dual(As[l - 1]), (3, -1, -2))
+    return env
+
+
+def _expectation_taped(ops, tp, As, site_ops):
+    """(num, den) = (<psi|O|psi>, <psi|psi>) as numbers on the tape (transfers, then the sum of
+    the last transfer's entries as a contraction with ones)."""
+    V0 = cspace(ops, As[0])[0]
+    L0 = CTensor(ops.fill(1.0, 0, (V0, ops.dual_space(V0))))
+    L, N = L0, L0
+
+    def transfer(T, A, op):
+        t = tp.contract(T, (-1, 1), tp.dual(A), (-1, 2, 3))
+        if op is not None:
+            t = tp.contract(t, (1, -1, 3), op, (-1, 2))
+        return tp.contract(t, (-1, -2, 1), A, (-1, -2, 2))
+
+    for x, A in enumerate(As, start=1):
+        L = transfer(L, A, site_ops.get(x))
+        N = transfer(N, A, None)
+    sp = cspace(ops, L)
+    ones = CTensor(ops.fill(1.0, 0, tuple(ops.dual_space(V) for V in sp)))
+    num = tp.contract(L, (-1, -2), ones, (-1, -2))
+    den = tp.contract(N, (-1, -2), ones, (-1, -2))
+    return num, den, L, N
+
+
+def evolve_with_adjoint(ops: Ops, As, Ws, dt: float, sweeps: int, site_ops: dict,
+                        turning: str = "symmetric", krylovdim: int = 30, tol: float = 1e-12,
+                        quad: int = 8, stats: TangentStats | None = None):
+    """Reverse mode of ``sweeps`` 1-site TDVP sweeps of the center-1 MPS ``As`` under the MPO
+    ``Ws``, for C = Re <psi|O|psi> / <psi|psi> (O = prod site_ops) at the end. Forward: the
+    plain sweeps, keeping only the MPS at the start of each sweep (checkpoints; the MPO and the
+    site operators are the other inputs). Backward, sweep by sweep from the last: the
+    environments are recomputed from the checkpoint, the sweep is replayed on a tape and the
+    cotangents pass through it (adjoint contractions, the gauge moves' adjoints, and for every
+    Krylov exponential exp(conj(t) F) on the cotangent plus a Gauss-Legendre quadrature of its
+    coupling gradient). Returns (C, grad_W, grad_A0): cotangents of every MPO tensor (real part
+    is the gradient for a real MPO) and of every initial site tensor. ``As`` ends evolved."""
+    from .tdvp import initialenv, tdvp1sitesweep
+    if turning not in TURNING:
+        raise ValueError(f"turning must be one of {TURNING}")
+    lx = len(As)
+    # cotangents are kept per tensor object: sites that share one MPO tensor (a uniform chain)
+    # get their own copy so that each site's gradient is returned separately
+    Ws = [ops.lincomb([(1.0, W)]) for W in Ws]
+    checkpoints = []
+    env = initialenv(ops, As, Ws)
+    for _ in range(sweeps):
+        checkpoints.append([creal(A) for A in As])
+        tdvp1sitesweep(ops, dt, As, Ws, env, turning=turning, krylovdim=krylovdim, tol=tol)
+    # the observable and its cotangents on the final state
+    tp = _Tape(ops)
+    final = list(As)
+    num, den, _, _ = _expectation_taped(ops, tp, final, site_ops)
+    num = complex(num)
+    den = complex(den)
+    C = num / den
+    # L = Re(num / den): cotangents conj(dL/dnum), conj(dL/dden)
+    gnum = np.conj(1.0 / den)
+    gden = np.conj(-num / den ** 2)
+    rec = tp.rec
+    # find the scalar outputs (the last two recorded contractions)
+    out_num, out_den = rec[-2][1][0], rec[-1][1][0]
+    g = tp.backward([(out_num, gnum), (out_den, gden)])
+    cot = [g(A) for A in final]
+    gW = [g(W) for W in Ws]
+    for k in range(sweeps - 1, -1, -1):
+        start = [creal(A) for A in checkpoints[k]]
+        tp = _Tape(ops)
+        work = list(start)
+        env0 = _initialenv_taped(ops, tp, work, Ws)
+        env = list(env0)
+        _sweep_taped(ops, tp, dt, work, Ws, env, turning, krylovdim, tol, quad, stats)
+        seeds = [(A, c) for A, c in zip(work, cot) if c is not None]
+        g = tp.backward(seeds)
+        cot = [g(A) for A in start]
+        gW = [_sum(ops, [(1.0, a), (1.0, g(W))]) for a, W in zip(gW, Ws)]
+    return C, gW, cot

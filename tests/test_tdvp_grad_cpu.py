@@ -120,3 +120,52 @@ def test_tangent_of_the_exponential_on_its_own():
     _, L = expm_frechet(t * Fd, t * Gd)
     want = xd @ L  # row vector times the (right-acting) operator
     assert np.linalg.norm(dense_site(ops, dy)[0] - want) < 1e-11 * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("turning,sweeps", [("symmetric", 2), ("reference", 1)])
+def test_adjoint_matches_the_tangent_and_differences_in_the_state(turning, sweeps):
+    """Reverse mode (``evolve_with_adjoint``, 6 quadrature nodes) over the sweeps of a
+    truncated chain: the MPO
+    cotangents contracted with dW/dDelta give the forward-mode derivative, every site's gradient
+    is its own (the chain's MPO shares one tensor between its middle sites), and the cotangent
+    of the initial state matches central differences along a random complex direction."""
+    from mps_gb300.ctensor import cdots, clincomb
+    ops = oracle_ops()
+    mps = random_state(LX, M, 4, seed=11)
+    sites = (3, 6)
+    Ws, dWs = mpo_and_derivative(ops, LX, DELTA)
+    assert len({id(W) for W in Ws}) < LX
+    sz = td.site_operator(ops, mps.As[0].space[1], {0: -0.5, 1: 0.5})
+    obs = {i: sz for i in sites}
+    As = [ct.CTensor(A) for A in mps.As]
+    c_t, dc = tg.evolve_with_tangent(ops, As, Ws, dWs, DT, sweeps, obs, turning=turning)
+    As = [ct.CTensor(A) for A in mps.As]
+    C, gW, gA = tg.evolve_with_adjoint(ops, As, Ws, DT, sweeps, obs, turning=turning, quad=6)
+    assert abs(C - c_t) < 1e-13
+    rev = sum(ops.dot(g.re, dW) for g, dW in zip(gW, dWs))
+    assert abs(rev - dc.real) <= 1e-9 * abs(dc.real)
+    # one site's MPO tensor alone: central differences of that site's coupling
+    l, h = 4, 1e-5
+    def c_site(eps):
+        Wx = list(Ws)
+        Wx[l - 1] = ops.lincomb([(1.0, Ws[l - 1]), (eps, dWs[l - 1])])
+        As = [ct.CTensor(A) for A in mps.As]
+        env = td.initialenv(ops, As, Wx)
+        for _ in range(sweeps):
+            td.tdvp1sitesweep(ops, DT, As, Wx, env, turning=turning)
+        return td.expectation(ops, As, obs).real
+    fd = (c_site(h) - c_site(-h)) / (2 * h)
+    assert abs(ops.dot(gW[l - 1].re, dWs[l - 1]) - fd) <= 1e-6 * abs(fd) + 1e-10
+    # the initial state
+    rng = np.random.default_rng(1)
+    A0 = [ct.CTensor(A) for A in mps.As]
+    D = [ct.CTensor(rand_tensor(0, A.space, rng), rand_tensor(0, A.space, rng)) for A in mps.As]
+    def c_state(eps):
+        As = [clincomb(ops, [(1.0, a), (eps, d)]) for a, d in zip(A0, D)]
+        env = td.initialenv(ops, As, Ws)
+        for _ in range(sweeps):
+            td.tdvp1sitesweep(ops, DT, As, Ws, env, turning=turning)
+        return td.expectation(ops, As, obs).real
+    fd = (c_state(h) - c_state(-h)) / (2 * h)
+    an = sum(cdots(ops, [g], d)[0].real for g, d in zip(gA, D))
+    assert abs(an - fd) <= 1e-6 * abs(fd) + 1e-10
