@@ -103,6 +103,9 @@ def parse(argv=None):
                         "events, algorithmic and executed TFLOP/s against the measured peak")
     p.add_argument("--tdvp-no-fd", action="store_true",
                    help="--tdvp: skip the finite-difference evolutions")
+    p.add_argument("--tdvp-adjoint", action="store_true",
+                   help="--tdvp: also the reverse-mode gradient (every MPO tensor and initial "
+                        "site tensor) over the same sweeps; its dC/dDelta and time")
     p.add_argument("--tdvp-precision", type=int, default=0,
                    help="block-GEMM arithmetic of the TDVP contractions (0 = FP64, S = slices)")
     return p.parse_args(argv)
@@ -871,7 +874,8 @@ def run_tdvp(args):
     C(t) = <Sz_i Sz_{i+1}>(t) (i = L/2) with dC/dDelta twice: by forward-mode tangents through
     the sweeps (one evolution carrying derivatives, ``mps_gb300.tdvp_grad``) and by central
     differences (h = 1e-5: evolutions under H(Delta +- h) from the same state; off with
-    --tdvp-no-fd)."""
+    --tdvp-no-fd); with --tdvp-adjoint also by reverse mode over the same sweeps (the gradient
+    with respect to every MPO tensor and initial site tensor, contracted with dW/dDelta)."""
     import numpy as np
     import mps_gb300 as mg
     from mps_gb300 import ctensor as ct
@@ -930,6 +934,29 @@ def run_tdvp(args):
     tangent_s = time.perf_counter() - t0
     print(json.dumps({"tangent_s": tangent_s, "dC": dc_t.real}), file=sys.stderr, flush=True)
     del As, mps
+    adj = {}
+    if args.tdvp_adjoint:
+        # reverse mode over the same sweeps: gradients of C with respect to every MPO tensor
+        # and every initial site tensor; dC/dDelta = sum over sites of <grad W_l, dW_l>
+        mps = gd.mps_from_host(host, ctx)
+        gd.center_at(mps, 1)
+        mg.rmul(mps.As[0], 1.0 / mg.norm(mps.As[0]))
+        As = [ct.CTensor(A) for A in mps.As]
+        astats = tg.TangentStats()
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        c_a, gW, gA = tg.evolve_with_adjoint(ops, As, Ws, dt, steps, {i: sz, i + 1: sz},
+                                             quad=6, stats=astats)
+        ctx.synchronize()
+        adjoint_s = time.perf_counter() - t0
+        dc_a = sum(ops.dot(g.re, dW) for g, dW in zip(gW, dWs))
+        adj = {"dC_dDelta_adjoint": dc_a, "C_t_adjoint_run": c_a.real,
+               "rel_diff_adjoint_vs_tangent": abs(dc_a - dc_t.real) / abs(dc_t.real),
+               "adjoint_evolution_s": adjoint_s, "adjoint_quadrature_nodes": 6,
+               "adjoint_matvecs": astats.matvecs, "adjoint_unconverged": astats.unconverged,
+               "adjoint_gradients": f"{len(gW)} MPO tensors + {len(gA)} initial site tensors"}
+        print(json.dumps({"adjoint_s": adjoint_s, "dC": dc_a}), file=sys.stderr, flush=True)
+        del As, mps, gW, gA
     fd = None
     if not args.tdvp_no_fd:
         rp = evolve(delta + h, False)
@@ -954,6 +981,7 @@ def run_tdvp(args):
         "matvecs_per_sweep": r0["matvecs"] / steps, "unconverged_exponentials": r0["unconverged"],
         "sweep_s": r0["sweep_s"],
     }
+    line.update(adj)
     print(json.dumps(line), flush=True)
 
 

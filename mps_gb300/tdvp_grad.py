@@ -1,8 +1,8 @@
 """Derivatives of TDVP-evolved observables with respect to a Hamiltonian coupling.
 
-The reference evolves MPS with the time-dependent variational principle (src/tdvp.jl:12-89);
-config 5 asks for d<Sz_i Sz_j>(t)/dDelta after 1-site TDVP. A single scalar parameter is a
-forward-mode (tangent) derivative: every quantity of the sweep in ``mps_gb300.tdvp`` carries
+The reference evolves MPS with the time-dependent variational principle (src/tdvp.jl:12-89).
+The quantity here is, e.g., d<Sz_i Sz_j>(t)/dDelta of an XXZ chain after 1-site TDVP. A single
+scalar parameter is a forward-mode (tangent) derivative: every quantity of the sweep in ``mps_gb300.tdvp`` carries
 its derivative with respect to the coupling, propagated through each step by the chain rule,
 so one tangent sweep costs a fixed multiple of a plain sweep and stores nothing beyond the
 current state and environments (no tape, no recomputation). The result is the exact
@@ -25,6 +25,15 @@ derivative, H_eff built from the environments L, R and W):
 * Environments: the four-term product rule over (environment, ket, MPO, bra) of
   ``_mpsupdateleft`` / ``_mpsupdateright`` (src/apply.jl:17-58).
 * Observables: <psi|O|psi> / <psi|psi> by transfer matrices with their tangents.
+
+Reverse mode (``evolve_with_adjoint``) gives the gradient with respect to every MPO tensor and
+every initial site tensor at once (many couplings, or a cost on the initial state). The forward
+sweeps keep only the MPS at the start of each sweep. Backward, sweep by sweep from the last, the
+environments are rebuilt from that checkpoint, the sweep is replayed on a tape (the same
+operations as ``tdvp1sitesweep``) and the cotangents are propagated through it. The adjoint of
+a Krylov exponential y = exp(t F) x is x_bar = exp(conj(t) F) y_bar, plus, for the operands of
+F, a Gauss-Legendre quadrature of int_0^1 <exp(s conj(t) F) y_bar, dF exp((1-s) t F) x> ds. All
+quadrature vectors of one step come from two Krylov integrations (``exponentiate_family``).
 """
 from __future__ import annotations
 
@@ -475,28 +484,109 @@ def _apply_tape(ops, kind, v, L, R, W):
     return tp, out
 
 
+def exponentiate_family(ops: Ops, f, t, x, fracs, krylovdim: int = 30, tol: float = 1e-12,
+                        maxiter: int = 100):
+    """[exp(p t f) x for p in fracs] (0 <= p <= 1, f Hermitian) from the Lanczos bases of one
+    integration of exp(t f) x: the same Krylov recurrence, a-posteriori error control and step
+    halving as ``ctensor.exponentiate``; every p that falls in a restart segment is evaluated
+    from that segment's basis (exp of the tridiagonal at the partial time), so the whole family
+    costs what the single exponential costs. Returns (list, ExpInfo); ``converged`` also checks
+    each p's own error estimate."""
+    from .ctensor import ExpInfo, _expT
+    fr = [float(p) for p in fracs]
+    if any(p < 0.0 or p > 1.0 for p in fr):
+        raise ValueError("fractions must lie in [0, 1]")
+    out = {p: x for p in fr if p == 0.0}
+    scale = cnorm(ops, x)
+    if scale == 0.0:
+        return [x for _ in fr], ExpInfo(0, 0, True)
+    pending = sorted(set(p for p in fr if p > 0.0))
+    v = cscale(ops, x, 1.0 / scale)
+    start = 0.0
+    numops = numsteps = 0
+    converged = True
+    while pending and numsteps < maxiter:
+        numsteps += 1
+        V = [v]
+        alphas, betas = [], []
+        left = 1.0 - start
+        step, b = None, 0.0
+        for j in range(krylovdim):
+            w = f(V[j])
+            numops += 1
+            a = 0.0
+            for rep in range(2):
+                coef = cdots(ops, V, w)
+                if rep == 0:
+                    a = coef[j].real
+                w = clincomb(ops, [(1.0, w)] + [(-cu, u) for cu, u in zip(coef, V)])
+            b = cnorm(ops, w)
+            alphas.append(a)
+            m = j + 1
+            tau = left
+            c = _expT(alphas, betas, tau * t)
+            err = b * abs(c[m - 1]) * scale
+            if err <= tol or b <= 1e-14 * max(1.0, abs(a)):
+                step = tau
+                break
+            if m == krylovdim:
+                while err > tol and tau > 1e-6 * left:
+                    tau *= 0.5
+                    c = _expT(alphas, betas, tau * t)
+                    err = b * abs(c[m - 1]) * scale
+                if err > tol:
+                    converged = False
+                step = tau
+                break
+            betas.append(b)
+            V.append(cscale(ops, w, 1.0 / b))
+        end = 1.0 if step >= left else start + step
+        m = len(alphas)
+        while pending and pending[0] <= end:
+            p = pending.pop(0)
+            cp = _expT(alphas, betas, (p - start) * t)
+            if b * abs(cp[m - 1]) * scale > tol and b > 1e-14 * max(1.0, abs(alphas[-1])):
+                converged = False
+            out[p] = clincomb(ops, [(complex(cp[i]) * scale, V[i]) for i in range(m)])
+        if not pending:
+            break
+        y = clincomb(ops, [(complex(c[i]) * scale, V[i]) for i in range(m)])
+        start = end
+        scale = cnorm(ops, y)
+        v = cscale(ops, y, 1.0 / scale)
+    if pending:
+        converged = False
+        for p in pending:
+            out[p] = cscale(ops, x, 0.0)
+    return [out[p] for p in fr], ExpInfo(numops, numsteps, converged)
+
+
 def _expo_vjp(ops, kind, L, R, W, tau, x, ybar, krylovdim, tol, quad):
     """Adjoint of y = exp(tau F) x, F the Hermitian H_eff built from (L, R, W):
     x_bar = exp(conj(tau) F) y_bar, and for the operands of F the gradient of
     Re tau int_0^1 <exp(s conj(tau) F) y_bar, dF exp((1-s) tau F) x> ds by Gauss-Legendre
-    quadrature (``quad`` nodes), each node one adjoint of the H_eff's contractions."""
+    quadrature (``quad`` nodes), each node one adjoint of the H_eff's contractions. The node
+    vectors come from two Krylov integrations (``exponentiate_family`` of y_bar under conj(tau),
+    which also gives x_bar, and of x under tau). Returns (x_bar, gL, gR, gW, ExpInfo list)."""
     if kind == 1:
         f = lambda v: apply1(ops, v, L, R, W)
     else:
         f = lambda v: apply0(ops, v, L, R)
-    xbar, _ = exponentiate(ops, f, np.conj(tau), ybar, krylovdim=krylovdim, tol=tol)
     s_nodes, weights = _gauss_legendre(quad)
+    us, iu = exponentiate_family(ops, f, np.conj(tau), ybar, list(s_nodes) + [1.0],
+                                 krylovdim=krylovdim, tol=tol)
+    vs, iv = exponentiate_family(ops, f, tau, x, [1.0 - s for s in s_nodes],
+                                 krylovdim=krylovdim, tol=tol)
+    xbar = us[-1]
     gL = gR = gW = None
-    for s, w in zip(s_nodes, weights):
-        u, _ = exponentiate(ops, f, s * np.conj(tau), ybar, krylovdim=krylovdim, tol=tol)
-        v, _ = exponentiate(ops, f, (1.0 - s) * tau, x, krylovdim=krylovdim, tol=tol)
+    for u, v, w in zip(us, vs, weights):
         tp, out = _apply_tape(ops, kind, v, L, R, W)
         grad = tp.backward([(out, cscale(ops, u, w * np.conj(tau)))])
         gL = _sum(ops, [(1.0, gL), (1.0, grad(L))])
         gR = _sum(ops, [(1.0, gR), (1.0, grad(R))])
         if kind == 1:
             gW = _sum(ops, [(1.0, gW), (1.0, grad(W))])
-    return xbar, gL, gR, gW
+    return xbar, gL, gR, gW, (iu, iv)
 
 
 def _same_shape_inverse(ops, s):
@@ -523,7 +613,11 @@ def _sweep_taped(ops, tp, dt, As, Ws, env, turning, krylovdim, tol, quad, stats)
         ins = (x, L, R) + ((W,) if kind == 1 else ())
 
         def vjp(g, kind=kind, L=L, R=R, W=W, tau=tau, x=x):
-            xb, gL, gR, gW = _expo_vjp(ops, kind, L, R, W, tau, x, g[0], krylovdim, tol, quad)
+            xb, gL, gR, gW, infos = _expo_vjp(ops, kind, L, R, W, tau, x, g[0], krylovdim,
+                                              tol, quad)
+            if stats is not None:
+                for info in infos:
+                    stats.add(info.numops, info.converged)
             return (xb, gL, gR) + ((gW,) if kind == 1 else ())
         tp.custom(ins, (y,), vjp)
         return y

@@ -75,3 +75,55 @@ def test_gpu_tangent_against_differences_oracle_and_exact(lx, chimax):
         for i in sites:
             O = O * (((idx >> (lx - i)) & 1) - 0.5)
         assert abs(dc.real - 2.0 * np.vdot(psi, O * dpsi).real) < 1e-8
+
+
+def test_gpu_adjoint_against_tangent_oracle_and_differences():
+    """Reverse mode on the GPU's operations (1 sweep, truncated chain): the MPO cotangents
+    contracted with dW/dDelta give the forward-mode derivative; the initial state's cotangents
+    equal, site by site, those of the same reverse sweep on the CPU oracle's operations (C is a
+    function of the initial state whatever gauge each SVD picks, so its gradient is unique); and
+    along the center site they match central differences of the GPU evolution. (Directions that
+    leave the middle sites off their canonical form curve strongly: there h = 1e-5 differences
+    are off by 1e-3 and only converge to the gradient for h near 1e-7.)"""
+    from helpers import dense_site, rand_tensor
+    lx, sweeps = 10, 1
+    mps = random_state(lx, lx // 2, 6, seed=21)
+    sites = (3, lx - 2)
+    ops = ct.gpu_ops()
+    Ws, dWs = gpu_mpo(ops, lx, DELTA)
+    sz = td.site_operator(ops, mg.VectorSpace(gd.SITE), {0: -0.5, 1: 0.5})
+    obs = {i: sz for i in sites}
+    As = [ct.CTensor(to_device(A)) for A in mps.As]
+    c, dc = tg.evolve_with_tangent(ops, As, Ws, dWs, DT, sweeps, obs)
+    As = [ct.CTensor(to_device(A)) for A in mps.As]
+    C, gW, gA = tg.evolve_with_adjoint(ops, As, Ws, DT, sweeps, obs, quad=6)
+    assert abs(C - c) < 1e-12
+    rev = sum(ops.dot(g.re, dW) for g, dW in zip(gW, dWs))
+    assert abs(rev - dc.real) <= 1e-9 * abs(dc.real)
+    # the same reverse sweep on the oracle
+    cops = oracle_ops()
+    csz = td.site_operator(cops, mps.As[0].space[1], {0: -0.5, 1: 0.5})
+    cC, _, cgA = tg.evolve_with_adjoint(cops, [ct.CTensor(A) for A in mps.As],
+                                        om.xxz_u1mpo(lx, DELTA), DT, sweeps,
+                                        {i: csz for i in sites}, quad=6)
+    assert abs(C - cC) < 1e-11
+    for g, cg in zip(gA, cgA):
+        a, b = dense_site(ops, g), dense_site(cops, cg)
+        assert np.abs(a - b).max() <= 1e-9 * max(1.0, np.abs(b).max())
+    # central differences along a random complex direction of the center site
+    rng = np.random.default_rng(3)
+    A1 = mps.As[0]
+    dr, di = rand_tensor(0, A1.space, rng), rand_tensor(0, A1.space, rng)
+
+    def c_center(eps):
+        As = [ct.CTensor(to_device(st.axpy(eps, dr, st.scaled(A1, 1.0))),
+                         to_device(st.scaled(di, eps)))]
+        As += [ct.CTensor(to_device(A)) for A in mps.As[1:]]
+        env = td.initialenv(ops, As, Ws)
+        for _ in range(sweeps):
+            td.tdvp1sitesweep(ops, DT, As, Ws, env, turning="symmetric")
+        return td.expectation(ops, As, obs).real
+    h = 1e-5
+    fd = (c_center(h) - c_center(-h)) / (2 * h)
+    an = ct.cdots(ops, [gA[0]], ct.CTensor(to_device(dr), to_device(di)))[0].real
+    assert abs(an - fd) <= 1e-6 * abs(fd) + 1e-10

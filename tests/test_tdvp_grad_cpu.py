@@ -169,3 +169,32 @@ def test_adjoint_matches_the_tangent_and_differences_in_the_state(turning, sweep
     fd = (c_state(h) - c_state(-h)) / (2 * h)
     an = sum(cdots(ops, [g], d)[0].real for g, d in zip(gA, D))
     assert abs(an - fd) <= 1e-6 * abs(fd) + 1e-10
+
+
+@pytest.mark.parametrize("t,krylovdim", [(-0.3j, 30), (-2.0j, 8), (0.7j, 6)])
+def test_exponential_family_equals_single_exponentials(t, krylovdim):
+    """exp(p t F) x for several p from one integration (with restarts where the basis is short)
+    against one ``exponentiate`` per p."""
+    ops = oracle_ops()
+    rng = np.random.default_rng(4)
+    V = U1Space((0, 15), (1, 16), (2, 14))
+    fb = {}
+    for c, n in V.sectors:
+        a = rng.standard_normal((n, n))
+        fb[(c, c)] = 0.1 * (a + a.T)
+    F = st.from_blocks(0, (dual_space(V), V), fb)
+    W = (dual_space(U1Space((0, 1))), V)
+    x = ct.CTensor(rand_tensor(0, W, rng), rand_tensor(0, W, rng))
+    f = lambda v: ct.ccontract(ops, v, (1, -1), F, (-1, 2))
+    fr = [0.0, 0.1, 0.35, 0.5, 0.9, 1.0]
+    ys, info = tg.exponentiate_family(ops, f, t, x, fr, krylovdim=krylovdim, tol=1e-12)
+    assert info.converged
+    steps = 0
+    for p, y in zip(fr, ys):
+        if p == 0.0:
+            want = x
+        else:
+            want, one = ct.exponentiate(ops, f, p * t, x, krylovdim=krylovdim, tol=1e-12)
+            steps = max(steps, one.numsteps)
+        assert np.abs(dense_site(ops, y) - dense_site(ops, want)).max() < 1e-12
+    assert info.numsteps == steps  # the family costs the longest single integration
