@@ -103,6 +103,12 @@ def parse(argv=None):
                         "events, algorithmic and executed TFLOP/s against the measured peak")
     p.add_argument("--tdvp-no-fd", action="store_true",
                    help="--tdvp: skip the finite-difference evolutions")
+    p.add_argument("--tdvp-forward-only", action="store_true",
+                   help="--tdvp: the plain sweeps alone (no derivative runs)")
+    p.add_argument("--tdvp-kernel-times", action="store_true",
+                   help="--tdvp: per-kernel device time of the plain sweeps (CUPTI activity "
+                        "records through torch.profiler), against their wall time; diagnostic, "
+                        "the sweep times of such a run are not reported as measurements")
     p.add_argument("--tdvp-adjoint", action="store_true",
                    help="--tdvp: also the reverse-mode gradient (every MPO tensor and initial "
                         "site tensor) over the same sweeps; its dC/dDelta and time")
@@ -899,12 +905,32 @@ def run_tdvp(args):
         e0 = td.energy(ops, As, Ws, env)
         stats = td.TDVPStats()
         times = []
+        prof = None
+        if timed and args.tdvp_kernel_times:
+            import torch
+            prof = torch.profiler.profile(activities=[torch.profiler.ProfilerActivity.CUDA])
+            prof.__enter__()
         for _ in range(steps):
             ctx.synchronize()
             t0 = time.perf_counter()
             td.tdvp1sitesweep(ops, dt, As, Ws, env, turning="symmetric", stats=stats)
             ctx.synchronize()
             times.append(time.perf_counter() - t0)
+        if prof is not None:
+            prof.__exit__(None, None, None)
+            kern = {}
+            for ev in prof.key_averages():
+                t = float(getattr(ev, "self_device_time_total",
+                                  getattr(ev, "self_cuda_time_total", 0.0)) or 0.0)
+                if t > 0:
+                    kern[ev.key] = (kern.get(ev.key, (0, 0.0))[0] + int(ev.count),
+                                    kern.get(ev.key, (0, 0.0))[1] + t)
+            busy = sum(t for _, t in kern.values()) / 1e6
+            top = sorted(kern.items(), key=lambda kv: -kv[1][1])[:25]
+            print(json.dumps({"kernel_times": {
+                "wall_s": sum(times), "device_busy_s": busy,
+                "top": [{"kernel": k[:120], "launches": c, "s": t / 1e6, "share": t / 1e6 / busy}
+                        for k, (c, t) in top]}}), file=sys.stderr, flush=True)
         c = td.expectation(ops, As, {i: sz, i + 1: sz}).real
         out = {"C": c, "sweep_s": times, "matvecs": stats.matvecs,
                "exponentials": stats.exponentials, "unconverged": stats.unconverged}
@@ -916,6 +942,17 @@ def run_tdvp(args):
     r0 = evolve(delta, True)
     print(json.dumps({"forward_s": sum(r0["sweep_s"]), "C": r0["C"]}), file=sys.stderr,
           flush=True)
+    if args.tdvp_forward_only:
+        print(json.dumps({
+            "metric": "1-site TDVP sweep s (complex U(1) MPS)",
+            "value": float(np.median(r0["sweep_s"])), "unit": "s", "higher_is_better": False,
+            "n_gpus": 1, "data": "synthetic (seeded Philox N(0,1) initial MPS)",
+            "config": {"workload": f"XXZ chain L={lx}, Delta={delta}, binomial bond profile "
+                                   f"~{chi}, {steps} sweeps of dt={dt}, forward only"},
+            "C_t": r0["C"], "sweep_s": r0["sweep_s"], "norm_drift": r0["norm_drift"],
+            "energy_drift": r0["energy_drift"],
+            "matvecs_per_sweep": r0["matvecs"] / steps}), flush=True)
+        return
     # the derivative by tangents through the same sweeps
     from mps_gb300 import tdvp_grad as tg
     mps = gd.mps_from_host(host, ctx)
