@@ -2,11 +2,11 @@
 
 The reference evolves MPS with the time-dependent variational principle (src/tdvp.jl:12-89).
 The quantity here is, e.g., d<Sz_i Sz_j>(t)/dDelta of an XXZ chain after 1-site TDVP. A single
-scalar parameter is a forward-mode (tangent) derivative: every quantity of the sweep in ``mps_gb300.tdvp`` carries
-its derivative with respect to the coupling, propagated through each step by the chain rule,
-so one tangent sweep costs a fixed multiple of a plain sweep and stores nothing beyond the
-current state and environments (no tape, no recomputation). The result is the exact
-derivative of the discrete algorithm's output (up to the Krylov tolerances).
+scalar parameter is a forward-mode (tangent) derivative: every quantity of the sweep in
+``mps_gb300.tdvp`` carries its derivative with respect to the coupling, propagated through each
+step by the chain rule, so one tangent sweep costs a fixed multiple of a plain sweep and stores
+nothing beyond the current state and environments (no tape, no recomputation). The result is
+the exact derivative of the discrete algorithm's output (up to the Krylov tolerances).
 
 Steps and their tangents (``d`` = derivative with respect to the coupling, W the MPO, dW its
 derivative, H_eff built from the environments L, R and W):
@@ -733,7 +733,6 @@ def evolve_with_adjoint(ops: Ops, As, Ws, dt: float, sweeps: int, site_ops: dict
     from .tdvp import initialenv, tdvp1sitesweep
     if turning not in TURNING:
         raise ValueError(f"turning must be one of {TURNING}")
-    lx = len(As)
     # cotangents are kept per tensor object: sites that share one MPO tensor (a uniform chain)
     # get their own copy so that each site's gradient is returned separately
     Ws = [ops.lincomb([(1.0, W)]) for W in Ws]
@@ -745,16 +744,12 @@ def evolve_with_adjoint(ops: Ops, As, Ws, dt: float, sweeps: int, site_ops: dict
     # the observable and its cotangents on the final state
     tp = _Tape(ops)
     final = list(As)
-    num, den, _, _ = _expectation_taped(ops, tp, final, site_ops)
-    num = complex(num)
-    den = complex(den)
+    out_num, out_den, _, _ = _expectation_taped(ops, tp, final, site_ops)
+    num, den = complex(out_num), complex(out_den)
     C = num / den
-    # L = Re(num / den): cotangents conj(dL/dnum), conj(dL/dden)
+    # L = Re(num / den): cotangents conj(dL/dnum), conj(dL/dden) of the recorded scalars
     gnum = np.conj(1.0 / den)
     gden = np.conj(-num / den ** 2)
-    rec = tp.rec
-    # find the scalar outputs (the last two recorded contractions)
-    out_num, out_den = rec[-2][1][0], rec[-1][1][0]
     g = tp.backward([(out_num, gnum), (out_den, gden)])
     cot = [g(A) for A in final]
     gW = [g(W) for W in Ws]
